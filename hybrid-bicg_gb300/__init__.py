@@ -1,0 +1,382 @@
+"""Python binding of the GB300 shifted BiCGStab solver (libhbicg.so).
+
+A thin ctypes layer over the C ABI in include/: the reference's drop-in entry
+points (shifted_lopbicg_{dynamic,static,normal}, src/solver.h:33-35; the
+matrix.h loaders and products) and the extended API (include/hbicg.h).  Host
+arrays are numpy; device arrays are torch CUDA tensors (PyTorch is used only
+for device memory and streams).  There is no CPU path: every call that
+computes goes through the CUDA library, and loading fails loudly when it has
+not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+from . import workloads  # noqa: F401  (re-exported)
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libhbicg.so"
+INCLUDE = HERE.parent / "include"
+
+_PD = C.POINTER(C.c_double)
+_PU = C.POINTER(C.c_uint)
+_PI = C.POINTER(C.c_int)
+
+HOST, DEVICE = 0, 1
+FORMS = {"plain": 0, "fused": 1}
+SHIFT_MODES = {"auto": 0, "incremental": 1, "deferred": 2}
+STATUS = {0: "ok", 1: "not square", 2: "no diagonal", 3: "breakdown", 4: "max_iter", 5: "cuda", 6: "timeout",
+          7: "argument", 8: "out of memory", 9: "io"}
+
+
+class HbicgError(RuntimeError):
+    pass
+
+
+def build(jobs: int | None = None, quiet: bool = True) -> Path:
+    """Compile libhbicg.so for sm_103a (nvcc + gcc, no cmake)."""
+    jobs = jobs or max(2, os.cpu_count() or 2)
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run(["make", "-s", "-j", str(jobs), "-C", str(HERE / "csrc")], check=True, stdout=out)
+    return LIB_PATH
+
+
+# ---------------------------------------------------------------- ctypes types
+class CSR_Matrix(C.Structure):
+    """src/matrix.h:19-26"""
+    _fields_ = [("val", _PD), ("col", _PU), ("ptr", _PU), ("nz", C.c_uint), ("rows", C.c_uint), ("cols", C.c_uint)]
+
+
+class INFO_Matrix(C.Structure):
+    """src/matrix.h:28-33 without MPI types"""
+    _fields_ = [("nz", C.c_uint), ("rows", C.c_uint), ("cols", C.c_uint), ("code", C.c_char * 4),
+                ("recvcounts", _PI), ("displs", _PI)]
+
+
+class Params(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("switching", C.c_int), ("form", C.c_int),
+                ("shift_mode", C.c_int), ("use_graph", C.c_int), ("graph_chunk", C.c_int),
+                ("basis_mem_frac", C.c_double), ("true_residuals", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("k", C.c_int), ("status", C.c_int), ("n_switches", C.c_int), ("final_seed", C.c_int),
+                ("shift_mode", C.c_int), ("basis_flushes", C.c_int), ("launches", C.c_int),
+                ("solve_ms", C.c_double), ("max_true_residual", C.c_double), ("bytes_algorithmic", C.c_double),
+                ("switch_k", _PI), ("switch_seed", _PI), ("conv_k", _PI), ("active_per_iter", _PI),
+                ("true_residual", _PD)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libhbicg.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise HbicgError(f"{LIB_PATH} is not built: call build() (needs nvcc); there is no CPU fallback")
+    L = C.CDLL(str(LIB_PATH))
+    sig = {
+        "hbicg_params_default": (None, [C.POINTER(Params)]),
+        "hbicg_status_string": (C.c_char_p, [C.c_int]),
+        "hbicg_last_message": (C.c_char_p, []),
+        "hbicg_context_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+        "hbicg_context_destroy": (None, [C.c_void_p]),
+        "hbicg_context_stream": (C.c_void_p, [C.c_void_p]),
+        "hbicg_matrix_create": (C.c_int, [C.c_void_p, C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                          C.POINTER(C.c_void_p)]),
+        "hbicg_matrix_destroy": (None, [C.c_void_p]),
+        "hbicg_matrix_spmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
+        "hbicg_solver_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(Params), C.POINTER(C.c_void_p)]),
+        "hbicg_solver_destroy": (None, [C.c_void_p]),
+        "hbicg_solver_run": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                       C.c_int, C.POINTER(Stats)]),
+        "hbicg_solve": (C.c_int, [C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_int, C.c_int, C.POINTER(Params), C.c_void_p, C.c_void_p, C.POINTER(Stats)]),
+        "hbicg_dropin_config": (None, [C.c_double, C.c_int, C.c_int]),
+        "shifted_lopbicg_dynamic": (C.c_int, [C.POINTER(CSR_Matrix), C.POINTER(CSR_Matrix), C.POINTER(INFO_Matrix),
+                                              _PD, _PD, _PD, C.c_int, C.c_int]),
+        "shifted_lopbicg_static": (C.c_int, [C.POINTER(CSR_Matrix), C.POINTER(CSR_Matrix), C.POINTER(INFO_Matrix),
+                                             _PD, _PD, _PD, C.c_int, C.c_int]),
+        "shifted_lopbicg_normal": (C.c_int, [C.POINTER(CSR_Matrix), C.POINTER(CSR_Matrix), C.POINTER(INFO_Matrix),
+                                             _PD, _PD, _PD, C.c_int, C.c_int]),
+        "mult": (None, [C.POINTER(CSR_Matrix), _PD, _PD]),
+        "mm_read_banner": (C.c_int, [C.c_void_p, C.c_void_p]),
+        "mm_read_mtx_crd_size": (C.c_int, [C.c_void_p, _PI, _PI, _PI]),
+        "csr_load_matrix": (C.c_int, [C.c_char_p, C.POINTER(CSR_Matrix)]),
+        "MPI_csr_load_matrix_block": (None, [C.c_char_p, C.POINTER(CSR_Matrix), C.POINTER(CSR_Matrix),
+                                             C.POINTER(INFO_Matrix)]),
+        "csr_free_matrix": (None, [C.POINTER(CSR_Matrix)]),
+        "csr_init_matrix": (None, [C.POINTER(CSR_Matrix)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        L = lib()
+        raise HbicgError(f"{what}: {L.hbicg_status_string(rc).decode()} ({L.hbicg_last_message().decode()})")
+
+
+def _ptr(a) -> int:
+    """Address of a contiguous numpy array or torch tensor."""
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return int(a.data_ptr())
+
+
+def params(tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="auto", use_graph=True,
+           graph_chunk=0, basis_mem_frac=0.0, true_residuals=False) -> Params:
+    p = Params()
+    lib().hbicg_params_default(C.byref(p))
+    p.tol = float(tol)
+    p.max_iter = int(max_iter)
+    p.switching = 1 if switching else 0
+    p.form = FORMS[form]
+    p.shift_mode = SHIFT_MODES[shift_mode]
+    p.use_graph = 1 if use_graph else 0
+    p.graph_chunk = int(graph_chunk)
+    if basis_mem_frac:
+        p.basis_mem_frac = float(basis_mem_frac)
+    p.true_residuals = 1 if true_residuals else 0
+    return p
+
+
+@dataclass
+class SolveResult:
+    k: int
+    x: object
+    r: object
+    status: int
+    switches: list
+    conv_k: np.ndarray
+    active: np.ndarray
+    final_seed: int
+    shift_mode: str
+    solve_ms: float
+    launches: int
+    flushes: int
+    bytes_algorithmic: float
+    true_residual: np.ndarray | None = None
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def max_true_residual(self) -> float:
+        return float(np.max(self.true_residual)) if self.true_residual is not None and len(self.true_residual) else 0.0
+
+
+def _stats(m: int, max_iter: int):
+    st = Stats()
+    bufs = {
+        "switch_k": np.zeros(max(m, 1), dtype=np.int32),
+        "switch_seed": np.zeros(max(m, 1), dtype=np.int32),
+        "conv_k": np.zeros(max(m, 1), dtype=np.int32),
+        "active_per_iter": np.zeros(max_iter + 2, dtype=np.int32),
+        "true_residual": np.zeros(max(m, 1)),
+    }
+    st.switch_k = bufs["switch_k"].ctypes.data_as(_PI)
+    st.switch_seed = bufs["switch_seed"].ctypes.data_as(_PI)
+    st.conv_k = bufs["conv_k"].ctypes.data_as(_PI)
+    st.active_per_iter = bufs["active_per_iter"].ctypes.data_as(_PI)
+    st.true_residual = bufs["true_residual"].ctypes.data_as(_PD)
+    return st, bufs
+
+
+def _result(st: Stats, bufs, m, x, r, want_res) -> SolveResult:
+    nsw = min(st.n_switches, m)
+    sw = [(int(bufs["switch_k"][i]), int(bufs["switch_seed"][i])) for i in range(nsw)]
+    return SolveResult(k=st.k, x=x, r=r, status=st.status, switches=sw, conv_k=bufs["conv_k"][:m].copy(),
+                       active=bufs["active_per_iter"][:st.k + 1].copy(), final_seed=st.final_seed,
+                       shift_mode={1: "incremental", 2: "deferred"}.get(st.shift_mode, "?"), solve_ms=st.solve_ms,
+                       launches=st.launches, flushes=st.basis_flushes, bytes_algorithmic=st.bytes_algorithmic,
+                       true_residual=bufs["true_residual"][:m].copy() if want_res else None)
+
+
+def _csr_arrays(a):
+    return (np.ascontiguousarray(a.ptr, dtype=np.uint32), np.ascontiguousarray(a.col, dtype=np.uint32),
+            np.ascontiguousarray(a.val, dtype=np.float64))
+
+
+def solve(a, b, sigma, seed=0, *, tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="auto",
+          use_graph=True, true_residuals=False, graph_chunk=0, basis_mem_frac=0.0) -> SolveResult:
+    """One-call solve with host (numpy) arrays through hbicg_solve."""
+    L = lib()
+    ptr, col, val = _csr_arrays(a)
+    n, m = int(ptr.shape[0] - 1), len(sigma)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    sig = np.ascontiguousarray(sigma, dtype=np.float64)
+    x = np.zeros((m, n))
+    r = np.zeros(n)
+    p = params(tol, max_iter, switching, form, shift_mode, use_graph, graph_chunk, basis_mem_frac, true_residuals)
+    st, bufs = _stats(m, max_iter)
+    rc = L.hbicg_solve(n, int(ptr[-1]), _ptr(ptr), _ptr(col), _ptr(val), _ptr(bb), _ptr(sig), m, int(seed),
+                       C.byref(p), _ptr(x), _ptr(r), C.byref(st))
+    if rc not in (0, 3, 4):
+        _check(rc, "hbicg_solve")
+    return _result(st, bufs, m, x, r, true_residuals)
+
+
+class Context:
+    def __init__(self):
+        self.h = C.c_void_p()
+        _check(lib().hbicg_context_create(C.byref(self.h)), "hbicg_context_create")
+
+    @property
+    def stream(self) -> int:
+        return int(lib().hbicg_context_stream(self.h) or 0)
+
+    def close(self):
+        if self.h:
+            lib().hbicg_context_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Matrix:
+    """Device CSR + SpMV schedule.  ptr/col/val: numpy (copied) or torch CUDA tensors (used in place)."""
+
+    def __init__(self, ctx: Context, ptr, col, val):
+        self.ctx = ctx
+        self._keep = (ptr, col, val)
+        where = HOST if isinstance(ptr, np.ndarray) else DEVICE
+        if where == HOST:
+            ptr = np.ascontiguousarray(ptr, dtype=np.uint32)
+            col = np.ascontiguousarray(col, dtype=np.uint32)
+            val = np.ascontiguousarray(val, dtype=np.float64)
+            self._keep = (ptr, col, val)
+        self.n = int(ptr.shape[0] - 1)
+        self.nnz = int(col.shape[0])
+        self.h = C.c_void_p()
+        _check(lib().hbicg_matrix_create(ctx.h, self.n, self.nnz, _ptr(ptr), _ptr(col), _ptr(val), where,
+                                         C.byref(self.h)), "hbicg_matrix_create")
+
+    def spmv(self, x, y, sigma: float = 0.0):
+        where = HOST if isinstance(x, np.ndarray) else DEVICE
+        _check(lib().hbicg_matrix_spmv(self.h, _ptr(x), _ptr(y), float(sigma), where), "hbicg_matrix_spmv")
+        return y
+
+    def close(self):
+        if self.h:
+            lib().hbicg_matrix_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    """Reusable workspace for m-shift families on one matrix (graphs are captured once)."""
+
+    def __init__(self, matrix: Matrix, m: int, **kw):
+        self.matrix = matrix
+        self.m = m
+        self.max_iter = kw.get("max_iter", 2000)
+        self.want_res = bool(kw.get("true_residuals", False))
+        self.p = params(**kw)
+        self.h = C.c_void_p()
+        _check(lib().hbicg_solver_create(matrix.ctx.h, matrix.h, m, C.byref(self.p), C.byref(self.h)),
+               "hbicg_solver_create")
+
+    def run(self, b, sigma, seed=0, x=None, r=None) -> SolveResult:
+        """b/sigma: numpy (host) or torch CUDA tensors (device); x [m, n] and r [n]
+        are written in the same kind of memory as given (allocated on the host if None)."""
+        in_where = HOST if isinstance(b, np.ndarray) else DEVICE
+        if in_where == HOST:
+            b = np.ascontiguousarray(b, dtype=np.float64)
+            sigma = np.ascontiguousarray(sigma, dtype=np.float64)
+        if x is None:
+            x = np.zeros((self.m, self.matrix.n))
+        out_where = HOST if isinstance(x, np.ndarray) else DEVICE
+        st, bufs = _stats(self.m, self.max_iter)
+        rc = lib().hbicg_solver_run(self.h, _ptr(b), _ptr(sigma), int(seed), in_where, _ptr(x),
+                                    _ptr(r) if r is not None else None, out_where, C.byref(st))
+        if rc not in (0, 3, 4):
+            _check(rc, "hbicg_solver_run")
+        return _result(st, bufs, self.m, x, r, self.want_res)
+
+    def close(self):
+        if self.h:
+            lib().hbicg_solver_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------- reference entry points
+def dropin_solve(variant: str, a, b, sigma, seed=0, tol=1e-12, max_iter=2000, switching=True):
+    """Call shifted_lopbicg_<variant> exactly as the reference's drivers do
+    (src/main.c:114-151): x zero, r_loc = b (overwritten), returns (k, x, r)."""
+    L = lib()
+    ptr, col, val = _csr_arrays(a)
+    n, m = int(ptr.shape[0] - 1), len(sigma)
+    diag = CSR_Matrix(val.ctypes.data_as(_PD), col.ctypes.data_as(_PU), ptr.ctypes.data_as(_PU), int(ptr[-1]), n, n)
+    optr = np.zeros(n + 1, dtype=np.uint32)
+    offd = CSR_Matrix(None, None, optr.ctypes.data_as(_PU), 0, n, n)
+    recv = (C.c_int * 1)(n)
+    displ = (C.c_int * 1)(0)
+    info = INFO_Matrix(int(ptr[-1]), n, n, b"MCRG", C.cast(recv, _PI), C.cast(displ, _PI))
+    x = np.zeros((m, n))
+    r = np.ascontiguousarray(b, dtype=np.float64).copy()
+    sig = np.ascontiguousarray(sigma, dtype=np.float64)
+    L.hbicg_dropin_config(float(tol), int(max_iter), 1 if switching else 0)
+    fn = getattr(L, f"shifted_lopbicg_{variant}")
+    k = fn(C.byref(diag), C.byref(offd), C.byref(info), x.ctypes.data_as(_PD), r.ctypes.data_as(_PD),
+           sig.ctypes.data_as(_PD), m, int(seed))
+    L.hbicg_dropin_config(1e-12, 2000, 1)
+    return k, x, r
+
+
+def mult(a, x, y=None) -> np.ndarray:
+    """The reference's mult (y += A x) through the C ABI, on the GPU."""
+    L = lib()
+    ptr, col, val = _csr_arrays(a)
+    n = int(ptr.shape[0] - 1)
+    A = CSR_Matrix(val.ctypes.data_as(_PD), col.ctypes.data_as(_PU), ptr.ctypes.data_as(_PU), int(ptr[-1]), n, n)
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    yy = np.zeros(n) if y is None else np.ascontiguousarray(y, dtype=np.float64)
+    L.mult(C.byref(A), xx.ctypes.data_as(_PD), yy.ctypes.data_as(_PD))
+    return yy
+
+
+def load_matrix_market(path: str):
+    """MPI_csr_load_matrix_block on one rank -> (Csr of the whole matrix, typecode)."""
+    L = lib()
+    d, o = CSR_Matrix(), CSR_Matrix()
+    recv = (C.c_int * 1)(0)
+    displ = (C.c_int * 1)(0)
+    info = INFO_Matrix(0, 0, 0, b"    ", C.cast(recv, _PI), C.cast(displ, _PI))
+    L.MPI_csr_load_matrix_block(str(path).encode(), C.byref(d), C.byref(o), C.byref(info))
+    n, nz = d.rows, d.nz
+    ptr = np.ctypeslib.as_array(d.ptr, shape=(n + 1,)).copy()
+    col = np.ctypeslib.as_array(d.col, shape=(nz,)).copy() if nz else np.zeros(0, np.uint32)
+    val = np.ctypeslib.as_array(d.val, shape=(nz,)).copy() if nz else np.zeros(0)
+    code = bytes(info.code).decode()
+    onz = o.nz
+    L.csr_free_matrix(C.byref(d))
+    L.csr_free_matrix(C.byref(o))
+    return workloads.Csr(ptr, col, val), code, int(onz)

@@ -1,0 +1,146 @@
+/* Thin C ABI between the C host code (solver driver, loaders) and the sm_103a
+ * CUDA kernels of the shifted BiCGStab solver.  Everything here is plain C:
+ * device pointers, sizes and a stream.  The structs describe how the solver
+ * lays its data out in HBM:
+ *   - the matrix: CSR with 32-bit row pointers and column indices and FP64
+ *     values, plus the SpMV schedule (row blocks) built once per matrix;
+ *   - per-shift vectors x_j, p_j: shift-major [m][n] FP64 arrays;
+ *   - the Krylov basis (deferred mode): slots of n doubles, [L][n];
+ *   - the scalar state of the iteration (seed scalars, per-shift recurrences,
+ *     the alpha/beta/omega history and the pi archive), all device-resident so
+ *     that a whole iteration runs without a host round trip.
+ */
+#ifndef HBK_H
+#define HBK_H
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HBK_THREADS 256      /* threads per block of every streaming kernel */
+#define HBK_MAX_GRID 4096    /* upper bound on persistent grids (partial-sum slots) */
+#define HBK_TILE_NNZ 2048    /* nonzeros staged in shared memory per SpMV row block */
+#define HBK_NCOEF 8          /* coefficients per shift per iteration */
+
+/* status bits (device and host) */
+#define HBK_ST_BREAKDOWN 1   /* a scalar of the recurrence became 0, inf or nan */
+#define HBK_ST_BASIS_FULL 2  /* deferred mode: the basis needs a flush */
+
+/* SpMV row-block kinds (bits 30..31 of blk_row entries are not used; kinds
+ * are a separate byte array) */
+#define HBK_BLK_TILE 0       /* up to HBK_THREADS short rows, <= HBK_TILE_NNZ nonzeros */
+#define HBK_BLK_LONG 1       /* one long row, reduced by the whole block */
+
+typedef struct {
+    unsigned n, nnz;
+    const unsigned *ptr, *col; /* device CSR, n+1 and nnz entries */
+    const double *val;
+    const unsigned *blk_row;   /* device: first row of each row block, nblk+1 entries */
+    const unsigned char *blk_kind;
+    unsigned nblk;
+    int grid;                  /* persistent grid of the SpMV kernels */
+} hbk_matrix;
+
+/* Device-resident scalars of one solve. */
+typedef struct {
+    double rr_hat;      /* (r^, r) */
+    double rr_hat_old;
+    double rr;          /* (r, r) at the end of the current iteration */
+    double bb;          /* (b, b) */
+    double rs, qq, qy;  /* raw reductions of the current iteration */
+    double alpha, omega, beta;
+    double r_scale;     /* 1 / (zeta_t pi_t) when the iteration ends with a switch */
+    double tol;
+    int k;              /* current iteration, 1-based */
+    int seed;           /* seed of the current iteration */
+    int next_seed;
+    int n_done;         /* converged systems */
+    int finished;       /* set once n_done == m or k == kcap */
+    int switched;       /* this iteration ends with a seed switch */
+    int n_active;       /* entries in act_list for the shift update */
+    int status;         /* HBK_ST_* */
+    int n_sw;           /* seed switches so far */
+    int max_sigma;      /* the argmax of the last convergence test */
+    int m, kcap;        /* shifts, history length (max_iter + 1) */
+    int switching;      /* 1 = seed switching on */
+    int slots;          /* deferred mode: basis slots in use */
+    int slot_r_old;     /* deferred mode: slot of r_{k-1} */
+    int slot_cap;
+    int need_ps;        /* deferred mode: the new seed's p must be formed from the basis */
+    double rs_switch;   /* (r^, r_k) after the switch rescale */
+} hbk_scalars;
+
+typedef struct {
+    hbk_scalars *sc;
+    const double *sigma;        /* [m] */
+    double *a_hist, *b_hist, *w_hist; /* [kcap] seed alpha / beta / omega history */
+    double *pi;                 /* [m][kcap] */
+    double *eta, *zeta;         /* [m] */
+    int *done, *conv_k;         /* [m] */
+    int *act_list;              /* [m] shifts updated this iteration */
+    double *coef;               /* [m][HBK_NCOEF] their coefficients */
+    int *sw_k, *sw_seed;        /* [m] switch log */
+    int *act_hist;              /* [kcap] active non-seed shifts per iteration */
+    double *partials;           /* [4][HBK_MAX_GRID] */
+    unsigned *counters;         /* [8] last-block tickets */
+    double *ratio;              /* [kcap] scratch for the switch replay */
+    int *lslot;                 /* [m] deferred mode: basis slots in use at a system's last update */
+    int m, kcap;
+} hbk_shifts;
+
+typedef struct {
+    unsigned n;
+    double *r_hat;              /* shadow residual = b */
+    double *rbuf[2];            /* r_{k-1} / r_k, alternating with k */
+    double *s, *q, *y;
+    double *X, *P;              /* [m][n] shift-major (P unused in deferred mode) */
+    /* deferred (Krylov basis) mode */
+    double *V;                  /* [slot_cap][n] */
+    double *ps;                 /* the seed's search vector */
+    double *Xc, *Pc;            /* [m][slot_cap] coefficients */
+    double *own;                /* [m][2]: coefficient of the flushed p_j in x_j and in p_j */
+    double *Pmat;               /* [m][n] flushed p_j (allocated on the first flush) */
+    int slot_cap;
+    int deferred;
+} hbk_vectors;
+
+/* ---- plain BLAS-1 and SpMV kernels (one launch per reference step) ---- */
+int hbk_copy(unsigned n, const double *x, double *y, cudaStream_t st);
+int hbk_zero(unsigned n, double *x, cudaStream_t st);
+int hbk_axpy(unsigned n, double a, const double *x, double *y, cudaStream_t st);
+int hbk_scal(unsigned n, double a, double *x, cudaStream_t st);
+int hbk_fill(unsigned n, double v, double *x, cudaStream_t st);
+/* deterministic dot: result written to *out (device), fixed summation tree */
+int hbk_dot(unsigned n, const double *x, const double *y, double *partials, unsigned *counter, double *out,
+            cudaStream_t st);
+/* y = A x (+ sigma * x when sigma_add != 0), rows summed in stored order by one thread */
+int hbk_spmv(const hbk_matrix *A, const double *x, double *y, double sigma, int sigma_add, cudaStream_t st);
+/* y += A x (the reference's mult accumulates into y) */
+int hbk_spmv_accumulate(const hbk_matrix *A, const double *x, double *y, cudaStream_t st);
+
+/* ---- SpMV schedule ---- */
+/* Host: split rows into blocks (counts only when blk_row is NULL). */
+unsigned hbk_plan_rows(unsigned n, const unsigned *ptr_host, unsigned *blk_row, unsigned char *blk_kind);
+int hbk_spmv_grid(unsigned nblk);
+
+/* ---- fused solver ---- */
+int hbk_fused_init(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, const double *b, int seed,
+                   double tol, cudaStream_t st);
+int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, cudaStream_t st);
+/* deferred mode: x_j (and p_j when keep_p) = coefficients x basis, then reset the basis */
+int hbk_deferred_flush(const hbk_vectors *v, const hbk_shifts *sh, int keep_p, cudaStream_t st);
+/* ||b - (A + sigma_j I) x_j||^2 for every shift into out[m] (device) */
+int hbk_true_residuals(const hbk_matrix *A, const double *X, const double *b, const double *sigma, int m,
+                       double *partials, unsigned *counter, double *out, cudaStream_t st);
+
+int hbk_last_error(void);
+const char *hbk_error_string(int code);
+int hbk_device_sm_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,139 @@
+// Device helpers shared by the solver's kernels: deterministic block
+// reductions, the last-block ticket, and the row-block CSR SpMV core.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hbk.h"
+
+namespace hbk {
+
+constexpr int NT = HBK_THREADS;
+constexpr int NW = NT / 32;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over the block with a fixed tree (same order on every run); every
+// thread gets the total.  `sh` needs NW doubles.
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double t = (l < NW) ? sh[l] : 0.0;
+    return warp_sum(t);
+}
+
+__device__ __forceinline__ double2 block_sum2(double2 v, double *sh) {
+    v.x = warp_sum(v.x);
+    v.y = warp_sum(v.y);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) {
+        sh[w] = v.x;
+        sh[NW + w] = v.y;
+    }
+    __syncthreads();
+    double2 t;
+    t.x = warp_sum((l < NW) ? sh[l] : 0.0);
+    t.y = warp_sum((l < NW) ? sh[NW + l] : 0.0);
+    return t;
+}
+
+// Writes this block's partial(s) and takes a ticket; returns true in every
+// thread of the block that arrives last.  That block then sums the partials
+// in block-index order (fixed tree), so results do not depend on timing.
+__device__ __forceinline__ bool take_ticket(unsigned *counter) {
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last != 0;
+}
+
+// Called by the last block: sums partials[0..nparts) in a fixed order.
+__device__ __forceinline__ double sum_partials(const double *partials, int nparts, double *sh) {
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += NT) acc += __ldcg(partials + i);
+    return block_sum(acc, sh);
+}
+
+__device__ __forceinline__ bool fin(double v) { return isfinite(v) != 0; }
+
+// ---------------------------------------------------------------------------
+// Row-block CSR SpMV core.
+//
+// Rows are cut on the host into blocks (hbk_plan_rows): a TILE block holds up
+// to NT consecutive short rows with at most HBK_TILE_NNZ nonzeros in total; a
+// LONG block holds one row.  A persistent grid walks the blocks in order.  For
+// a TILE block the CTA stages the block's values and the gathered x values in
+// shared memory with coalesced loads, then each thread sums one row in stored
+// order with FMAs (the same order as the reference's row loop,
+// src/openmp_matrix.c:47-58).  A LONG row is summed by the whole CTA with a
+// fixed tree.  `epi(row, acc)` finishes each row; it runs once per row.
+// ---------------------------------------------------------------------------
+struct SpmvSmem {
+    double val[HBK_TILE_NNZ];
+    double xv[HBK_TILE_NNZ];
+    double red[2 * NW];
+};
+
+template <class Epi>
+__device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__restrict__ x, Epi &epi,
+                                          SpmvSmem &sm) {
+    const unsigned *__restrict__ ptr = A.ptr;
+    const unsigned *__restrict__ col = A.col;
+    const double *__restrict__ val = A.val;
+    for (unsigned b = blockIdx.x; b < A.nblk; b += gridDim.x) {
+        const unsigned r0 = __ldg(A.blk_row + b), r1 = __ldg(A.blk_row + b + 1);
+        const unsigned e0 = __ldg(ptr + r0), e1 = __ldg(ptr + r1);
+        if (__ldg(A.blk_kind + b) == HBK_BLK_LONG) {
+            double acc = 0.0;
+            for (unsigned e = e0 + threadIdx.x; e < e1; e += NT) acc = fma(__ldg(val + e), __ldg(x + __ldg(col + e)), acc);
+            acc = block_sum(acc, sm.red);
+            if (threadIdx.x == 0) epi(r0, acc);
+            __syncthreads();
+            continue;
+        }
+        const unsigned cnt = e1 - e0;
+        for (unsigned e = threadIdx.x; e < cnt; e += NT) {
+            const unsigned c = __ldg(col + e0 + e);
+            sm.val[e] = __ldg(val + e0 + e);
+            sm.xv[e] = __ldg(x + c);
+        }
+        __syncthreads();
+        const unsigned r = r0 + threadIdx.x;
+        if (r < r1) {
+            const unsigned a = __ldg(ptr + r) - e0, z = __ldg(ptr + r + 1) - e0;
+            double acc = 0.0;
+            for (unsigned e = a; e < z; ++e) acc = fma(sm.val[e], sm.xv[e], acc);
+            epi(r, acc);
+        }
+        __syncthreads();
+    }
+}
+
+inline int grid_for(unsigned n, int per_thread) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    long need = ((long)n + (long)NT * per_thread - 1) / ((long)NT * per_thread);
+    long cap = (long)sms * 8;
+    if (cap > HBK_MAX_GRID) cap = HBK_MAX_GRID;
+    if (need < 1) need = 1;
+    return (int)(need < cap ? need : cap);
+}
+
+}  // namespace hbk

@@ -1,0 +1,212 @@
+// Plain per-step kernels (one launch per step of the reference's iteration)
+// and the CSR SpMV entry points.  The plain solver form drives these from the
+// host exactly in the reference's order (src/solver_dynamic.c:156-256).
+#include <stdio.h>
+
+#include "hbk_device.cuh"
+
+using namespace hbk;
+
+namespace {
+
+__global__ void __launch_bounds__(NT) k_copy(unsigned n, const double *__restrict__ x, double *__restrict__ y) {
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) y[i] = x[i];
+}
+
+__global__ void __launch_bounds__(NT) k_fill(unsigned n, double v, double *__restrict__ x) {
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) x[i] = v;
+}
+
+// y[i] += a * x[i]   (my_openmp_daxpy, src/openmp_vector.c:3-9)
+__global__ void __launch_bounds__(NT) k_axpy(unsigned n, double a, const double *__restrict__ x,
+                                             double *__restrict__ y) {
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) y[i] = fma(a, x[i], y[i]);
+}
+
+__global__ void __launch_bounds__(NT) k_scal(unsigned n, double a, double *__restrict__ x) {
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) x[i] *= a;
+}
+
+__global__ void __launch_bounds__(NT) k_dot(unsigned n, const double *__restrict__ x, const double *__restrict__ y,
+                                            double *partials, unsigned *counter, double *out) {
+    __shared__ double sh[NW];
+    double acc = 0.0;
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) acc = fma(x[i], y[i], acc);
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+    if (take_ticket(counter)) {
+        double t = sum_partials(partials, gridDim.x, sh);
+        if (threadIdx.x == 0) {
+            *out = t;
+            *counter = 0;
+        }
+    }
+}
+
+struct EpiStore {
+    double *y;
+    const double *x;
+    double sigma;
+    int add;
+    __device__ void operator()(unsigned r, double acc) const { y[r] = add ? fma(sigma, x[r], acc) : acc; }
+};
+
+struct EpiAccum {
+    double *y;
+    __device__ void operator()(unsigned r, double acc) const { y[r] += acc; }
+};
+
+__global__ void __launch_bounds__(NT) k_spmv(hbk_matrix A, const double *__restrict__ x, double *__restrict__ y,
+                                             double sigma, int add) {
+    __shared__ SpmvSmem sm;
+    EpiStore epi{y, x, sigma, add};
+    spmv_rows(A, x, epi, sm);
+}
+
+__global__ void __launch_bounds__(NT) k_spmv_acc(hbk_matrix A, const double *__restrict__ x, double *__restrict__ y) {
+    __shared__ SpmvSmem sm;
+    EpiAccum epi{y};
+    spmv_rows(A, x, epi, sm);
+}
+
+// out[j] = ||b - (A + sigma_j I) x_j||^2 ; one launch per shift block (grid.y = shift)
+__global__ void __launch_bounds__(NT) k_true_res(hbk_matrix A, const double *__restrict__ X, size_t ld,
+                                                 const double *__restrict__ b, const double *__restrict__ sigma,
+                                                 double *partials, unsigned *counters, double *out) {
+    __shared__ SpmvSmem sm;
+    __shared__ double sh[NW];
+    const int j = blockIdx.y;
+    const double *xj = X + (size_t)j * ld;
+    const double sg = sigma[j];
+    double acc = 0.0;
+    auto epi = [&](unsigned r, double ax) {
+        const double res = b[r] - fma(sg, xj[r], ax);
+        acc = fma(res, res, acc);
+    };
+    spmv_rows(A, xj, epi, sm);
+    acc = block_sum(acc, sh);
+    double *pj = partials + (size_t)j * gridDim.x;
+    if (threadIdx.x == 0) pj[blockIdx.x] = acc;
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(counters + j, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        double t = sum_partials(pj, gridDim.x, sh);
+        if (threadIdx.x == 0) {
+            out[j] = t;
+            counters[j] = 0;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int hbk_last_error(void) { return (int)cudaGetLastError(); }
+const char *hbk_error_string(int code) { return cudaGetErrorString((cudaError_t)code); }
+
+int hbk_device_sm_count(void) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+int hbk_copy(unsigned n, const double *x, double *y, cudaStream_t st) {
+    if (!n) return 0;
+    k_copy<<<grid_for(n, 4), NT, 0, st>>>(n, x, y);
+    return (int)cudaGetLastError();
+}
+
+int hbk_fill(unsigned n, double v, double *x, cudaStream_t st) {
+    if (!n) return 0;
+    k_fill<<<grid_for(n, 4), NT, 0, st>>>(n, v, x);
+    return (int)cudaGetLastError();
+}
+
+int hbk_zero(unsigned n, double *x, cudaStream_t st) { return hbk_fill(n, 0.0, x, st); }
+
+int hbk_axpy(unsigned n, double a, const double *x, double *y, cudaStream_t st) {
+    if (!n) return 0;
+    k_axpy<<<grid_for(n, 4), NT, 0, st>>>(n, a, x, y);
+    return (int)cudaGetLastError();
+}
+
+int hbk_scal(unsigned n, double a, double *x, cudaStream_t st) {
+    if (!n) return 0;
+    k_scal<<<grid_for(n, 4), NT, 0, st>>>(n, a, x);
+    return (int)cudaGetLastError();
+}
+
+int hbk_dot(unsigned n, const double *x, const double *y, double *partials, unsigned *counter, double *out,
+            cudaStream_t st) {
+    k_dot<<<grid_for(n, 4), NT, 0, st>>>(n, x, y, partials, counter, out);
+    return (int)cudaGetLastError();
+}
+
+int hbk_spmv_grid(unsigned nblk) {
+    int g = grid_for(nblk * (unsigned)NT, 1);
+    return g < 1 ? 1 : g;
+}
+
+int hbk_spmv(const hbk_matrix *A, const double *x, double *y, double sigma, int sigma_add, cudaStream_t st) {
+    if (!A->n) return 0;
+    k_spmv<<<A->grid, NT, 0, st>>>(*A, x, y, sigma, sigma_add);
+    return (int)cudaGetLastError();
+}
+
+int hbk_spmv_accumulate(const hbk_matrix *A, const double *x, double *y, cudaStream_t st) {
+    if (!A->n) return 0;
+    k_spmv_acc<<<A->grid, NT, 0, st>>>(*A, x, y);
+    return (int)cudaGetLastError();
+}
+
+int hbk_true_residuals(const hbk_matrix *A, const double *X, const double *b, const double *sigma, int m,
+                       double *partials, unsigned *counters, double *out, cudaStream_t st) {
+    if (!A->n || m <= 0) return 0;
+    size_t ld = ((size_t)A->n + 31) / 32 * 32;
+    dim3 grid(A->grid, m);
+    k_true_res<<<grid, NT, 0, st>>>(*A, X, ld, b, sigma, partials, counters, out);
+    return (int)cudaGetLastError();
+}
+
+// Row blocks: consecutive short rows are packed while the block stays within
+// NT rows and HBK_TILE_NNZ nonzeros; a row longer than HBK_TILE_NNZ / 8 gets a
+// block of its own and is reduced by the whole CTA.
+unsigned hbk_plan_rows(unsigned n, const unsigned *ptr, unsigned *blk_row, unsigned char *blk_kind) {
+    const unsigned long_row = HBK_TILE_NNZ / 8;
+    unsigned nb = 0, i = 0;
+    while (i < n) {
+        const unsigned len = ptr[i + 1] - ptr[i];
+        if (len > long_row) {
+            if (blk_row) {
+                blk_row[nb] = i;
+                blk_kind[nb] = HBK_BLK_LONG;
+            }
+            nb++;
+            i++;
+            continue;
+        }
+        unsigned j = i, nz = 0;
+        while (j < n && j - i < (unsigned)NT) {
+            const unsigned l = ptr[j + 1] - ptr[j];
+            if (l > long_row || nz + l > HBK_TILE_NNZ) break;
+            nz += l;
+            j++;
+        }
+        if (blk_row) {
+            blk_row[nb] = i;
+            blk_kind[nb] = HBK_BLK_TILE;
+        }
+        nb++;
+        i = j;
+    }
+    if (blk_row) blk_row[nb] = n;
+    return nb;
+}
+
+}  // extern "C"

@@ -1,0 +1,798 @@
+// Fused shifted BiCGStab iteration with on-device scalars and seed switching.
+//
+// One iteration is five launches (seven in deferred mode), each reading the
+// device-resident scalars, so an iteration (or a CUDA graph of many) needs no
+// host round trip:
+//   K1 seed_s     s = (A + sigma_s I) p_s, (r^,s) fused        -> alpha
+//   K2 seed_q     q = r_{k-1} - alpha s
+//   K3 seed_y     y = (A + sigma_s I) q, (q,q), (q,y) fused     -> omega
+//   K4 seed_upd   x_s += alpha p_s + omega q ; r_k = q - omega y ; (r,r), (r^,r)
+//                 last block: beta, every shift's recurrence and coefficients,
+//                 the convergence test, argmax and the seed switch
+//   K5 shifts     p_s and every unconverged shift's x_j, p_j in one pass
+//                 (incremental mode); r_k rescaled on a switch
+//   K6/K7         deferred mode only: coefficient update of every system in
+//                 the Krylov basis; materialise the new seed's p after a switch
+// Reference: src/solver_dynamic.c:147-381 (seed step :156-210, shift loop
+// :239-256, convergence test :278-303, seed switch :312-359).
+#include "hbk_device.cuh"
+
+using namespace hbk;
+
+namespace {
+
+// Scalar arithmetic of the recurrences is written with explicit round-to-nearest
+// operations so no multiply-add is contracted: the recurrences then round
+// exactly as the reference's C does for the same inputs.
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+
+struct Ctx {
+    hbk_matrix A;
+    hbk_vectors v;
+    hbk_shifts sh;
+};
+
+__device__ __forceinline__ size_t ldn(unsigned n) { return ((size_t)n + 31) / 32 * 32; }
+
+__device__ __forceinline__ const double *seed_p(const Ctx &c, int seed) {
+    return c.v.deferred ? c.v.ps : c.v.P + (size_t)seed * ldn(c.v.n);
+}
+__device__ __forceinline__ double *vec_r_old(const Ctx &c, const hbk_scalars *sc) {
+    return c.v.deferred ? c.v.V + (size_t)sc->slot_r_old * ldn(c.v.n) : c.v.rbuf[(sc->k - 1) & 1];
+}
+__device__ __forceinline__ double *vec_r_new(const Ctx &c, const hbk_scalars *sc) {
+    return c.v.deferred ? c.v.V + (size_t)(sc->slots + 1) * ldn(c.v.n) : c.v.rbuf[sc->k & 1];
+}
+__device__ __forceinline__ double *vec_q(const Ctx &c, const hbk_scalars *sc) {
+    return c.v.deferred ? c.v.V + (size_t)sc->slots * ldn(c.v.n) : c.v.q;
+}
+
+__device__ __forceinline__ bool stopped(const hbk_scalars *sc) { return sc->finished != 0; }
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(NT) k_init(Ctx c, int seed, double tol) {
+    hbk_scalars *sc = c.sh.sc;
+    const int m = c.sh.m, kcap = c.sh.kcap;
+    for (int j = threadIdx.x; j < m; j += NT) {
+        double *pij = c.sh.pi + (size_t)j * kcap;
+        pij[0] = 1.0;
+        if (kcap > 1) pij[1] = 1.0;
+        c.sh.eta[j] = 0.0;
+        c.sh.zeta[j] = 1.0;
+        c.sh.done[j] = 0;
+        c.sh.conv_k[j] = 0;
+    }
+    for (int i = threadIdx.x; i < 8; i += NT) c.sh.counters[i] = 0;
+    if (threadIdx.x == 0) {
+        c.sh.a_hist[0] = 1.0;
+        c.sh.b_hist[0] = 0.0;
+        c.sh.w_hist[0] = 0.0;
+        const double bb = sc->bb;  // written by the (b,b) reduction launched just before
+        sc->rr_hat = bb;
+        sc->rr_hat_old = bb;
+        sc->rr = bb;
+        sc->alpha = sc->omega = sc->beta = 0.0;
+        sc->r_scale = 1.0;
+        sc->tol = tol;
+        sc->k = 1;
+        sc->seed = seed;
+        sc->next_seed = seed;
+        sc->n_done = 0;
+        sc->switched = 0;
+        sc->n_active = 0;
+        sc->status = 0;
+        sc->n_sw = 0;
+        sc->max_sigma = seed;
+        sc->m = m;
+        sc->kcap = kcap;
+        sc->slots = 1;
+        sc->slot_r_old = 0;
+        sc->slot_cap = c.v.slot_cap;
+        sc->need_ps = 0;
+        sc->finished = (m <= 0 || kcap <= 1) ? 1 : 0;
+        if (bb == 0.0) {  // b = 0: x = 0 solves every system exactly
+            sc->finished = 1;
+            sc->n_done = m;
+        }
+    }
+}
+
+// deferred mode: X = 0, Xc = 0, Pc[j][0] = 1 (p_j = b = basis slot 0), own = (0, 0)
+__global__ void __launch_bounds__(NT) k_init_coef(Ctx c) {
+    const int m = c.sh.m, cap = c.v.slot_cap;
+    const size_t tot = (size_t)m * cap;
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < tot; i += (size_t)gridDim.x * NT) {
+        c.v.Xc[i] = 0.0;
+        c.v.Pc[i] = (i % cap == 0) ? 1.0 : 0.0;
+    }
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < (size_t)m; i += (size_t)gridDim.x * NT) {
+        c.v.own[2 * i] = 0.0;
+        c.v.own[2 * i + 1] = 0.0;
+        c.sh.lslot[i] = 1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K1: s = (A + sigma_s I) p_s and (r^, s)
+__global__ void __launch_bounds__(NT) k_seed_s(Ctx c) {
+    __shared__ SpmvSmem sm;
+    hbk_scalars *sc = c.sh.sc;
+    if (stopped(sc)) return;
+    const int seed = sc->seed;
+    const double sig = c.sh.sigma[seed];
+    const double *__restrict__ ps = seed_p(c, seed);
+    const double *__restrict__ rh = c.v.r_hat;
+    double *__restrict__ s = c.v.s;
+    double acc = 0.0;
+    auto epi = [&](unsigned r, double ax) {
+        const double sv = fma(sig, ps[r], ax);
+        s[r] = sv;
+        acc = fma(rh[r], sv, acc);
+    };
+    spmv_rows(c.A, ps, epi, sm);
+    acc = block_sum(acc, sm.red);
+    if (threadIdx.x == 0) c.sh.partials[blockIdx.x] = acc;
+    if (take_ticket(c.sh.counters + 0)) {
+        const double rs = sum_partials(c.sh.partials, gridDim.x, sm.red);
+        if (threadIdx.x == 0) {
+            const int k = sc->k;
+            const double a = dvd(sc->rr_hat, rs);
+            sc->rs = rs;
+            c.sh.a_hist[k] = a;
+            sc->alpha = a;
+            if (!fin(a)) {
+                sc->status |= HBK_ST_BREAKDOWN;
+                sc->finished = 1;
+            }
+            c.sh.counters[0] = 0;
+        }
+    }
+}
+
+// K2: q = r_{k-1} - alpha s
+__global__ void __launch_bounds__(NT) k_seed_q(Ctx c) {
+    const hbk_scalars *sc = c.sh.sc;
+    if (stopped(sc)) return;
+    const double a = sc->alpha;
+    const double *__restrict__ ro = vec_r_old(c, sc);
+    const double *__restrict__ s = c.v.s;
+    double *__restrict__ q = vec_q(c, sc);
+    const unsigned n = c.v.n;
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) q[i] = fma(-a, s[i], ro[i]);
+}
+
+// K3: y = (A + sigma_s I) q, (q,q) and (q,y)
+__global__ void __launch_bounds__(NT) k_seed_y(Ctx c) {
+    __shared__ SpmvSmem sm;
+    hbk_scalars *sc = c.sh.sc;
+    if (stopped(sc)) return;
+    const double sig = c.sh.sigma[sc->seed];
+    const double *__restrict__ q = vec_q(c, sc);
+    double *__restrict__ y = c.v.y;
+    double2 acc = make_double2(0.0, 0.0);
+    auto epi = [&](unsigned r, double ax) {
+        const double qr = q[r];
+        const double yv = fma(sig, qr, ax);
+        y[r] = yv;
+        acc.x = fma(qr, qr, acc.x);
+        acc.y = fma(qr, yv, acc.y);
+    };
+    spmv_rows(c.A, q, epi, sm);
+    acc = block_sum2(acc, sm.red);
+    if (threadIdx.x == 0) {
+        c.sh.partials[blockIdx.x] = acc.x;
+        c.sh.partials[HBK_MAX_GRID + blockIdx.x] = acc.y;
+    }
+    if (take_ticket(c.sh.counters + 1)) {
+        const double qq = sum_partials(c.sh.partials, gridDim.x, sm.red);
+        const double qy = sum_partials(c.sh.partials + HBK_MAX_GRID, gridDim.x, sm.red);
+        if (threadIdx.x == 0) {
+            const int k = sc->k;
+            const double w = dvd(qq, qy);
+            sc->qq = qq;
+            sc->qy = qy;
+            c.sh.w_hist[k] = w;
+            sc->omega = w;
+            sc->rr_hat_old = sc->rr_hat;
+            if (!fin(w) || w == 0.0) {
+                sc->status |= HBK_ST_BREAKDOWN;
+                sc->finished = 1;
+            }
+            c.sh.counters[1] = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// End of the seed step, run by the last block of K4: beta, the shift
+// recurrences (src/solver_dynamic.c:243-253), the convergence test
+// (:278-303) and the seed switch (:312-359).
+__device__ void seed_step_scalars(const Ctx &c, double rr, double rrh) {
+    __shared__ double s_bk;
+    __shared__ int s_ok, s_sw, s_t, s_nconv;
+    __shared__ double s_best[NW];
+    __shared__ int s_bidx[NW];
+    hbk_scalars *sc = c.sh.sc;
+    const hbk_shifts &S = c.sh;
+    const int k = sc->k, seed = sc->seed, m = S.m, kcap = S.kcap;
+    const int deferred = c.v.deferred;
+    if (threadIdx.x == 0) {
+        sc->rr = rr;
+        const double bk = mul(dvd(S.a_hist[k], S.w_hist[k]), dvd(rrh, sc->rr_hat_old));
+        S.b_hist[k] = bk;
+        sc->beta = bk;
+        sc->rr_hat = rrh;
+        s_bk = bk;
+        s_ok = fin(bk);
+        if (!s_ok) {
+            sc->status |= HBK_ST_BREAKDOWN;
+            sc->finished = 1;
+        }
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    const double ak = S.a_hist[k], wk = S.w_hist[k], bk = s_bk;
+    const double c_prev = mul(dvd(S.b_hist[k - 1], S.a_hist[k - 1]), ak);
+    const double sig_s = S.sigma[seed];
+
+    // (1) per-shift recurrences and this iteration's vector coefficients
+    for (int j = threadIdx.x; j < m; j += NT) {
+        double *co = S.coef + (size_t)j * HBK_NCOEF;
+        if (j == seed) {
+            // the seed as a system of its own (deferred mode): pi = zeta = 1, shift 0
+            co[0] = wk;
+            co[1] = ak;
+            co[2] = dvd(wk, ak);
+            co[3] = -dvd(wk, ak);
+            co[4] = bk;
+            co[5] = 1.0;
+            continue;
+        }
+        if (S.done[j]) continue;
+        double *pij = S.pi + (size_t)j * kcap;
+        const double d = sub(sig_s, S.sigma[j]);
+        const double pik1 = pij[k - 1];
+        const double eta = sub(mul(c_prev, S.eta[j]), mul(mul(d, ak), pik1));
+        const double pik = add(eta, pik1);
+        pij[k] = pik;
+        S.eta[j] = eta;
+        const double aj = mul(dvd(pik1, pik), ak);
+        const double wj = dvd(wk, sub(1.0, mul(wk, d)));
+        const double z = S.zeta[j];
+        co[0] = dvd(wj, mul(pik, z));
+        co[1] = aj;
+        co[2] = dvd(wj, mul(mul(aj, z), pik));
+        co[3] = dvd(-wj, mul(mul(aj, z), pik1));
+        const double zn = mul(sub(1.0, mul(wk, d)), z);
+        S.zeta[j] = zn;
+        const double rp = dvd(pik1, pik);
+        co[4] = mul(mul(rp, rp), bk);
+        co[5] = dvd(1.0, mul(pik, zn));
+    }
+    __syncthreads();
+
+    // (2) the systems updated this iteration, in index order
+    if (threadIdx.x == 0) {
+        int na = 0;
+        if (deferred) S.act_list[na++] = seed;
+        for (int j = 0; j < m; j++)
+            if (j != seed && !S.done[j]) S.act_list[na++] = j;
+        sc->n_active = na;
+        if (k < kcap) S.act_hist[k] = na - deferred;
+    }
+    __syncthreads();
+
+    // (3) convergence test on the recursive residual; argmax of |1/(zeta pi)|
+    //     over the systems still running, strict '>' from 1.0 (lowest index
+    //     wins an exact tie)
+    const double thr = mul(mul(sc->tol, sc->tol), sc->bb);
+    double best = 1.0;
+    int bidx = -1, nconv = 0;
+    for (int j = threadIdx.x; j < m; j += NT) {
+        if (S.done[j]) continue;
+        const double a = (j == seed) ? 1.0 : fabs(dvd(1.0, mul(S.zeta[j], S.pi[(size_t)j * kcap + k])));
+        if (mul(mul(a, a), rr) <= thr) {
+            S.done[j] = 1;
+            S.conv_k[j] = k;
+            nconv++;
+        } else if (a > best) {
+            best = a;
+            bidx = j;
+        }
+    }
+    // block argmax: larger value wins, lower index on ties
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+        if (oi >= 0 && (bidx < 0 || ob > best || (ob == best && oi < bidx))) {
+            best = ob;
+            bidx = oi;
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_best[threadIdx.x >> 5] = best;
+        s_bidx[threadIdx.x >> 5] = bidx;
+    }
+    if (threadIdx.x == 0) s_nconv = 0;
+    __syncthreads();
+    if (nconv) atomicAdd(&s_nconv, nconv);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double bb2 = 1.0;
+        int bi = -1;
+        for (int w = 0; w < NW; w++) {
+            const int oi = s_bidx[w];
+            const double ob = s_best[w];
+            if (oi >= 0 && (bi < 0 || ob > bb2 || (ob == bb2 && oi < bi))) {
+                bb2 = ob;
+                bi = oi;
+            }
+        }
+        if (bi >= 0) sc->max_sigma = bi;
+        sc->n_done += s_nconv;
+        s_sw = (sc->switching && S.done[seed] && sc->n_done < m) ? 1 : 0;
+        s_t = sc->max_sigma;
+        sc->next_seed = s_sw ? s_t : seed;
+        sc->switched = s_sw;
+        sc->r_scale = 1.0;
+    }
+    __syncthreads();
+    if (!s_sw) return;
+
+    // (4) seed switch to t: rescale the seed history, rescale r (K5), replay
+    //     eta/pi/zeta of every running shift relative to sigma_t
+    const int t = s_t;
+    const double *pit = S.pi + (size_t)t * kcap;
+    const double dst = sub(sig_s, S.sigma[t]);
+    if (threadIdx.x == 0) sc->r_scale = dvd(1.0, mul(S.zeta[t], pit[k]));
+    for (int i = 1 + threadIdx.x; i <= k; i += NT) {
+        const double rp = dvd(pit[i - 1], pit[i]);
+        S.a_hist[i] = mul(rp, S.a_hist[i]);
+        S.b_hist[i] = mul(mul(rp, rp), S.b_hist[i]);
+        S.w_hist[i] = dvd(S.w_hist[i], sub(1.0, mul(S.w_hist[i], dst)));
+    }
+    __syncthreads();
+    for (int i = 1 + threadIdx.x; i <= k; i += NT) S.ratio[i] = mul(dvd(S.b_hist[i - 1], S.a_hist[i - 1]), S.a_hist[i]);
+    __syncthreads();
+    const double sig_t = S.sigma[t];
+    for (int j = threadIdx.x; j < m; j += NT) {
+        if (S.done[j] || j == t) {
+            S.eta[j] = 0.0;
+            S.zeta[j] = 1.0;
+            continue;
+        }
+        double *pij = S.pi + (size_t)j * kcap;
+        const double d = sub(sig_t, S.sigma[j]);
+        double e = 0.0, z = 1.0, pprev = pij[0];
+        for (int i = 1; i <= k; i++) {
+            e = sub(mul(S.ratio[i], e), mul(mul(d, S.a_hist[i]), pprev));
+            const double pc = add(e, pprev);
+            pij[i] = pc;
+            z = mul(sub(1.0, mul(S.w_hist[i], d)), z);
+            pprev = pc;
+        }
+        S.eta[j] = e;
+        S.zeta[j] = z;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        S.eta[t] = 0.0;
+        S.zeta[t] = 1.0;
+        if (sc->n_sw < m) {
+            S.sw_k[sc->n_sw] = k;
+            S.sw_seed[sc->n_sw] = t;
+        }
+        sc->n_sw++;
+    }
+}
+
+// K4: x_s += alpha p_s + omega q ; r_k = q - omega y ; (r,r), (r^,r)
+__global__ void __launch_bounds__(NT) k_seed_update(Ctx c) {
+    __shared__ double sh[2 * NW];
+    hbk_scalars *sc = c.sh.sc;
+    if (stopped(sc)) return;
+    const double a = sc->alpha, w = sc->omega;
+    const int seed = sc->seed;
+    const unsigned n = c.v.n;
+    const double *__restrict__ ps = seed_p(c, seed);
+    const double *__restrict__ q = vec_q(c, sc);
+    const double *__restrict__ y = c.v.y;
+    const double *__restrict__ rh = c.v.r_hat;
+    double *__restrict__ rn = vec_r_new(c, sc);
+    double2 acc = make_double2(0.0, 0.0);
+    if (!c.v.deferred) {
+        double *__restrict__ xs = c.v.X + (size_t)seed * ldn(n);
+        for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
+            const double qi = q[i];
+            xs[i] = fma(w, qi, fma(a, ps[i], xs[i]));
+            const double r = fma(-w, y[i], qi);
+            rn[i] = r;
+            acc.x = fma(r, r, acc.x);
+            acc.y = fma(rh[i], r, acc.y);
+        }
+    } else {
+        for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
+            const double r = fma(-w, y[i], q[i]);
+            rn[i] = r;
+            acc.x = fma(r, r, acc.x);
+            acc.y = fma(rh[i], r, acc.y);
+        }
+    }
+    acc = block_sum2(acc, sh);
+    if (threadIdx.x == 0) {
+        c.sh.partials[blockIdx.x] = acc.x;
+        c.sh.partials[HBK_MAX_GRID + blockIdx.x] = acc.y;
+    }
+    if (take_ticket(c.sh.counters + 2)) {
+        const double rr = sum_partials(c.sh.partials, gridDim.x, sh);
+        const double rrh = sum_partials(c.sh.partials + HBK_MAX_GRID, gridDim.x, sh);
+        seed_step_scalars(c, rr, rrh);
+        if (threadIdx.x == 0) c.sh.counters[2] = 0;
+    }
+}
+
+// End of an iteration (one thread): apply the switch, advance k, test the loop.
+__device__ void finish_iteration(const Ctx &c, hbk_scalars *sc, double rrh_scaled) {
+    if (sc->switched) {
+        sc->rr_hat = rrh_scaled;
+        sc->seed = sc->next_seed;
+        sc->switched = 0;
+        if (c.v.deferred) {
+            sc->slot_r_old = sc->slots + 2;  // the rescaled r_k
+            sc->slots += 3;
+            sc->need_ps = 1;
+        }
+    } else if (c.v.deferred) {
+        sc->slot_r_old = sc->slots + 1;
+        sc->slots += 2;
+    }
+    sc->k += 1;
+    if (sc->n_done >= sc->m || sc->k >= sc->kcap) sc->finished = 1;
+    if (c.v.deferred && !sc->finished && sc->slots + 3 > sc->slot_cap) {
+        sc->status |= HBK_ST_BASIS_FULL;
+        sc->finished = 1;  // the host flushes the basis and resumes
+    }
+}
+
+// K5 (incremental): p_s, then every running shift's x_j and p_j in one pass
+// over q, r_{k-1}, r_k (src/solver_dynamic.c:208-210, :248-255)
+template <int MAXS>
+__global__ void __launch_bounds__(NT) k_shift_update(Ctx c) {
+    __shared__ double s_co[MAXS * 6];
+    __shared__ int s_j[MAXS];
+    __shared__ double sh[NW];
+    hbk_scalars *sc = c.sh.sc;
+    if (stopped(sc)) return;
+    const int seed = sc->seed, na = sc->n_active, k = sc->k;
+    const double bk = sc->beta, wk = sc->omega, bw = -mul(bk, wk);
+    const int sw = sc->switched;
+    const double rsc = sc->r_scale;
+    const unsigned n = c.v.n;
+    const size_t ld = ldn(n);
+    double *__restrict__ ps = c.v.P + (size_t)seed * ld;
+    const double *__restrict__ q = c.v.q;
+    const double *__restrict__ s = c.v.s;
+    const double *__restrict__ ro = c.v.rbuf[(k - 1) & 1];
+    double *__restrict__ rn = c.v.rbuf[k & 1];
+    const double *__restrict__ rh = c.v.r_hat;
+    double acc = 0.0;
+    for (int base = 0; base < na || base == 0; base += MAXS) {
+        const int cnt = min(MAXS, na - base);
+        for (int a = threadIdx.x; a < cnt; a += NT) {
+            const int j = c.sh.act_list[base + a];
+            s_j[a] = j;
+            const double *co = c.sh.coef + (size_t)j * HBK_NCOEF;
+#pragma unroll
+            for (int t = 0; t < 6; t++) s_co[a * 6 + t] = co[t];
+        }
+        __syncthreads();
+        for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
+            const double qi = q[i], oi = ro[i], ri = rn[i];
+            if (base == 0) ps[i] = fma(bw, s[i], fma(bk, ps[i], ri));
+            for (int a = 0; a < cnt; a++) {
+                const double *co = s_co + a * 6;
+                double *xj = c.v.X + (size_t)s_j[a] * ld;
+                double *pj = c.v.P + (size_t)s_j[a] * ld;
+                double x = xj[i], p = pj[i];
+                x = fma(co[0], qi, x);
+                x = fma(co[1], p, x);
+                p = fma(co[2], qi, p);
+                p = fma(co[3], oi, p);
+                p = co[4] * p;
+                p = fma(co[5], ri, p);
+                xj[i] = x;
+                pj[i] = p;
+            }
+            if (sw && base + MAXS >= na) {
+                const double rs = ri * rsc;
+                rn[i] = rs;
+                acc = fma(rh[i], rs, acc);
+            }
+        }
+        __syncthreads();
+        if (na <= MAXS) break;
+    }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) c.sh.partials[blockIdx.x] = acc;
+    if (take_ticket(c.sh.counters + 3)) {
+        const double rrh = sum_partials(c.sh.partials, gridDim.x, sh);
+        if (threadIdx.x == 0) {
+            finish_iteration(c, sc, rrh);
+            c.sh.counters[3] = 0;
+        }
+    }
+}
+
+// K5 (deferred): p_s update; on a switch the rescaled r_k goes to a new slot
+__global__ void __launch_bounds__(NT) k_seed_p_deferred(Ctx c) {
+    __shared__ double sh[NW];
+    hbk_scalars *sc = c.sh.sc;
+    if (stopped(sc)) return;
+    const double bk = sc->beta, bw = -mul(bk, sc->omega);
+    const int sw = sc->switched;
+    const double rsc = sc->r_scale;
+    const unsigned n = c.v.n;
+    const size_t ld = ldn(n);
+    double *__restrict__ ps = c.v.ps;
+    const double *__restrict__ s = c.v.s;
+    const double *__restrict__ rn = c.v.V + (size_t)(sc->slots + 1) * ld;
+    double *__restrict__ rsl = c.v.V + (size_t)(sc->slots + 2) * ld;
+    const double *__restrict__ rh = c.v.r_hat;
+    double acc = 0.0;
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
+        const double ri = rn[i];
+        ps[i] = fma(bw, s[i], fma(bk, ps[i], ri));
+        if (sw) {
+            const double rs = ri * rsc;
+            rsl[i] = rs;
+            acc = fma(rh[i], rs, acc);
+        }
+    }
+    if (!sw) return;  // uniform: the reduction is needed only after a switch
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) c.sh.partials[blockIdx.x] = acc;
+    if (take_ticket(c.sh.counters + 3)) {
+        const double rrh = sum_partials(c.sh.partials, gridDim.x, sh);
+        if (threadIdx.x == 0) {
+            sc->rs_switch = rrh;
+            c.sh.counters[3] = 0;
+        }
+    }
+}
+
+// K6 (deferred): coefficient update of every running system over the basis
+// slots in use, then the end-of-iteration bookkeeping.  Per coefficient the
+// operations follow the vector update's order (x += c0 q; x += c1 p;
+// p += c2 q; p += c3 r_{k-1}; p *= beta_j; p += c5 r_k).
+__global__ void __launch_bounds__(NT) k_coef_update(Ctx c) {
+    hbk_scalars *sc = c.sh.sc;
+    if (stopped(sc)) return;
+    const int na = sc->n_active;
+    const int sq = sc->slots, sr = sc->slots + 1, so = sc->slot_r_old;
+    const int L = sc->slots + 2;
+    const int cap = c.v.slot_cap;
+    const size_t tot = (size_t)na * L;
+    for (size_t it = blockIdx.x * (size_t)NT + threadIdx.x; it < tot; it += (size_t)gridDim.x * NT) {
+        const int a = (int)(it / L), i = (int)(it % L);
+        const int j = c.sh.act_list[a];
+        const double *co = c.sh.coef + (size_t)j * HBK_NCOEF;
+        double *xc = c.v.Xc + (size_t)j * cap + i;
+        double *pc = c.v.Pc + (size_t)j * cap + i;
+        double x = *xc, p = *pc;
+        if (i == sq) x = x + co[0];
+        x = fma(co[1], p, x);
+        if (i == sq) p = p + co[2];
+        if (i == so) p = p + co[3];
+        p = co[4] * p;
+        if (i == sr) p = p + co[5];
+        *xc = x;
+        *pc = p;
+        if (i == 0) {
+            double *ow = c.v.own + 2 * (size_t)j;
+            ow[0] = fma(co[1], ow[1], ow[0]);
+            ow[1] = co[4] * ow[1];
+            c.sh.lslot[j] = L;
+        }
+    }
+    if (take_ticket(c.sh.counters + 4)) {
+        if (threadIdx.x == 0) {
+            finish_iteration(c, sc, sc->rs_switch);
+            c.sh.counters[4] = 0;
+        }
+    }
+}
+
+// K7 (deferred): after a switch, the new seed's p = own term + Pc[t] . V
+__global__ void __launch_bounds__(NT) k_materialize_ps(Ctx c) {
+    __shared__ double s_c[1024];
+    hbk_scalars *sc = c.sh.sc;
+    if (!sc->need_ps) return;
+    const int t = sc->seed;
+    const int L = c.sh.lslot[t];
+    const unsigned n = c.v.n;
+    const size_t ld = ldn(n);
+    const double *pc = c.v.Pc + (size_t)t * c.v.slot_cap;
+    const double rho = c.v.own[2 * (size_t)t + 1];
+    const double *pm = c.v.Pmat ? c.v.Pmat + (size_t)t * ld : nullptr;
+    for (size_t i0 = (size_t)blockIdx.x * NT; i0 < n; i0 += (size_t)gridDim.x * NT) {
+        const size_t i = i0 + threadIdx.x;
+        double acc = (pm && i < n) ? rho * pm[i] : 0.0;
+        for (int l0 = 0; l0 < L; l0 += 1024) {
+            const int cnt = min(1024, L - l0);
+            __syncthreads();
+            for (int l = threadIdx.x; l < cnt; l += NT) s_c[l] = pc[l0 + l];
+            __syncthreads();
+            if (i < n)
+                for (int l = 0; l < cnt; l++) acc = fma(s_c[l], c.v.V[(size_t)(l0 + l) * ld + i], acc);
+        }
+        if (i < n) c.v.ps[i] = acc;
+    }
+    if (take_ticket(c.sh.counters + 5)) {
+        if (threadIdx.x == 0) {
+            sc->need_ps = 0;
+            c.sh.counters[5] = 0;
+        }
+    }
+}
+
+// Flush: X_j += xi_j Pmat_j + Xc_j . V ; when keep_p, Pmat_j = rho_j Pmat_j + Pc_j . V.
+// Each thread owns one row and GROUP systems; coefficients are staged in
+// shared memory per chunk of slots.  FP64 FMA-bound by design: it is the
+// only place the per-shift solutions are formed.
+constexpr int GROUP = 16;
+constexpr int LCH = 64;
+__global__ void __launch_bounds__(NT) k_flush(Ctx c, int keep_p, int which) {
+    __shared__ double s_c[GROUP * LCH];
+    const unsigned n = c.v.n;
+    const size_t ld = ldn(n);
+    const int m = c.sh.m, cap = c.v.slot_cap;
+    const int j0 = blockIdx.y * GROUP;
+    const int g = min(GROUP, m - j0);
+    int L = 0;
+    for (int t = 0; t < g; t++) L = max(L, c.sh.lslot[j0 + t]);
+    const double *coef = which == 0 ? c.v.Xc : c.v.Pc;
+    double *out = which == 0 ? c.v.X : c.v.Pmat;
+    for (size_t i0 = (size_t)blockIdx.x * NT; i0 < n; i0 += (size_t)gridDim.x * NT) {
+        const size_t i = i0 + threadIdx.x;
+        double acc[GROUP];
+#pragma unroll
+        for (int t = 0; t < GROUP; t++) {
+            acc[t] = 0.0;
+            if (t < g && i < n) {
+                const int j = j0 + t;
+                const double *pm = c.v.Pmat ? c.v.Pmat + (size_t)j * ld : nullptr;
+                if (which == 0) {
+                    acc[t] = c.v.X[(size_t)j * ld + i];
+                    if (pm) acc[t] = fma(c.v.own[2 * (size_t)j], pm[i], acc[t]);
+                } else if (pm) {
+                    acc[t] = c.v.own[2 * (size_t)j + 1] * pm[i];
+                }
+            }
+        }
+        for (int l0 = 0; l0 < L; l0 += LCH) {
+            const int cnt = min(LCH, L - l0);
+            __syncthreads();
+            for (int e = threadIdx.x; e < GROUP * LCH; e += NT) {
+                const int t = e / LCH, l = e % LCH;
+                s_c[e] = (t < g && l < cnt) ? coef[(size_t)(j0 + t) * cap + l0 + l] : 0.0;
+            }
+            __syncthreads();
+            if (i < n) {
+                for (int l = 0; l < cnt; l++) {
+                    const double v = c.v.V[(size_t)(l0 + l) * ld + i];
+#pragma unroll
+                    for (int t = 0; t < GROUP; t++) acc[t] = fma(s_c[t * LCH + l], v, acc[t]);
+                }
+            }
+        }
+        if (i < n) {
+#pragma unroll
+            for (int t = 0; t < GROUP; t++)
+                if (t < g) out[(size_t)(j0 + t) * ld + i] = acc[t];
+        }
+    }
+    (void)keep_p;
+}
+
+// after a flush: reset the coefficients, own = (0, 1), slot 0 = r_{k-1}
+__global__ void __launch_bounds__(NT) k_flush_reset(Ctx c, int keep_p) {
+    hbk_scalars *sc = c.sh.sc;
+    const int m = c.sh.m, cap = c.v.slot_cap;
+    const unsigned n = c.v.n;
+    const size_t ld = ldn(n);
+    const int so = sc->slot_r_old;
+    const size_t tot = (size_t)m * cap;
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < tot; i += (size_t)gridDim.x * NT) {
+        c.v.Xc[i] = 0.0;
+        c.v.Pc[i] = 0.0;
+    }
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < (size_t)m; i += (size_t)gridDim.x * NT) {
+        c.v.own[2 * i] = 0.0;
+        c.v.own[2 * i + 1] = keep_p ? 1.0 : 0.0;
+        c.sh.lslot[i] = 1;
+    }
+    if (so != 0)
+        for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT)
+            c.v.V[i] = c.v.V[(size_t)so * ld + i];
+    if (take_ticket(c.sh.counters + 6)) {
+        if (threadIdx.x == 0) {
+            sc->slots = 1;
+            sc->slot_r_old = 0;
+            sc->status &= ~HBK_ST_BASIS_FULL;
+            if (sc->n_done < sc->m && sc->k < sc->kcap && !(sc->status & HBK_ST_BREAKDOWN)) sc->finished = 0;
+            c.sh.counters[6] = 0;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+static Ctx make_ctx(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh) {
+    Ctx c;
+    c.A = *A;
+    c.v = *v;
+    c.sh = *sh;
+    return c;
+}
+
+int hbk_fused_init(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, const double *b, int seed,
+                   double tol, cudaStream_t st) {
+    Ctx c = make_ctx(A, v, sh);
+    const unsigned n = v->n;
+    const size_t ld = ((size_t)n + 31) / 32 * 32;
+    int e;
+    if ((e = hbk_copy(n, b, v->r_hat, st))) return e;
+    if ((e = hbk_dot(n, b, b, sh->partials, sh->counters + 7, &sh->sc->bb, st))) return e;
+    if (!v->deferred) {
+        if ((e = hbk_copy(n, b, v->rbuf[0], st))) return e;
+        for (int j = 0; j < sh->m; j++) {
+            if ((e = hbk_copy(n, b, v->P + (size_t)j * ld, st))) return e;
+        }
+    } else {
+        if ((e = hbk_copy(n, b, v->V, st))) return e;
+        if ((e = hbk_copy(n, b, v->ps, st))) return e;
+        k_init_coef<<<grid_for((unsigned)((size_t)sh->m * v->slot_cap), 1), NT, 0, st>>>(c);
+        if ((e = (int)cudaGetLastError())) return e;
+    }
+    if ((e = (int)cudaMemsetAsync(v->X, 0, sizeof(double) * ld * (size_t)sh->m, st))) return e;
+    k_init<<<1, NT, 0, st>>>(c, seed, tol);
+    return (int)cudaGetLastError();
+}
+
+int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, cudaStream_t st) {
+    Ctx c = make_ctx(A, v, sh);
+    const int gv = grid_for(v->n, 2);
+    k_seed_s<<<A->grid, NT, 0, st>>>(c);
+    k_seed_q<<<gv, NT, 0, st>>>(c);
+    k_seed_y<<<A->grid, NT, 0, st>>>(c);
+    k_seed_update<<<gv, NT, 0, st>>>(c);
+    if (!v->deferred) {
+        k_shift_update<64><<<gv, NT, 0, st>>>(c);
+    } else {
+        k_seed_p_deferred<<<gv, NT, 0, st>>>(c);
+        k_coef_update<<<grid_for((unsigned)((size_t)sh->m * v->slot_cap), 1), NT, 0, st>>>(c);
+        k_materialize_ps<<<gv, NT, 0, st>>>(c);
+    }
+    return (int)cudaGetLastError();
+}
+
+int hbk_deferred_flush(const hbk_vectors *v, const hbk_shifts *sh, int keep_p, cudaStream_t st) {
+    hbk_matrix A0 = {};
+    Ctx c = make_ctx(&A0, v, sh);
+    const int groups = (sh->m + GROUP - 1) / GROUP;
+    dim3 grid(grid_for(v->n, 1), groups);
+    // p first (it reads the old Pmat that the x update also reads): write into X
+    // before Pmat is overwritten
+    k_flush<<<grid, NT, 0, st>>>(c, keep_p, 0);
+    if (keep_p) k_flush<<<grid, NT, 0, st>>>(c, keep_p, 1);
+    k_flush_reset<<<grid_for(v->n, 2), NT, 0, st>>>(c, keep_p);
+    return (int)cudaGetLastError();
+}
+
+}  // extern "C"

@@ -1,0 +1,924 @@
+/* Host driver of the GB300 shifted BiCGStab solver (C11 + CUDA runtime).
+ *
+ * Owns the device workspace, uploads inputs, runs one of the two iteration
+ * forms and returns results through the reference's entry points
+ * (src/solver.h:33-35) and the extended API (include/hbicg.h):
+ *   plain  one kernel per step of the reference's iteration; dot products come
+ *          back to the host, which keeps the scalars, runs the shift
+ *          recurrences, the convergence test and the seed switch exactly as
+ *          src/solver_dynamic.c:147-381 does (the per-kernel form);
+ *   fused  five to seven kernels per iteration with every scalar on the device
+ *          (hbk_fused_iteration); iterations are captured in CUDA graphs and
+ *          the host only polls a finished flag between graph launches.
+ * In the fused form the shifts are either updated every iteration by one
+ * multi-shift kernel (incremental) or kept as coefficient vectors over the
+ * seed's Krylov basis and formed once at the end by an FP64 GEMM-like kernel
+ * (deferred), which cuts the FP64 work per shift per iteration by three.
+ */
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cuda_runtime.h>
+
+#include "hbicg.h"
+#include "hbk.h"
+#include "solver.h"
+
+/* ------------------------------------------------------------------------ */
+static _Thread_local char g_msg[512];
+
+static void set_msg(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_msg, sizeof g_msg, fmt, ap);
+    va_end(ap);
+}
+
+const char *hbicg_last_message(void) { return g_msg; }
+
+const char *hbicg_status_string(int s) {
+    switch (s) {
+    case HBICG_OK: return "ok";
+    case HBICG_E_NOT_SQUARE: return "matrix is not square";
+    case HBICG_E_NO_DIAG: return "diagonal entry missing";
+    case HBICG_E_BREAKDOWN: return "breakdown (zero or non-finite recurrence scalar)";
+    case HBICG_E_MAXITER: return "maximum iterations reached";
+    case HBICG_E_CUDA: return "CUDA error";
+    case HBICG_E_TIMEOUT: return "timeout";
+    case HBICG_E_ARG: return "invalid argument";
+    case HBICG_E_NOMEM: return "out of device memory";
+    case HBICG_E_IO: return "I/O error";
+    default: return "unknown status";
+    }
+}
+
+#define CUDA_TRY(call)                                                                                   \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess) {                                                                         \
+            set_msg("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));                  \
+            return e_ == cudaErrorMemoryAllocation ? HBICG_E_NOMEM : HBICG_E_CUDA;                       \
+        }                                                                                                \
+    } while (0)
+
+#define HBK_TRY(call)                                                                                    \
+    do {                                                                                                 \
+        int e_ = (call);                                                                                 \
+        if (e_) {                                                                                        \
+            set_msg("%s:%d %s: %s", __FILE__, __LINE__, #call, hbk_error_string(e_));                    \
+            return HBICG_E_CUDA;                                                                         \
+        }                                                                                                \
+    } while (0)
+
+static size_t ld_of(unsigned n) { return ((size_t)n + 31) / 32 * 32; }
+
+void hbicg_params_default(hbicg_params *p) {
+    memset(p, 0, sizeof *p);
+    p->tol = EPS;
+    p->max_iter = MAX_ITER;
+    p->switching = 1;
+    p->form = HBICG_FORM_FUSED;
+    p->shift_mode = HBICG_SHIFTS_AUTO;
+    p->use_graph = 1;
+    p->graph_chunk = 0;
+    p->basis_mem_frac = 0.6;
+    p->true_residuals = 0;
+}
+
+/* ------------------------------------------------------------------------ */
+struct hbicg_context {
+    cudaStream_t stream;
+    cudaEvent_t ev0, ev1;
+    hbk_scalars *h_sc; /* pinned */
+    double *h_dbl;     /* pinned scratch */
+};
+
+int hbicg_context_create(hbicg_context **out) {
+    hbicg_context *c = calloc(1, sizeof *c);
+    if (!c) return HBICG_E_NOMEM;
+    CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&c->ev0));
+    CUDA_TRY(cudaEventCreate(&c->ev1));
+    CUDA_TRY(cudaMallocHost((void **)&c->h_sc, sizeof(hbk_scalars)));
+    CUDA_TRY(cudaMallocHost((void **)&c->h_dbl, sizeof(double) * 64));
+    *out = c;
+    return HBICG_OK;
+}
+
+void hbicg_context_destroy(hbicg_context *c) {
+    if (!c) return;
+    cudaStreamSynchronize(c->stream);
+    cudaFreeHost(c->h_sc);
+    cudaFreeHost(c->h_dbl);
+    cudaEventDestroy(c->ev0);
+    cudaEventDestroy(c->ev1);
+    cudaStreamDestroy(c->stream);
+    free(c);
+}
+
+void *hbicg_context_stream(hbicg_context *c) { return (void *)c->stream; }
+
+/* ------------------------------------------------------------------------ */
+struct hbicg_matrix {
+    hbicg_context *ctx;
+    hbk_matrix k;
+    unsigned *d_ptr, *d_col;
+    double *d_val;
+    int owns;
+    unsigned *d_blk_row;
+    unsigned char *d_blk_kind;
+};
+
+int hbicg_matrix_create(hbicg_context *ctx, unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *col,
+                        const double *val, int where, hbicg_matrix **out) {
+    hbicg_matrix *A = calloc(1, sizeof *A);
+    if (!A) return HBICG_E_NOMEM;
+    A->ctx = ctx;
+    cudaStream_t st = ctx->stream;
+    unsigned *h_ptr = NULL;
+    if (where == HBICG_DEVICE) {
+        A->d_ptr = (unsigned *)ptr;
+        A->d_col = (unsigned *)col;
+        A->d_val = (double *)val;
+        A->owns = 0;
+        h_ptr = malloc(sizeof(unsigned) * ((size_t)n + 1));
+        if (!h_ptr) return HBICG_E_NOMEM;
+        CUDA_TRY(cudaMemcpyAsync(h_ptr, ptr, sizeof(unsigned) * ((size_t)n + 1), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+    } else {
+        A->owns = 1;
+        CUDA_TRY(cudaMalloc((void **)&A->d_ptr, sizeof(unsigned) * ((size_t)n + 1)));
+        CUDA_TRY(cudaMalloc((void **)&A->d_col, sizeof(unsigned) * ((size_t)nnz + 1)));
+        CUDA_TRY(cudaMalloc((void **)&A->d_val, sizeof(double) * ((size_t)nnz + 1)));
+        CUDA_TRY(cudaMemcpyAsync(A->d_ptr, ptr, sizeof(unsigned) * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
+        if (nnz) {
+            CUDA_TRY(cudaMemcpyAsync(A->d_col, col, sizeof(unsigned) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+            CUDA_TRY(cudaMemcpyAsync(A->d_val, val, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+        }
+        h_ptr = (unsigned *)ptr;
+    }
+    if (h_ptr[n] != nnz) {
+        set_msg("ptr[n] = %u but nnz = %u", h_ptr[n], nnz);
+        if (where == HBICG_DEVICE) free(h_ptr);
+        free(A);
+        return HBICG_E_ARG;
+    }
+    unsigned nb = hbk_plan_rows(n, h_ptr, NULL, NULL);
+    unsigned *blk = malloc(sizeof(unsigned) * ((size_t)nb + 1));
+    unsigned char *kind = malloc((size_t)nb + 1);
+    hbk_plan_rows(n, h_ptr, blk, kind);
+    CUDA_TRY(cudaMalloc((void **)&A->d_blk_row, sizeof(unsigned) * ((size_t)nb + 1)));
+    CUDA_TRY(cudaMalloc((void **)&A->d_blk_kind, (size_t)nb + 1));
+    CUDA_TRY(cudaMemcpyAsync(A->d_blk_row, blk, sizeof(unsigned) * ((size_t)nb + 1), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(A->d_blk_kind, kind, (size_t)nb + 1, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    free(blk);
+    free(kind);
+    if (where == HBICG_DEVICE) free(h_ptr);
+    A->k.n = n;
+    A->k.nnz = nnz;
+    A->k.ptr = A->d_ptr;
+    A->k.col = A->d_col;
+    A->k.val = A->d_val;
+    A->k.blk_row = A->d_blk_row;
+    A->k.blk_kind = A->d_blk_kind;
+    A->k.nblk = nb;
+    A->k.grid = hbk_spmv_grid(nb);
+    *out = A;
+    return HBICG_OK;
+}
+
+void hbicg_matrix_destroy(hbicg_matrix *A) {
+    if (!A) return;
+    cudaStreamSynchronize(A->ctx->stream);
+    if (A->owns) {
+        cudaFree(A->d_ptr);
+        cudaFree(A->d_col);
+        cudaFree(A->d_val);
+    }
+    cudaFree(A->d_blk_row);
+    cudaFree(A->d_blk_kind);
+    free(A);
+}
+
+unsigned hbicg_matrix_rows(const hbicg_matrix *A) { return A->k.n; }
+unsigned long long hbicg_matrix_nnz(const hbicg_matrix *A) { return A->k.nnz; }
+
+int hbicg_matrix_spmv(hbicg_matrix *A, const double *x, double *y, double sigma, int where) {
+    cudaStream_t st = A->ctx->stream;
+    const unsigned n = A->k.n;
+    if (where == HBICG_DEVICE) {
+        HBK_TRY(hbk_spmv(&A->k, x, y, sigma, sigma != 0.0, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        return HBICG_OK;
+    }
+    double *dx = NULL, *dy = NULL;
+    CUDA_TRY(cudaMalloc((void **)&dx, sizeof(double) * ((size_t)n + 1)));
+    CUDA_TRY(cudaMalloc((void **)&dy, sizeof(double) * ((size_t)n + 1)));
+    CUDA_TRY(cudaMemcpyAsync(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    HBK_TRY(hbk_spmv(&A->k, dx, dy, sigma, sigma != 0.0, st));
+    CUDA_TRY(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    cudaFree(dx);
+    cudaFree(dy);
+    return HBICG_OK;
+}
+
+/* Host-pointer product used by the matrix.h entry points: y (+)= A x with A
+ * rows x cols.  Runs the CSR SpMV kernel on a process-wide context. */
+static hbicg_context *g_host_ctx = NULL;
+
+int hbicg__host_spmv(unsigned rows, unsigned cols, unsigned nnz, const unsigned *ptr, const unsigned *col,
+                     const double *val, const double *x, double *y, int accumulate) {
+    if (!rows) return HBICG_OK;
+    if (!g_host_ctx) {
+        int rc = hbicg_context_create(&g_host_ctx);
+        if (rc) return rc;
+    }
+    hbicg_matrix *A = NULL;
+    int rc = hbicg_matrix_create(g_host_ctx, rows, nnz, ptr, col, val, HBICG_HOST, &A);
+    if (rc) return rc;
+    cudaStream_t st = g_host_ctx->stream;
+    double *dx = NULL, *dy = NULL;
+    CUDA_TRY(cudaMalloc((void **)&dx, sizeof(double) * ((size_t)cols + 1)));
+    CUDA_TRY(cudaMalloc((void **)&dy, sizeof(double) * ((size_t)rows + 1)));
+    if (cols) CUDA_TRY(cudaMemcpyAsync(dx, x, sizeof(double) * cols, cudaMemcpyHostToDevice, st));
+    if (accumulate) {
+        CUDA_TRY(cudaMemcpyAsync(dy, y, sizeof(double) * rows, cudaMemcpyHostToDevice, st));
+        HBK_TRY(hbk_spmv_accumulate(&A->k, dx, dy, st));
+    } else {
+        HBK_TRY(hbk_spmv(&A->k, dx, dy, 0.0, 0, st));
+    }
+    CUDA_TRY(cudaMemcpyAsync(y, dy, sizeof(double) * rows, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    cudaFree(dx);
+    cudaFree(dy);
+    hbicg_matrix_destroy(A);
+    return HBICG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+struct hbicg_solver {
+    hbicg_context *ctx;
+    hbicg_matrix *A;
+    int m, kcap, mode;
+    hbicg_params p;
+    size_t ld;
+    hbk_vectors v;
+    hbk_shifts sh;
+    hbk_scalars *d_sc;
+    double *d_sigma, *d_b, *d_res;
+    /* plain form */
+    double *d_rold, *d_qcopy, *d_r, *d_dot;
+    /* fused form graphs */
+    cudaGraphExec_t graph;
+    int chunk;
+    int launches_per_iter;
+};
+
+static int pick_mode(const hbicg_params *p, unsigned n, int m) {
+    if (p->form == HBICG_FORM_PLAIN) return HBICG_SHIFTS_INCREMENTAL;
+    if (p->shift_mode != HBICG_SHIFTS_AUTO) return p->shift_mode;
+    /* Deferred mode pays a fixed per-iteration cost (two small kernels and the
+     * coefficient update) and saves 4 of 6 FP64 operations per element and
+     * shift; it wins once the per-shift vector work dominates. */
+    if (m >= 2 && (double)n * (double)m >= (double)(1u << 21)) return HBICG_SHIFTS_DEFERRED;
+    return HBICG_SHIFTS_INCREMENTAL;
+}
+
+#define DALLOC(ptr, bytes) CUDA_TRY(cudaMalloc((void **)&(ptr), (size_t)(bytes) > 0 ? (size_t)(bytes) : 8))
+
+int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_params *pp, hbicg_solver **out) {
+    hbicg_params p;
+    if (pp) p = *pp;
+    else hbicg_params_default(&p);
+    if (m < 0 || p.max_iter < 0) {
+        set_msg("m = %d, max_iter = %d", m, p.max_iter);
+        return HBICG_E_ARG;
+    }
+    hbicg_solver *s = calloc(1, sizeof *s);
+    if (!s) return HBICG_E_NOMEM;
+    s->ctx = ctx;
+    s->A = A;
+    s->m = m;
+    s->p = p;
+    s->kcap = p.max_iter + 1;
+    const unsigned n = A->k.n;
+    const size_t ld = ld_of(n);
+    s->ld = ld;
+    const int mm = m > 0 ? m : 1;
+    s->mode = pick_mode(&p, n, m);
+    size_t vb = sizeof(double) * ld;
+
+    hbk_vectors *v = &s->v;
+    memset(v, 0, sizeof *v);
+    v->n = n;
+    DALLOC(v->r_hat, vb);
+    DALLOC(v->s, vb);
+    DALLOC(v->y, vb);
+    DALLOC(v->X, vb * mm);
+    if (s->mode == HBICG_SHIFTS_INCREMENTAL) {
+        DALLOC(v->rbuf[0], vb);
+        DALLOC(v->rbuf[1], vb);
+        DALLOC(v->q, vb);
+        DALLOC(v->P, vb * mm);
+    } else {
+        v->deferred = 1;
+        DALLOC(v->ps, vb);
+        size_t fr = 0, tot = 0;
+        CUDA_TRY(cudaMemGetInfo(&fr, &tot));
+        double frac = p.basis_mem_frac > 0 ? p.basis_mem_frac : 0.6;
+        /* keep room for a later flush buffer (m*n) out of the basis budget */
+        double budget = frac * (double)fr - (double)vb * mm;
+        long cap = (long)(budget / (double)vb);
+        long want = 2L * s->kcap + 8;
+        if (cap > want) cap = want;
+        if (cap < 8) {
+            /* not enough memory for a useful basis: fall back */
+            s->mode = HBICG_SHIFTS_INCREMENTAL;
+            v->deferred = 0;
+            cudaFree(v->ps);
+            v->ps = NULL;
+            DALLOC(v->rbuf[0], vb);
+            DALLOC(v->rbuf[1], vb);
+            DALLOC(v->q, vb);
+            DALLOC(v->P, vb * mm);
+        } else {
+            v->slot_cap = (int)cap;
+            DALLOC(v->V, vb * (size_t)cap);
+            DALLOC(v->Xc, sizeof(double) * (size_t)mm * (size_t)cap);
+            DALLOC(v->Pc, sizeof(double) * (size_t)mm * (size_t)cap);
+            DALLOC(v->own, sizeof(double) * 2 * (size_t)mm);
+        }
+    }
+
+    hbk_shifts *sh = &s->sh;
+    memset(sh, 0, sizeof *sh);
+    sh->m = m;
+    sh->kcap = s->kcap;
+    DALLOC(s->d_sc, sizeof(hbk_scalars));
+    CUDA_TRY(cudaMemset(s->d_sc, 0, sizeof(hbk_scalars)));
+    sh->sc = s->d_sc;
+    DALLOC(s->d_sigma, sizeof(double) * mm);
+    sh->sigma = s->d_sigma;
+    DALLOC(sh->a_hist, sizeof(double) * ((size_t)s->kcap + 1));
+    DALLOC(sh->b_hist, sizeof(double) * ((size_t)s->kcap + 1));
+    DALLOC(sh->w_hist, sizeof(double) * ((size_t)s->kcap + 1));
+    DALLOC(sh->ratio, sizeof(double) * ((size_t)s->kcap + 1));
+    DALLOC(sh->pi, sizeof(double) * (size_t)mm * ((size_t)s->kcap + 1));
+    DALLOC(sh->eta, sizeof(double) * mm);
+    DALLOC(sh->zeta, sizeof(double) * mm);
+    DALLOC(sh->done, sizeof(int) * mm);
+    DALLOC(sh->conv_k, sizeof(int) * mm);
+    DALLOC(sh->act_list, sizeof(int) * mm);
+    DALLOC(sh->lslot, sizeof(int) * mm);
+    DALLOC(sh->coef, sizeof(double) * HBK_NCOEF * (size_t)mm);
+    DALLOC(sh->sw_k, sizeof(int) * mm);
+    DALLOC(sh->sw_seed, sizeof(int) * mm);
+    DALLOC(sh->act_hist, sizeof(int) * ((size_t)s->kcap + 1));
+    CUDA_TRY(cudaMemset(sh->act_hist, 0, sizeof(int) * ((size_t)s->kcap + 1)));
+    size_t nparts = (size_t)(mm > 4 ? mm : 4) * HBK_MAX_GRID;
+    DALLOC(sh->partials, sizeof(double) * nparts);
+    DALLOC(sh->counters, sizeof(unsigned) * (16 + (size_t)mm));
+    CUDA_TRY(cudaMemset(sh->counters, 0, sizeof(unsigned) * (16 + (size_t)mm)));
+    DALLOC(s->d_b, vb);
+    DALLOC(s->d_res, sizeof(double) * mm);
+    DALLOC(s->d_dot, sizeof(double) * 8);
+    if (p.form == HBICG_FORM_PLAIN) {
+        DALLOC(s->d_rold, vb);
+        DALLOC(s->d_qcopy, vb);
+        s->d_r = v->rbuf[0];
+    }
+    s->chunk = p.graph_chunk > 0 ? p.graph_chunk : (n >= (1u << 22) ? 2 : (n >= (1u << 18) ? 4 : 16));
+    s->launches_per_iter = s->mode == HBICG_SHIFTS_DEFERRED ? 7 : 5;
+    *out = s;
+    return HBICG_OK;
+}
+
+void hbicg_solver_destroy(hbicg_solver *s) {
+    if (!s) return;
+    cudaStreamSynchronize(s->ctx->stream);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    hbk_vectors *v = &s->v;
+    hbk_shifts *sh = &s->sh;
+    void *ptrs[] = {v->r_hat, v->rbuf[0], v->rbuf[1], v->s, v->q, v->y, v->X, v->P, v->V, v->ps, v->Xc, v->Pc,
+                    v->own, v->Pmat, s->d_sc, s->d_sigma, sh->a_hist, sh->b_hist, sh->w_hist, sh->ratio, sh->pi,
+                    sh->eta, sh->zeta, sh->done, sh->conv_k, sh->act_list, sh->lslot, sh->coef, sh->sw_k,
+                    sh->sw_seed, sh->act_hist, sh->partials, sh->counters, s->d_b, s->d_res, s->d_dot, s->d_rold,
+                    s->d_qcopy};
+    for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++)
+        if (ptrs[i]) cudaFree(ptrs[i]);
+    free(s);
+}
+
+/* ------------------------------------------------------------------------ */
+/* plain form: the reference's iteration, one kernel per step, host scalars */
+
+static int dev_dot(hbicg_solver *s, const double *x, const double *y, double *out) {
+    cudaStream_t st = s->ctx->stream;
+    HBK_TRY(hbk_dot(s->A->k.n, x, y, s->sh.partials, s->sh.counters + 7, s->d_dot, st));
+    CUDA_TRY(cudaMemcpyAsync(s->ctx->h_dbl, s->d_dot, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    *out = s->ctx->h_dbl[0];
+    return HBICG_OK;
+}
+
+typedef struct {
+    int k, n_sw, final_seed, launches, status;
+    int *sw_k, *sw_seed, *conv_k, *act;
+} plain_out;
+
+static int run_plain(hbicg_solver *s, const double *h_sigma, int seed, plain_out *o) {
+    cudaStream_t st = s->ctx->stream;
+    const hbk_matrix *A = &s->A->k;
+    const unsigned n = A->n;
+    const int m = s->m, kcap = s->kcap;
+    const size_t ld = s->ld;
+    const double tol = s->p.tol;
+    hbk_vectors *v = &s->v;
+    double *r = s->d_r, *r_old = s->d_rold, *r_hat = v->r_hat, *sv = v->s, *y = v->y, *qc = s->d_qcopy;
+    double *ah = malloc(sizeof(double) * (kcap + 1)), *bh = malloc(sizeof(double) * (kcap + 1));
+    double *wh = malloc(sizeof(double) * (kcap + 1));
+    double *pi = malloc(sizeof(double) * (size_t)m * (kcap + 1));
+    double *eta = calloc(m, sizeof(double)), *zeta = malloc(sizeof(double) * m);
+    char *done = calloc(m, 1);
+    int launches = 0, rc = HBICG_OK;
+#define PL(call)                                                                                         \
+    do {                                                                                                 \
+        launches++;                                                                                      \
+        int e_ = (call);                                                                                 \
+        if (e_) {                                                                                        \
+            set_msg("%s: %s", #call, hbk_error_string(e_));                                              \
+            rc = HBICG_E_CUDA;                                                                           \
+            goto out;                                                                                    \
+        }                                                                                                \
+    } while (0)
+#define PD(x, y, res)                                                                                    \
+    do {                                                                                                 \
+        launches++;                                                                                      \
+        if ((rc = dev_dot(s, x, y, res))) goto out;                                                      \
+    } while (0)
+
+    double rr_hat, rr, bb, rs, qq, qy, rr_hat_old;
+    PL(hbk_copy(n, s->d_b, r, st));
+    PD(r, r, &rr_hat);
+    PL(hbk_copy(n, r, r_hat, st));
+    for (int j = 0; j < m; j++) {
+        PL(hbk_copy(n, r, v->P + (size_t)j * ld, st));
+        zeta[j] = 1.0;
+        pi[(size_t)j * kcap + 0] = 1.0;
+        if (kcap > 1) pi[(size_t)j * kcap + 1] = 1.0;
+    }
+    if (cudaMemsetAsync(v->X, 0, sizeof(double) * ld * (size_t)(m > 0 ? m : 1), st) != cudaSuccess) {
+        rc = HBICG_E_CUDA;
+        goto out;
+    }
+    rr = bb = rr_hat;
+    ah[0] = 1.0;
+    bh[0] = 0.0;
+    int k = 1, n_done = 0, argmax = seed;
+    if (bb == 0.0) n_done = m; /* x = 0 is exact */
+    while (n_done < m && k < kcap) {
+        double *ps = v->P + (size_t)seed * ld, *xs = v->X + (size_t)seed * ld;
+        const double sig_s = h_sigma[seed];
+        PL(hbk_copy(n, r, r_old, st));
+        PL(hbk_zero(n, sv, st));
+        PL(hbk_spmv_accumulate(A, ps, sv, st));
+        PL(hbk_axpy(n, sig_s, ps, sv, st));
+        PD(r_hat, sv, &rs);
+        ah[k] = rr_hat / rs;
+        const double ak = ah[k];
+        PL(hbk_axpy(n, -ak, sv, r, st));
+        PL(hbk_copy(n, r, qc, st));
+        PL(hbk_zero(n, y, st));
+        PL(hbk_spmv_accumulate(A, r, y, st));
+        PL(hbk_axpy(n, sig_s, r, y, st));
+        PD(r, r, &qq);
+        PD(r, y, &qy);
+        wh[k] = qq / qy;
+        rr_hat_old = rr_hat;
+        const double wk = wh[k];
+        PL(hbk_axpy(n, ak, ps, xs, st));
+        PL(hbk_axpy(n, wk, r, xs, st));
+        PL(hbk_axpy(n, -wk, y, r, st));
+        PD(r, r, &rr);
+        PD(r_hat, r, &rr_hat);
+        bh[k] = (ah[k] / wh[k]) * (rr_hat / rr_hat_old);
+        const double bk = bh[k];
+        if (!isfinite(ak) || !isfinite(wk) || !isfinite(bk) || wk == 0.0) {
+            rc = HBICG_E_BREAKDOWN;
+            o->status = HBICG_E_BREAKDOWN;
+            break;
+        }
+        PL(hbk_scal(n, bk, ps, st));
+        PL(hbk_axpy(n, 1.0, r, ps, st));
+        PL(hbk_axpy(n, -bk * wk, sv, ps, st));
+        const double c_prev = (bh[k - 1] / ah[k - 1]) * ak;
+        int active = 0;
+        for (int j = 0; j < m; j++) {
+            if (j == seed || done[j]) continue;
+            active++;
+            double *pij = pi + (size_t)j * kcap;
+            double *xj = v->X + (size_t)j * ld, *pj = v->P + (size_t)j * ld;
+            const double d = sig_s - h_sigma[j];
+            eta[j] = c_prev * eta[j] - d * ak * pij[k - 1];
+            pij[k] = eta[j] + pij[k - 1];
+            const double aj = (pij[k - 1] / pij[k]) * ak;
+            const double wj = wk / (1.0 - wk * d);
+            PL(hbk_axpy(n, wj / (pij[k] * zeta[j]), qc, xj, st));
+            PL(hbk_axpy(n, aj, pj, xj, st));
+            PL(hbk_axpy(n, wj / (aj * zeta[j] * pij[k]), qc, pj, st));
+            PL(hbk_axpy(n, -wj / (aj * zeta[j] * pij[k - 1]), r_old, pj, st));
+            zeta[j] = (1.0 - wk * d) * zeta[j];
+            const double bj = (pij[k - 1] / pij[k]) * (pij[k - 1] / pij[k]) * bk;
+            PL(hbk_scal(n, bj, pj, st));
+            PL(hbk_axpy(n, 1.0 / (pij[k] * zeta[j]), r, pj, st));
+        }
+        if (o->act && k < kcap) o->act[k] = active;
+        double best = 1.0;
+        for (int j = 0; j < m; j++) {
+            if (done[j]) continue;
+            const double a = (j == seed) ? 1.0 : fabs(1.0 / (zeta[j] * pi[(size_t)j * kcap + k]));
+            if (a * a * rr <= tol * tol * bb) {
+                done[j] = 1;
+                n_done++;
+                if (o->conv_k) o->conv_k[j] = k;
+            } else if (a > best) {
+                best = a;
+                argmax = j;
+            }
+        }
+        if (s->p.switching && done[seed] && n_done < m) {
+            const int t = argmax;
+            const double *pit = pi + (size_t)t * kcap;
+            const double dst = h_sigma[seed] - h_sigma[t];
+            for (int i = 1; i <= k; i++) {
+                ah[i] = (pit[i - 1] / pit[i]) * ah[i];
+                bh[i] = (pit[i - 1] / pit[i]) * (pit[i - 1] / pit[i]) * bh[i];
+                wh[i] = wh[i] / (1.0 - wh[i] * dst);
+            }
+            PL(hbk_scal(n, 1.0 / (zeta[t] * pit[k]), r, st));
+            PD(r_hat, r, &rr_hat);
+            for (int j = 0; j < m; j++) {
+                eta[j] = 0.0;
+                zeta[j] = 1.0;
+            }
+            for (int i = 1; i <= k; i++) {
+                for (int j = 0; j < m; j++) {
+                    if (done[j] || j == t) continue;
+                    double *pij = pi + (size_t)j * kcap;
+                    const double d = h_sigma[t] - h_sigma[j];
+                    eta[j] = (bh[i - 1] / ah[i - 1]) * ah[i] * eta[j] - d * ah[i] * pij[i - 1];
+                    pij[i] = eta[j] + pij[i - 1];
+                    zeta[j] = (1.0 - wh[i] * d) * zeta[j];
+                }
+            }
+            seed = t;
+            if (o->n_sw < m) {
+                if (o->sw_k) o->sw_k[o->n_sw] = k;
+                if (o->sw_seed) o->sw_seed[o->n_sw] = t;
+            }
+            o->n_sw++;
+        }
+        k++;
+    }
+    o->k = k;
+    o->final_seed = seed;
+out:
+    o->launches = launches;
+    free(ah); free(bh); free(wh); free(pi); free(eta); free(zeta); free(done);
+    return rc;
+#undef PL
+#undef PD
+}
+
+/* ------------------------------------------------------------------------ */
+/* fused form */
+
+static int capture_graph(hbicg_solver *s) {
+    cudaStream_t st = s->ctx->stream;
+    cudaGraph_t g;
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < s->chunk; i++) {
+        int e = hbk_fused_iteration(&s->A->k, &s->v, &s->sh, st);
+        if (e) {
+            cudaStreamEndCapture(st, &g);
+            set_msg("capture: %s", hbk_error_string(e));
+            return HBICG_E_CUDA;
+        }
+    }
+    CUDA_TRY(cudaStreamEndCapture(st, &g));
+    CUDA_TRY(cudaGraphInstantiate(&s->graph, g, 0));
+    cudaGraphDestroy(g);
+    return HBICG_OK;
+}
+
+static int ensure_pmat(hbicg_solver *s) {
+    if (s->v.Pmat) return HBICG_OK;
+    const int mm = s->m > 0 ? s->m : 1;
+    CUDA_TRY(cudaMalloc((void **)&s->v.Pmat, sizeof(double) * s->ld * (size_t)mm));
+    CUDA_TRY(cudaMemsetAsync(s->v.Pmat, 0, sizeof(double) * s->ld * (size_t)mm, s->ctx->stream));
+    /* the graphs captured the old (null) Pmat pointer: capture again */
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = NULL;
+    }
+    return HBICG_OK;
+}
+
+static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes) {
+    cudaStream_t st = s->ctx->stream;
+    hbk_scalars *h = s->ctx->h_sc;
+    HBK_TRY(hbk_fused_init(&s->A->k, &s->v, &s->sh, s->d_b, seed, s->p.tol, st));
+    /* switching flag lives in the device scalars */
+    int sw = s->p.switching ? 1 : 0;
+    CUDA_TRY(cudaMemcpyAsync(&s->d_sc->switching, &sw, sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    *launches += 6 + (s->v.deferred ? 1 : s->m);
+    const int use_graph = s->p.use_graph;
+    /* every launch of a chunk advances k by chunk unless the solve ends or
+     * the basis pauses it; bound the host loop all the same */
+    long guard = 0;
+    const long guard_max = 4L * s->kcap / s->chunk + 64;
+    for (;;) {
+        if (++guard > guard_max) {
+            set_msg("fused loop made no progress after %ld chunks", guard_max);
+            return HBICG_E_TIMEOUT;
+        }
+        if (use_graph) {
+            if (!s->graph) {
+                int rc = capture_graph(s);
+                if (rc) return rc;
+            }
+            CUDA_TRY(cudaGraphLaunch(s->graph, st));
+        } else {
+            for (int i = 0; i < s->chunk; i++) HBK_TRY(hbk_fused_iteration(&s->A->k, &s->v, &s->sh, st));
+        }
+        *launches += s->chunk * s->launches_per_iter;
+        CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if (!h->finished) continue;
+        if ((h->status & HBK_ST_BASIS_FULL) && !(h->status & HBK_ST_BREAKDOWN)) {
+            int rc = ensure_pmat(s);
+            if (rc) return rc;
+            HBK_TRY(hbk_deferred_flush(&s->v, &s->sh, 1, st));
+            *launches += 3;
+            (*flushes)++;
+            continue;
+        }
+        break;
+    }
+    if (s->v.deferred) {
+        HBK_TRY(hbk_deferred_flush(&s->v, &s->sh, 0, st));
+        *launches += 2;
+    }
+    CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return HBICG_OK;
+}
+
+/* compulsory HBM bytes of the fused schedule for one solve */
+static double algorithmic_bytes(const hbicg_solver *s, int k_end, const int *act) {
+    const double n = s->A->k.n, nnz = s->A->k.nnz;
+    const double spmv = 12.0 * nnz + 4.0 * (n + 1) + 16.0 * n;
+    double tot = 0.0;
+    for (int k = 1; k < k_end; k++) {
+        const double ma = act ? act[k] : 0;
+        if (s->mode == HBICG_SHIFTS_DEFERRED) tot += 2.0 * spmv + 8.0 * n * 13.0;
+        else tot += 2.0 * spmv + 8.0 * n * 17.0 + 32.0 * n * ma;
+    }
+    if (s->mode == HBICG_SHIFTS_DEFERRED) tot += 8.0 * n * (2.0 * (k_end - 1) + 1.0) + 8.0 * n * s->m;
+    return tot;
+}
+
+int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int seed, int in_where, double *x,
+                     double *r_out, int out_where, hbicg_stats *stats) {
+    hbicg_context *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    const unsigned n = s->A->k.n;
+    const int m = s->m;
+    if (m > 0 && (seed < 0 || seed >= m)) {
+        set_msg("seed %d out of range [0, %d)", seed, m);
+        return HBICG_E_ARG;
+    }
+    const enum cudaMemcpyKind kin = in_where == HBICG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const enum cudaMemcpyKind kout = out_where == HBICG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    double *h_sigma = malloc(sizeof(double) * (m > 0 ? m : 1));
+    int *act = calloc((size_t)s->kcap + 1, sizeof(int));
+    if (m > 0) {
+        if (in_where == HBICG_DEVICE) CUDA_TRY(cudaMemcpyAsync(h_sigma, sigma, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+        else memcpy(h_sigma, sigma, sizeof(double) * m);
+        CUDA_TRY(cudaMemcpyAsync(s->d_sigma, sigma, sizeof(double) * m, kin, st));
+    }
+    CUDA_TRY(cudaMemcpyAsync(s->d_b, b, sizeof(double) * n, kin, st));
+    CUDA_TRY(cudaEventRecord(ctx->ev0, st));
+    int rc = HBICG_OK, launches = 0, flushes = 0;
+    int k = 1, n_sw = 0, final_seed = seed, status = HBICG_OK;
+    int *sw_k = calloc(m > 0 ? m : 1, sizeof(int)), *sw_seed = calloc(m > 0 ? m : 1, sizeof(int));
+    int *conv = calloc(m > 0 ? m : 1, sizeof(int));
+    const double *r_final = NULL;
+    if (s->p.form == HBICG_FORM_PLAIN) {
+        plain_out o;
+        memset(&o, 0, sizeof o);
+        o.sw_k = sw_k;
+        o.sw_seed = sw_seed;
+        o.conv_k = conv;
+        o.act = act;
+        rc = run_plain(s, h_sigma, seed, &o);
+        k = o.k;
+        n_sw = o.n_sw;
+        final_seed = o.final_seed;
+        launches = o.launches;
+        if (rc == HBICG_E_BREAKDOWN) {
+            status = rc;
+            rc = HBICG_OK;
+        }
+        r_final = s->d_r;
+    } else {
+        rc = run_fused(s, seed, &launches, &flushes);
+        if (rc == HBICG_OK) {
+            hbk_scalars *h = ctx->h_sc;
+            k = h->k;
+            n_sw = h->n_sw;
+            final_seed = h->seed;
+            if (h->status & HBK_ST_BREAKDOWN) status = HBICG_E_BREAKDOWN;
+            if (m > 0) {
+                CUDA_TRY(cudaMemcpyAsync(conv, s->sh.conv_k, sizeof(int) * m, cudaMemcpyDeviceToHost, st));
+                int nl = n_sw < m ? n_sw : m;
+                if (nl) {
+                    CUDA_TRY(cudaMemcpyAsync(sw_k, s->sh.sw_k, sizeof(int) * nl, cudaMemcpyDeviceToHost, st));
+                    CUDA_TRY(cudaMemcpyAsync(sw_seed, s->sh.sw_seed, sizeof(int) * nl, cudaMemcpyDeviceToHost, st));
+                }
+            }
+            CUDA_TRY(cudaMemcpyAsync(act, s->sh.act_hist, sizeof(int) * ((size_t)s->kcap + 1), cudaMemcpyDeviceToHost, st));
+            r_final = s->v.deferred ? s->v.V + (size_t)h->slot_r_old * s->ld : s->v.rbuf[(h->k - 1) & 1];
+        }
+    }
+    CUDA_TRY(cudaEventRecord(ctx->ev1, st));
+    if (rc == HBICG_OK && x && m > 0)
+        CUDA_TRY(cudaMemcpy2DAsync(x, sizeof(double) * n, s->v.X, sizeof(double) * s->ld, sizeof(double) * n, m, kout, st));
+    if (rc == HBICG_OK && r_out && r_final) CUDA_TRY(cudaMemcpyAsync(r_out, r_final, sizeof(double) * n, kout, st));
+    double maxres = 0.0;
+    double *h_res = NULL;
+    if (rc == HBICG_OK && s->p.true_residuals && m > 0) {
+        HBK_TRY(hbk_true_residuals(&s->A->k, s->v.X, s->d_b, s->d_sigma, m, s->sh.partials, s->sh.counters + 16,
+                                   s->d_res, st));
+        HBK_TRY(hbk_dot(n, s->d_b, s->d_b, s->sh.partials, s->sh.counters + 7, s->d_dot, st));
+        h_res = malloc(sizeof(double) * m);
+        CUDA_TRY(cudaMemcpyAsync(h_res, s->d_res, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(ctx->h_dbl, s->d_dot, sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (h_res) {
+        const double bn = sqrt(ctx->h_dbl[0]);
+        for (int j = 0; j < m; j++) {
+            h_res[j] = sqrt(h_res[j]) / bn;
+            if (h_res[j] > maxres || isnan(h_res[j])) maxres = h_res[j];
+        }
+    }
+    if (rc == HBICG_OK && status == HBICG_OK && k >= s->kcap && m > 0) {
+        int all = 1;
+        for (int j = 0; j < m; j++)
+            if (!conv[j]) all = 0;
+        if (!all) status = HBICG_E_MAXITER;
+    }
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        stats->k = k;
+        stats->status = rc ? rc : status;
+        stats->n_switches = n_sw;
+        stats->final_seed = final_seed;
+        stats->shift_mode = s->mode;
+        stats->basis_flushes = flushes;
+        stats->launches = launches;
+        stats->solve_ms = ms;
+        stats->max_true_residual = maxres;
+        stats->bytes_algorithmic = algorithmic_bytes(s, k, act);
+        int nl = n_sw < m ? n_sw : m;
+        if (stats->switch_k) memcpy(stats->switch_k, sw_k, sizeof(int) * nl);
+        if (stats->switch_seed) memcpy(stats->switch_seed, sw_seed, sizeof(int) * nl);
+        if (stats->conv_k && m > 0) memcpy(stats->conv_k, conv, sizeof(int) * m);
+        if (stats->active_per_iter) memcpy(stats->active_per_iter, act, sizeof(int) * ((size_t)s->kcap + 1));
+        if (stats->true_residual && h_res) memcpy(stats->true_residual, h_res, sizeof(double) * m);
+    }
+    free(h_res);
+    free(h_sigma);
+    free(act);
+    free(sw_k);
+    free(sw_seed);
+    free(conv);
+    if (rc) return rc;
+    return status;
+}
+
+int hbicg_solve(unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *col, const double *val,
+                const double *b, const double *sigma, int m, int seed, const hbicg_params *p, double *x,
+                double *r_out, hbicg_stats *stats) {
+    hbicg_context *ctx = NULL;
+    hbicg_matrix *A = NULL;
+    hbicg_solver *s = NULL;
+    int rc = hbicg_context_create(&ctx);
+    if (!rc) rc = hbicg_matrix_create(ctx, n, nnz, ptr, col, val, HBICG_HOST, &A);
+    if (!rc) rc = hbicg_solver_create(ctx, A, m, p, &s);
+    if (!rc) rc = hbicg_solver_run(s, b, sigma, seed, HBICG_HOST, x, r_out, HBICG_HOST, stats);
+    hbicg_solver_destroy(s);
+    hbicg_matrix_destroy(A);
+    hbicg_context_destroy(ctx);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* the reference's entry points (src/solver.h:33-35) */
+
+static double g_tol = EPS;
+static int g_maxit = MAX_ITER;
+static int g_switching = 1;
+
+void hbicg_dropin_config(double tol, int max_iter, int switching) {
+    g_tol = tol;
+    g_maxit = max_iter;
+    g_switching = switching;
+}
+
+/* A_loc_offd holds global column indices (src/matrix.c:387-389); on one rank
+ * it is empty.  A non-empty one is merged row by row after the diagonal
+ * block's entries. */
+static int merged_csr(const CSR_Matrix *d, const CSR_Matrix *o, unsigned **ptr, unsigned **col, double **val) {
+    const unsigned n = d->rows;
+    const unsigned nz = d->nz + o->nz;
+    *ptr = malloc(sizeof(unsigned) * ((size_t)n + 1));
+    *col = malloc(sizeof(unsigned) * ((size_t)nz + 1));
+    *val = malloc(sizeof(double) * ((size_t)nz + 1));
+    if (!*ptr || !*col || !*val) return HBICG_E_NOMEM;
+    unsigned e = 0;
+    (*ptr)[0] = 0;
+    for (unsigned i = 0; i < n; i++) {
+        for (unsigned a = d->ptr[i]; a < d->ptr[i + 1]; a++) {
+            (*col)[e] = d->col[a];
+            (*val)[e++] = d->val[a];
+        }
+        for (unsigned a = o->ptr[i]; a < o->ptr[i + 1]; a++) {
+            (*col)[e] = o->col[a];
+            (*val)[e++] = o->val[a];
+        }
+        (*ptr)[i + 1] = e;
+    }
+    return HBICG_OK;
+}
+
+static int dropin(CSR_Matrix *A_loc_diag, CSR_Matrix *A_loc_offd, INFO_Matrix *A_info, double *x_loc_set,
+                  double *r_loc, double *sigma, int sigma_len, int seed, int form, int use_graph) {
+    if (A_info->cols != A_info->rows) {
+        printf("Error: matrix is not square.\n");
+        exit(1);
+    }
+    hbicg_params p;
+    hbicg_params_default(&p);
+    p.tol = g_tol;
+    p.max_iter = g_maxit;
+    p.switching = g_switching;
+    p.form = form;
+    p.use_graph = use_graph;
+    const CSR_Matrix *A = A_loc_diag;
+    unsigned *ptr = A->ptr, *col = A->col;
+    double *val = A->val;
+    int merged = 0;
+    if (A_loc_offd && A_loc_offd->nz > 0 && A_loc_offd->ptr) {
+        int rc = merged_csr(A_loc_diag, A_loc_offd, &ptr, &col, &val);
+        if (rc) return -rc;
+        merged = 1;
+    }
+    hbicg_stats st;
+    memset(&st, 0, sizeof st);
+    const unsigned nz = ptr[A->rows];
+    int rc = hbicg_solve(A->rows, nz, ptr, col, val, r_loc, sigma, sigma_len, seed, &p, x_loc_set, r_loc, &st);
+    if (merged) {
+        free(ptr);
+        free(col);
+        free(val);
+    }
+    if (rc != HBICG_OK && rc != HBICG_E_MAXITER && rc != HBICG_E_BREAKDOWN) {
+        fprintf(stderr, "hbicg: %s (%s)\n", hbicg_status_string(rc), hbicg_last_message());
+        return -rc;
+    }
+    return st.k;
+}
+
+int shifted_lopbicg_dynamic(CSR_Matrix *A_loc_diag, CSR_Matrix *A_loc_offd, INFO_Matrix *A_info, double *x_loc_set,
+                            double *r_loc, double *sigma, int sigma_len, int seed) {
+    return dropin(A_loc_diag, A_loc_offd, A_info, x_loc_set, r_loc, sigma, sigma_len, seed, HBICG_FORM_FUSED, 1);
+}
+
+int shifted_lopbicg_static(CSR_Matrix *A_loc_diag, CSR_Matrix *A_loc_offd, INFO_Matrix *A_info, double *x_loc_set,
+                           double *r_loc, double *sigma, int sigma_len, int seed) {
+    return dropin(A_loc_diag, A_loc_offd, A_info, x_loc_set, r_loc, sigma, sigma_len, seed, HBICG_FORM_PLAIN, 0);
+}
+
+int shifted_lopbicg_normal(CSR_Matrix *A_loc_diag, CSR_Matrix *A_loc_offd, INFO_Matrix *A_info, double *x_loc_set,
+                           double *r_loc, double *sigma, int sigma_len, int seed) {
+    return dropin(A_loc_diag, A_loc_offd, A_info, x_loc_set, r_loc, sigma, sigma_len, seed, HBICG_FORM_FUSED, 0);
+}

@@ -1,0 +1,118 @@
+/* Extended C API of the GB300 shifted BiCGStab solver.
+ *
+ * The reference has no counterpart beyond its three solver entry points
+ * (src/solver.h:33-35); this API adds what a library needs around them:
+ * run-time parameters instead of compile-time constants (src/solver.h:13-31),
+ * status codes instead of exit() (src/solver_dynamic.c:11-14), per-solve
+ * statistics (switch log, per-shift convergence iteration, true residuals,
+ * timings), device-pointer entry points that keep inputs resident in HBM, and
+ * a matrix/solver split so the device CSR, the SpMV schedule, the workspace
+ * and the captured CUDA graphs are built once and reused.
+ *
+ * Threading: one hbicg_context per host thread (each owns a CUDA stream).
+ */
+#ifndef HBICG_H
+#define HBICG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    HBICG_OK = 0,
+    HBICG_E_NOT_SQUARE = 1,
+    HBICG_E_NO_DIAG = 2,
+    HBICG_E_BREAKDOWN = 3, /* (r^,s), (q,y) or a shift denominator became 0, inf or nan */
+    HBICG_E_MAXITER = 4,   /* some shift did not converge within max_iter */
+    HBICG_E_CUDA = 5,
+    HBICG_E_TIMEOUT = 6,
+    HBICG_E_ARG = 7,
+    HBICG_E_NOMEM = 8,
+    HBICG_E_IO = 9
+} hbicg_status;
+
+typedef enum { HBICG_FORM_PLAIN = 0, HBICG_FORM_FUSED = 1 } hbicg_form;
+
+typedef enum {
+    HBICG_SHIFTS_AUTO = 0,
+    HBICG_SHIFTS_INCREMENTAL = 1, /* x_j, p_j updated every iteration by one multi-shift kernel */
+    HBICG_SHIFTS_DEFERRED = 2     /* x_j, p_j kept as coefficients over the seed's Krylov basis */
+} hbicg_shift_mode;
+
+typedef enum { HBICG_HOST = 0, HBICG_DEVICE = 1 } hbicg_memory;
+
+typedef struct {
+    double tol;            /* relative tolerance on the recursive residual (default 1e-12) */
+    int max_iter;          /* default 2000; the loop runs while k < max_iter + 1 */
+    int switching;         /* 1 = seed switching (default) */
+    int form;              /* hbicg_form, default FUSED */
+    int shift_mode;        /* hbicg_shift_mode, default AUTO */
+    int use_graph;         /* fused form: capture iterations in CUDA graphs (default 1) */
+    int graph_chunk;       /* iterations per graph launch, 0 = automatic */
+    double basis_mem_frac; /* deferred mode: share of free device memory for the basis (default 0.6) */
+    int true_residuals;    /* compute ||b-(A+sigma_j I)x_j||/||b|| after the solve (default 0) */
+} hbicg_params;
+
+typedef struct {
+    int k;                    /* the reference's return value: iterations + 1 on convergence */
+    int status;               /* hbicg_status */
+    int n_switches;
+    int final_seed;
+    int shift_mode;           /* mode actually used */
+    int basis_flushes;        /* deferred mode: basis flushes during the solve */
+    int launches;             /* kernel launches issued for the solve */
+    double solve_ms;          /* device time of init + iterations + final flush (CUDA events) */
+    double max_true_residual; /* when params.true_residuals */
+    double bytes_algorithmic; /* compulsory HBM bytes of the fused schedule for this solve */
+    /* optional caller-owned outputs (NULL to skip) */
+    int *switch_k;            /* [m] iteration of each switch */
+    int *switch_seed;         /* [m] seed chosen at each switch */
+    int *conv_k;              /* [m] iteration at which each shift met the test (0 = never) */
+    int *active_per_iter;     /* [max_iter + 1] non-seed shifts updated at iteration k */
+    double *true_residual;    /* [m] */
+} hbicg_stats;
+
+typedef struct hbicg_context hbicg_context;
+typedef struct hbicg_matrix hbicg_matrix;
+typedef struct hbicg_solver hbicg_solver;
+
+void hbicg_params_default(hbicg_params *p);
+const char *hbicg_status_string(int status);
+/* message of the last failure in this thread (CUDA error text, argument) */
+const char *hbicg_last_message(void);
+
+int hbicg_context_create(hbicg_context **ctx);
+void hbicg_context_destroy(hbicg_context *ctx);
+/* the context's CUDA stream (cudaStream_t) */
+void *hbicg_context_stream(hbicg_context *ctx);
+
+/* Square CSR with 32-bit indices; `where` says whether ptr/col/val are host or
+ * device pointers (device arrays are used in place, host arrays are copied). */
+int hbicg_matrix_create(hbicg_context *ctx, unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *col,
+                        const double *val, int where, hbicg_matrix **out);
+void hbicg_matrix_destroy(hbicg_matrix *A);
+unsigned hbicg_matrix_rows(const hbicg_matrix *A);
+unsigned long long hbicg_matrix_nnz(const hbicg_matrix *A);
+/* y = A x (+ sigma x); x, y device or host per `where` */
+int hbicg_matrix_spmv(hbicg_matrix *A, const double *x, double *y, double sigma, int where);
+
+/* Workspace for families of m shifts on A (device vectors, scalar state, graphs). */
+int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_params *p, hbicg_solver **out);
+void hbicg_solver_destroy(hbicg_solver *s);
+/* Solve.  b [n], sigma [m] and x [m*n, shift-major, leading dimension n] are
+ * host or device pointers per in_where / out_where; r_out [n] (optional)
+ * receives the final seed residual.  Returns hbicg_status; stats optional. */
+int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int seed, int in_where, double *x,
+                     double *r_out, int out_where, hbicg_stats *stats);
+
+/* One-call form with host pointers (creates and frees everything). */
+int hbicg_solve(unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *col, const double *val,
+                const double *b, const double *sigma, int m, int seed, const hbicg_params *p, double *x,
+                double *r_out, hbicg_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HBICG_H */

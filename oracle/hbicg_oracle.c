@@ -99,6 +99,20 @@ void hbo_spmv(unsigned n, const unsigned *ptr, const unsigned *col, const double
     }
 }
 
+/* The same row sums with every step a fused multiply-add (C99 fma, exact on
+ * any host): acc = fma(val, x, acc) from acc = 0 in stored order.  This is
+ * what a row loop compiled with contraction computes, and what the GPU SpMV
+ * kernel computes per row. */
+void hbo_spmv_fma(unsigned n, const unsigned *ptr, const unsigned *col, const double *val, const double *x,
+                  double *y) {
+#pragma omp parallel for
+    for (long i = 0; i < (long)n; i++) {
+        double acc = 0.0;
+        for (unsigned e = ptr[i]; e < ptr[i + 1]; e++) acc = fma(val[e], x[col[e]], acc);
+        y[i] = acc;
+    }
+}
+
 /* ---- the solver ----------------------------------------------------------- */
 
 /* Per-shift scalar state.  pi holds the whole history pi_j[0..max_iter] of

@@ -44,6 +44,10 @@ typedef struct {
 void hbo_spmv(unsigned n, const unsigned *ptr, const unsigned *col, const double *val, const double *x,
               double *y);
 
+/* y = A x with each row accumulated by fused multiply-adds in stored order. */
+void hbo_spmv_fma(unsigned n, const unsigned *ptr, const unsigned *col, const double *val, const double *x,
+                  double *y);
+
 /* Shifted BiCGStab with seed switching on (A + sigma_j I) x_j = b.
  * x: m*n doubles, shift-major, zero on entry.  r: b on entry, the final seed
  * residual on exit.  Returns k (iterations + 1 on convergence), exactly as the

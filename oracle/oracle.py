@@ -75,6 +75,7 @@ def lib():
         _lib.hbo_shifted_bicgstab.argtypes = [C.c_uint, _PU, _PU, _PD, _PD, _PD, _PD, C.c_int, C.c_int,
                                               C.POINTER(_Opts), C.POINTER(_Trace)]
         _lib.hbo_spmv.argtypes = [C.c_uint, _PU, _PU, _PD, _PD, _PD]
+        _lib.hbo_spmv_fma.argtypes = [C.c_uint, _PU, _PU, _PD, _PD, _PD]
         _lib.hbo_true_residuals.argtypes = [C.c_uint, _PU, _PU, _PD, _PD, _PD, _PD, C.c_int, _PD]
     return _lib
 
@@ -154,6 +155,15 @@ def spmv(a, x) -> np.ndarray:
     xx = np.ascontiguousarray(x, dtype=np.float64)
     y = np.zeros(a.n)
     lib().hbo_spmv(a.n, _p(ptr, _PU), _p(col, _PU), _p(val, _PD), _p(xx, _PD), _p(y, _PD))
+    return y
+
+
+def spmv_fma(a, x) -> np.ndarray:
+    """Row sums as fused multiply-adds in stored order (the GPU kernel's order)."""
+    ptr, col, val = _csr(a)
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros(a.n)
+    lib().hbo_spmv_fma(a.n, _p(ptr, _PU), _p(col, _PU), _p(val, _PD), _p(xx, _PD), _p(y, _PD))
     return y
 
 

@@ -1,0 +1,139 @@
+"""Solver parity on the GPU against the oracle and the reference's golden
+vectors.  Tolerances (FP64): solutions within 1e-8 relative to max|x| of the
+reference's answers; iteration counts within 2% (at least one iteration);
+seed-switch sequences identical; every shift's true relative residual within
+the tolerance (1e-3 relative slack: the test is on the recursive residual, as
+in the reference)."""
+import numpy as np
+import pytest
+
+from conftest import GoldenCsr, golden
+
+pytestmark = pytest.mark.gpu
+
+X_RTOL = 1e-8
+MODES = [
+    dict(form="plain"),
+    dict(form="fused", shift_mode="incremental"),
+    dict(form="fused", shift_mode="deferred"),
+    dict(form="fused", shift_mode="incremental", use_graph=False),
+    dict(form="fused", shift_mode="deferred", use_graph=False),
+]
+MODE_IDS = ["plain", "fused-inc", "fused-def", "fused-inc-eager", "fused-def-eager"]
+
+
+def k_close(k, want):
+    return abs(k - want) <= max(1, int(0.02 * want))
+
+
+def x_err(x, want):
+    return np.max(np.abs(x - want)) / max(np.max(np.abs(want)), 1e-300)
+
+
+GOLDEN_CASES = ["stencil8_seed0", "stencil8_seed5", "stencil8_maxiter5", "stencil8_single_shift",
+                "irregular_two_switches", "irregular_fixed_seed", "stencil2d_seed8"]
+
+
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_golden(cuda, pkg, name, mode):
+    g = golden(name)
+    a = GoldenCsr(g)
+    res = pkg.solve(a, g["b"], g["sigma"], seed=int(g["seed"]), tol=float(g["tol"]), max_iter=int(g["max_iter"]),
+                    switching=bool(g["switching"]), **mode)
+    assert k_close(res.k, int(g["k"])), (res.k, int(g["k"]))
+    assert res.switches == [tuple(map(int, s)) for s in g["switches"]]
+    if name == "stencil8_maxiter5":
+        assert res.k == 6
+    assert x_err(res.x, g["x"]) < X_RTOL
+
+
+@pytest.mark.parametrize("seed", [0, 15])
+@pytest.mark.parametrize("mode", MODES[:3], ids=MODE_IDS[:3])
+def test_c1_full(cuda, pkg, oracle, seed, mode):
+    f = pkg.workloads.family("c1")
+    want = oracle.solve(f.a, f.b, f.sigma, seed=seed, tol=f.tol, max_iter=f.max_iter)
+    res = pkg.solve(f.a, f.b, f.sigma, seed=seed, tol=f.tol, max_iter=f.max_iter, true_residuals=True, **mode)
+    assert k_close(res.k, want.k)
+    assert res.switches == want.switches
+    assert x_err(res.x, want.x) < X_RTOL
+    assert res.max_true_residual <= f.tol * (1 + 1e-3)
+    tr = oracle.true_residuals(f.a, res.x, f.b, f.sigma)
+    assert np.allclose(tr, res.true_residual, rtol=1e-6, atol=1e-16)
+    assert np.array_equal(res.conv_k, want.conv_k)
+
+
+def test_dense_direct_solve(cuda, pkg):
+    a = pkg.workloads.stencil_cd3d(16)
+    b = np.random.default_rng(11).standard_normal(a.n)
+    sigma = np.array([1e-3, 0.01, 0.1, 0.5, 1.0])
+    res = pkg.solve(a, b, sigma, seed=0, tol=1e-13, max_iter=3000)
+    dense = a.to_dense()
+    for j, s in enumerate(sigma):
+        xd = np.linalg.solve(dense + s * np.eye(a.n), b)
+        assert x_err(res.x[j], xd) < 1e-9
+
+
+@pytest.mark.parametrize("variant", ["dynamic", "static", "normal"])
+def test_dropin_entry_points(cuda, pkg, oracle, variant):
+    g = golden("stencil8_seed5")
+    a = GoldenCsr(g)
+    k, x, r = pkg.dropin_solve(variant, a, g["b"], g["sigma"], seed=5, tol=1e-10, max_iter=10000)
+    assert k_close(k, int(g["k"]))
+    assert x_err(x, g["x"]) < X_RTOL
+    bn = np.linalg.norm(g["b"])
+    assert np.linalg.norm(r - g["r"]) / bn < 1e-9  # final seed residual, overwritten like r_loc
+
+
+def test_dropin_defaults_are_reference_constants(cuda, pkg, oracle):
+    f = pkg.workloads.family("c1", scale=10)
+    k, x, _ = pkg.dropin_solve("dynamic", f.a, f.b, f.sigma[:4], seed=0)  # EPS 1e-12, MAX_ITER 2000
+    want = oracle.solve(f.a, f.b, f.sigma[:4], seed=0, tol=1e-12, max_iter=2000)
+    assert k_close(k, want.k) and x_err(x, want.x) < X_RTOL
+
+
+def test_zero_rhs(cuda, pkg):
+    a = pkg.workloads.stencil_cd3d(6)
+    res = pkg.solve(a, np.zeros(a.n), np.array([0.0, 0.5]), seed=0, tol=1e-10, max_iter=100)
+    assert res.k == 1 and np.all(res.x == 0.0) and res.status == 0
+
+
+@pytest.mark.parametrize("mode", ["incremental", "deferred"])
+def test_fixed_seed_matches_reference_fixed_seed(cuda, pkg, mode):
+    g = golden("irregular_fixed_seed")
+    res = pkg.solve(GoldenCsr(g), g["b"], g["sigma"], seed=int(g["seed"]), tol=1e-10, max_iter=3000,
+                    switching=False, shift_mode=mode)
+    assert k_close(res.k, int(g["k"])) and res.switches == []
+    assert x_err(res.x, g["x"]) < X_RTOL
+
+
+def test_deferred_basis_flushes(cuda, pkg, oracle):
+    f = pkg.workloads.family("c1", scale=20)
+    want = oracle.solve(f.a, f.b, f.sigma, seed=15, tol=f.tol, max_iter=f.max_iter)
+    # a basis of a few dozen slots forces several flushes during the solve
+    res = pkg.solve(f.a, f.b, f.sigma, seed=15, tol=f.tol, max_iter=f.max_iter, shift_mode="deferred",
+                    basis_mem_frac=1e-5, true_residuals=True)
+    assert res.flushes >= 1
+    assert k_close(res.k, want.k) and res.switches == want.switches
+    assert x_err(res.x, want.x) < X_RTOL
+    assert res.max_true_residual <= f.tol * (1 + 1e-3)
+
+
+def test_solver_reuse_device_pointers(cuda, pkg, oracle):
+    torch = cuda
+    f = pkg.workloads.family("c1", scale=12)
+    ctx = pkg.Context()
+    A = pkg.Matrix(ctx, f.a.ptr, f.a.col, f.a.val)
+    s = pkg.Solver(A, len(f.sigma), tol=f.tol, max_iter=f.max_iter)
+    want = oracle.solve(f.a, f.b, f.sigma, seed=3, tol=f.tol, max_iter=f.max_iter)
+    b = torch.tensor(f.b, device="cuda")
+    sig = torch.tensor(f.sigma, device="cuda")
+    x = torch.zeros((len(f.sigma), f.a.n), dtype=torch.float64, device="cuda")
+    for _ in range(2):  # graphs are captured once and replayed
+        res = s.run(b, sig, seed=3, x=x)
+        torch.cuda.synchronize()
+        assert k_close(res.k, want.k) and res.switches == want.switches
+        assert x_err(x.cpu().numpy(), want.x) < X_RTOL
+    s.close()
+    A.close()
+    ctx.close()
