@@ -53,6 +53,15 @@ def solver_cases(wl):
     seed = int(rng.integers(0, m))
     cases.append(("irregular_two_switches", a_irr, b, sig, seed, 1e-10, 3000, "dynamic", True))
     cases.append(("irregular_fixed_seed", a_irr, b, sig, seed, 1e-10, 3000, "dynamic", False))
+    # two seed switches that survive 1e-14 relative perturbations of b (seeded
+    # search); the case above is chaotic: its switch points move under rounding
+    rng = np.random.default_rng(1060)
+    a_r = wl.stencil_cd2d(int(rng.integers(8, 24)))
+    m = int(rng.integers(4, 10))
+    sig = rng.uniform(-0.5, 2.0, m)
+    b = rng.standard_normal(a_r.n)
+    seed = int(rng.integers(0, m))
+    cases.append(("stencil2d_two_switches", a_r, b, sig, seed, 1e-10, 2000, "dynamic", True))
     a2 = wl.stencil_cd2d(12)
     rng2 = np.random.default_rng(7)
     b2 = rng2.standard_normal(a2.n)

@@ -6,7 +6,7 @@ import pytest
 
 from conftest import GOLDEN, GoldenCsr, golden
 
-SOLVER_CASES = ["stencil8_seed0", "stencil8_seed5", "stencil8_seed5_static", "stencil8_seed5_normal",
+SOLVER_CASES = ["stencil8_seed0", "stencil8_seed5", "stencil8_seed5_static", "stencil8_seed5_normal", "stencil2d_two_switches",
                 "stencil8_maxiter5", "stencil8_single_shift", "irregular_two_switches", "irregular_fixed_seed",
                 "stencil2d_seed8"]
 
