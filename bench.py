@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""Benchmark of the shifted BiCGStab solve on one GB300 (one JSON line).
+
+Workload (default): the 256^3 convection-diffusion family — n = 16,777,216,
+nnz = 117,047,296, 64 shifts geometric in [1e-4, 1], b ~ N(0,1) normalised,
+tol 1e-10 on every shift, seed 0, dynamic seed switching.  Synthetic and
+seeded (the reference ships no matrices).
+
+A step is one complete solve of the family.  `value` is the time per step (s)
+with matrix, b and sigma already resident in HBM; `e2e` is the same solve
+through the reference-facing C ABI (shifted_lopbicg_dynamic) from pinned host
+buffers, the matrix and b copied in and all 64 solutions copied out inside the
+timed region.  Every working set is far larger than the 129 MB L2, so no flush
+is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank solves its own copy of the family (replicas only:
+the solve does not shard across GPUs); the step time is the max over ranks.
+`--impl reference` times the reference's CPU solver (its C restatement, built
+in oracle/) on the host cores for a bounded sample and prints the same line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+import __graft_entry__ as graft  # noqa: E402
+
+METRIC = "time-to-solution, all shifts @1e-10 true rel. residual; SpMV HBM GB/s vs peak"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------- distributed
+class Dist:
+    """Replica bookkeeping: barrier and max/sum reductions over ranks."""
+
+    def __init__(self, backend=None):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group(backend or ("nccl" if _cuda() else "gloo"))
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def reduce(self, value: float, op: str) -> float:
+        if not self.pg:
+            return value
+        import torch
+
+        dev = "cuda" if self.pg.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([value], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX if op == "max" else self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def aggregate(dist: Dist, step_s: float, units: float):
+    """Whole-job step time (max over ranks) and units processed by all ranks."""
+    return dist.reduce(step_s, "max"), dist.reduce(units, "sum")
+
+
+def _cuda():
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+# ------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        mhz, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                mhz.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(mhz)) if mhz else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+# ------------------------------------------------------------- workload
+def workload(name: str, scale):
+    pkg = graft.load_package()
+    return pkg, pkg.workloads.family(name, scale)
+
+
+def spmv_bytes(n: int, nnz: int) -> float:
+    """Compulsory HBM bytes of one y = (A + sigma I) x: values and column
+    indices once (12 B per nonzero), row pointers once, x read once, y written
+    once (x's neighbours come from L2)."""
+    return 12.0 * nnz + 4.0 * (n + 1) + 16.0 * n
+
+
+# ------------------------------------------------------------- CPU baseline
+def cpu_baseline(f, threads: int | None = None):
+    """The reference's algorithm (its C restatement, oracle/) on the host cores,
+    bounded: (1) the seed system alone to convergence, timed, which also yields
+    the seed's scalar history; (2) every shift's convergence iteration replayed
+    from that history; (3) all shifts for a few iterations, timed, for the cost
+    of one shift update.  Estimate = seed time + per-shift time x the number of
+    shift updates the full solve performs."""
+    orc = graft.load_oracle()
+    orc.build(ref=False)
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    bb = float(f.b @ f.b)
+    t0 = time.perf_counter()
+    seed_run = orc.solve(f.a, f.b, f.sigma[f.seed:f.seed + 1], seed=0, tol=f.tol, max_iter=f.max_iter)
+    t_seed = time.perf_counter() - t0
+    k_iters = seed_run.k - 1
+    conv, act = orc.shift_profile(seed_run.hist, f.sigma, f.seed, f.tol, bb)
+    shift_updates = int(act.sum())
+    # all shifts for 1 and for 3 iterations: the difference is two steady
+    # iterations with every shift running (set-up cost cancels)
+    times = {}
+    for s_iters in (1, 3):
+        t0 = time.perf_counter()
+        orc.solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=s_iters)
+        times[s_iters] = time.perf_counter() - t0
+    t_iter_all = (times[3] - times[1]) / 2.0
+    t_iter_seed = t_seed / max(k_iters, 1)
+    per_shift = max(t_iter_all - t_iter_seed, 0.0) / max(len(f.sigma) - 1, 1)
+    est = t_seed + per_shift * shift_updates
+    sample = (f"seed system alone to convergence ({k_iters} iterations, {t_seed:.2f} s) + all {len(f.sigma)} "
+              f"shifts for 1 and 3 iterations ({times[1]:.2f} s, {times[3]:.2f} s); estimate = seed time + "
+              f"{per_shift * 1e3:.3f} ms per shift update x {shift_updates} shift updates replayed from the seed's "
+              f"scalar history")
+    return {"value": est, "unit": "s", "cores": cores, "kind": "port", "sample": sample,
+            "iterations": k_iters + 1, "shift_updates": shift_updates}
+
+
+# ------------------------------------------------------------- our arm
+def run_ours(args, dist: Dist):
+    import torch
+
+    torch.cuda.set_device(dist.local)
+    pkg, f = workload(args.workload, args.scale)
+    n, nnz, m = f.a.n, f.a.nnz, len(f.sigma)
+    form = "plain" if args.mode == "static" else "fused"
+    use_graph = args.mode != "normal"
+    kw = dict(tol=f.tol, max_iter=f.max_iter, form=form, shift_mode=args.shift_mode, use_graph=use_graph)
+    ctx = pkg.Context()
+    ptr = torch.from_numpy(f.a.ptr.astype(np.int32)).cuda()
+    col = torch.from_numpy(f.a.col.astype(np.int32)).cuda()
+    val = torch.from_numpy(f.a.val).cuda()
+    A = pkg.Matrix(ctx, ptr, col, val)
+    solver = pkg.Solver(A, m, **kw)
+    b = torch.from_numpy(f.b).cuda()
+    sig = torch.from_numpy(f.sigma).cuda()
+    x = torch.empty((m, n), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    for _ in range(args.warmup):
+        res = solver.run(b, sig, seed=f.seed, x=x)
+    torch.cuda.synchronize()
+    dist.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    flush_ms = 0.0
+    with Clocks(dist.local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            res = solver.run(b, sig, seed=f.seed, x=x)
+            launches += res.launches
+            flush_ms += res.flush_ms
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    dist.barrier()
+    step_s = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    step_max, units = aggregate(dist, step_s, 1.0)
+
+    # verification solve (not timed): every shift's true residual
+    ver = pkg.Solver(A, m, **{**kw, "true_residuals": True})
+    vres = ver.run(b, sig, seed=f.seed, x=x)
+    ver.close()
+
+    # SpMV kernel alone (same kernel as the solve's two products), CUDA events
+    xs = torch.randn(n, dtype=torch.float64, device="cuda")
+    ys = torch.empty_like(xs)
+    spmv_ms = A.time_spmv(xs, ys, float(f.sigma[0]), iters=20)
+    hbm, peak_kind = peaks()
+    sb = spmv_bytes(n, nnz)
+    spmv = {"bound": "hbm", "achieved": sb / (spmv_ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+            "frac": sb / (spmv_ms * 1e-3) / 1e9 / hbm, "traffic": None, "kernel": "k_spmv",
+            "bytes_per_launch": sb, "ms_per_launch": spmv_ms, "peak_kind": peak_kind}
+
+    # e2e through the reference-facing C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        h_ptr = torch.from_numpy(f.a.ptr).pin_memory()
+        h_col = torch.from_numpy(f.a.col).pin_memory()
+        h_val = torch.from_numpy(f.a.val).pin_memory()
+        h_b = torch.from_numpy(f.b).pin_memory()
+        h_sig = torch.from_numpy(f.sigma).pin_memory()
+        h_x = torch.empty((m, n), dtype=torch.float64).pin_memory()
+        h_r = torch.empty(n, dtype=torch.float64).pin_memory()
+        e2e_steps = max(1, min(args.steps, 2))
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            h_x.zero_()
+            h_r.copy_(h_b)
+            k = pkg.dropin_raw("dynamic", h_ptr, h_col, h_val, h_x, h_r, h_sig, f.seed, f.tol, f.max_iter)
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        e2e_max, _ = aggregate(dist, e2e_s, 1.0)
+        e2e = {"value": e2e_max, "unit": "s", "h2d_bytes_per_step": int(h_ptr.nbytes + h_col.nbytes + h_val.nbytes
+                                                                          + h_b.nbytes + h_sig.nbytes),
+               "d2h_bytes_per_step": int(h_x.nbytes + h_r.nbytes), "api": "shifted_lopbicg_dynamic", "k": int(k)}
+
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(f)
+
+    line = {
+        "metric": METRIC, "value": step_max, "unit": "s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_max * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator; the reference ships no matrices)",
+        "config": {"workload": f"{args.workload}: {f.a.n} rows, {f.a.nnz} nonzeros, 3-D 7-point convection-"
+                   f"diffusion, {m} shifts in [{f.sigma.min():g}, {f.sigma.max():g}], tol {f.tol:g}, seed {f.seed}",
+                   "mode": args.mode, "shift_mode": res.shift_mode, "parallelism": f"replicas x{dist.world}",
+                   "l2": "working set >> 129 MB L2 (no flush needed)"},
+        "iterations": res.k, "switches": res.switches, "max_true_residual": vres.max_true_residual,
+        "all_converged": bool(np.all(vres.conv_k > 0)),
+        "solve_breakdown_ms": {"flush": flush_ms / args.steps},
+        "roofline": spmv, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    solver.close()
+    A.close()
+    ctx.close()
+    return line
+
+
+def run_reference(args, dist: Dist):
+    """The reference's CPU path on the host cores (rank 0 only)."""
+    if dist.rank != 0:
+        return None
+    _, f = workload(args.workload, args.scale)
+    vals = []
+    info = None
+    for i in range(max(1, min(args.warmup, 1)) + args.steps):
+        info = cpu_baseline(f)
+        if i >= max(1, min(args.warmup, 1)):
+            vals.append(info["value"])
+    v = float(np.median(vals))
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "implementation": "reference algorithm, C restatement + OpenMP"},
+            "cpu_baseline": {**info, "value": v},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2")
+    ap.add_argument("--scale", type=int, default=None, help="grid side override (smaller case of the same shape)")
+    ap.add_argument("--mode", default="dynamic", choices=["dynamic", "static", "normal"])
+    ap.add_argument("--shift-mode", default="auto", choices=["auto", "incremental", "deferred"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    if args.impl == "ours" and args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    try:
+        line = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
+        if line is not None and dist.rank == 0:
+            print(json.dumps(line), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -68,7 +68,8 @@ class Params(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("k", C.c_int), ("status", C.c_int), ("n_switches", C.c_int), ("final_seed", C.c_int),
                 ("shift_mode", C.c_int), ("basis_flushes", C.c_int), ("launches", C.c_int),
-                ("solve_ms", C.c_double), ("max_true_residual", C.c_double), ("bytes_algorithmic", C.c_double),
+                ("solve_ms", C.c_double), ("flush_ms", C.c_double), ("max_true_residual", C.c_double),
+                ("bytes_algorithmic", C.c_double),
                 ("switch_k", _PI), ("switch_seed", _PI), ("conv_k", _PI), ("active_per_iter", _PI),
                 ("true_residual", _PD)]
 
@@ -95,6 +96,8 @@ def lib() -> C.CDLL:
                                           C.POINTER(C.c_void_p)]),
         "hbicg_matrix_destroy": (None, [C.c_void_p]),
         "hbicg_matrix_spmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
+        "hbicg_matrix_time_spmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
+                                             C.POINTER(C.c_double)]),
         "hbicg_solver_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(Params), C.POINTER(C.c_void_p)]),
         "hbicg_solver_destroy": (None, [C.c_void_p]),
         "hbicg_solver_run": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
@@ -167,6 +170,7 @@ class SolveResult:
     final_seed: int
     shift_mode: str
     solve_ms: float
+    flush_ms: float
     launches: int
     flushes: int
     bytes_algorithmic: float
@@ -201,6 +205,7 @@ def _result(st: Stats, bufs, m, x, r, want_res) -> SolveResult:
     return SolveResult(k=st.k, x=x, r=r, status=st.status, switches=sw, conv_k=bufs["conv_k"][:m].copy(),
                        active=bufs["active_per_iter"][:st.k + 1].copy(), final_seed=st.final_seed,
                        shift_mode={1: "incremental", 2: "deferred"}.get(st.shift_mode, "?"), solve_ms=st.solve_ms,
+                       flush_ms=st.flush_ms,
                        launches=st.launches, flushes=st.basis_flushes, bytes_algorithmic=st.bytes_algorithmic,
                        true_residual=bufs["true_residual"][:m].copy() if want_res else None)
 
@@ -272,6 +277,13 @@ class Matrix:
         where = HOST if isinstance(x, np.ndarray) else DEVICE
         _check(lib().hbicg_matrix_spmv(self.h, _ptr(x), _ptr(y), float(sigma), where), "hbicg_matrix_spmv")
         return y
+
+    def time_spmv(self, x, y, sigma: float = 0.0, iters: int = 20) -> float:
+        """Mean milliseconds per SpMV launch (device tensors), CUDA events on the context stream."""
+        ms = C.c_double()
+        _check(lib().hbicg_matrix_time_spmv(self.h, _ptr(x), _ptr(y), float(sigma), int(iters), C.byref(ms)),
+               "hbicg_matrix_time_spmv")
+        return ms.value
 
     def close(self):
         if self.h:
@@ -349,6 +361,29 @@ def dropin_solve(variant: str, a, b, sigma, seed=0, tol=1e-12, max_iter=2000, sw
            sig.ctypes.data_as(_PD), m, int(seed))
     L.hbicg_dropin_config(1e-12, 2000, 1)
     return k, x, r
+
+
+def dropin_raw(variant: str, ptr, col, val, x, r, sigma, seed=0, tol=1e-12, max_iter=2000, switching=True) -> int:
+    """shifted_lopbicg_<variant> on caller-owned host buffers (numpy arrays or
+    pinned torch CPU tensors, used in place): x [m, n] zero on entry, r = b on
+    entry and the final seed residual on exit.  Returns the reference's k."""
+    L = lib()
+    n = int(ptr.shape[0] - 1)
+    nz = int(col.shape[0])
+    m = int(sigma.shape[0])
+    diag = CSR_Matrix(C.cast(_ptr(val), _PD), C.cast(_ptr(col), _PU), C.cast(_ptr(ptr), _PU), nz, n, n)
+    optr = np.zeros(n + 1, dtype=np.uint32)
+    offd = CSR_Matrix(None, None, optr.ctypes.data_as(_PU), 0, n, n)
+    recv = (C.c_int * 1)(n)
+    displ = (C.c_int * 1)(0)
+    info = INFO_Matrix(nz, n, n, b"MCRG", C.cast(recv, _PI), C.cast(displ, _PI))
+    L.hbicg_dropin_config(float(tol), int(max_iter), 1 if switching else 0)
+    try:
+        fn = getattr(L, f"shifted_lopbicg_{variant}")
+        return fn(C.byref(diag), C.byref(offd), C.byref(info), C.cast(_ptr(x), _PD), C.cast(_ptr(r), _PD),
+                  C.cast(_ptr(sigma), _PD), m, int(seed))
+    finally:
+        L.hbicg_dropin_config(1e-12, 2000, 1)
 
 
 def mult(a, x, y=None) -> np.ndarray:

@@ -91,7 +91,7 @@ void hbicg_params_default(hbicg_params *p) {
 /* ------------------------------------------------------------------------ */
 struct hbicg_context {
     cudaStream_t stream;
-    cudaEvent_t ev0, ev1;
+    cudaEvent_t ev0, ev1, evf0, evf1;
     hbk_scalars *h_sc; /* pinned */
     double *h_dbl;     /* pinned scratch */
 };
@@ -102,6 +102,8 @@ int hbicg_context_create(hbicg_context **out) {
     CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreate(&c->ev0));
     CUDA_TRY(cudaEventCreate(&c->ev1));
+    CUDA_TRY(cudaEventCreate(&c->evf0));
+    CUDA_TRY(cudaEventCreate(&c->evf1));
     CUDA_TRY(cudaMallocHost((void **)&c->h_sc, sizeof(hbk_scalars)));
     CUDA_TRY(cudaMallocHost((void **)&c->h_dbl, sizeof(double) * 64));
     *out = c;
@@ -115,6 +117,8 @@ void hbicg_context_destroy(hbicg_context *c) {
     cudaFreeHost(c->h_dbl);
     cudaEventDestroy(c->ev0);
     cudaEventDestroy(c->ev1);
+    cudaEventDestroy(c->evf0);
+    cudaEventDestroy(c->evf1);
     cudaStreamDestroy(c->stream);
     free(c);
 }
@@ -224,6 +228,20 @@ int hbicg_matrix_spmv(hbicg_matrix *A, const double *x, double *y, double sigma,
     CUDA_TRY(cudaStreamSynchronize(st));
     cudaFree(dx);
     cudaFree(dy);
+    return HBICG_OK;
+}
+
+int hbicg_matrix_time_spmv(hbicg_matrix *A, const double *x, double *y, double sigma, int iters, double *ms) {
+    cudaStream_t st = A->ctx->stream;
+    if (iters < 1) iters = 1;
+    HBK_TRY(hbk_spmv(&A->k, x, y, sigma, sigma != 0.0, st)); /* warm */
+    CUDA_TRY(cudaEventRecord(A->ctx->ev0, st));
+    for (int i = 0; i < iters; i++) HBK_TRY(hbk_spmv(&A->k, x, y, sigma, sigma != 0.0, st));
+    CUDA_TRY(cudaEventRecord(A->ctx->ev1, st));
+    CUDA_TRY(cudaEventSynchronize(A->ctx->ev1));
+    float t = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t, A->ctx->ev0, A->ctx->ev1));
+    *ms = (double)t / iters;
     return HBICG_OK;
 }
 
@@ -629,7 +647,7 @@ static int ensure_pmat(hbicg_solver *s) {
     return HBICG_OK;
 }
 
-static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes) {
+static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, double *flush_ms) {
     cudaStream_t st = s->ctx->stream;
     hbk_scalars *h = s->ctx->h_sc;
     HBK_TRY(hbk_fused_init(&s->A->k, &s->v, &s->sh, s->d_b, seed, s->p.tol, st));
@@ -664,7 +682,13 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes) {
         if ((h->status & HBK_ST_BASIS_FULL) && !(h->status & HBK_ST_BREAKDOWN)) {
             int rc = ensure_pmat(s);
             if (rc) return rc;
+            float t = 0.f;
+            CUDA_TRY(cudaEventRecord(s->ctx->evf0, st));
             HBK_TRY(hbk_deferred_flush(&s->v, &s->sh, 1, st));
+            CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
+            CUDA_TRY(cudaEventSynchronize(s->ctx->evf1));
+            CUDA_TRY(cudaEventElapsedTime(&t, s->ctx->evf0, s->ctx->evf1));
+            *flush_ms += t;
             *launches += 3;
             (*flushes)++;
             continue;
@@ -672,8 +696,16 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes) {
         break;
     }
     if (s->v.deferred) {
+        float t = 0.f;
+        CUDA_TRY(cudaEventRecord(s->ctx->evf0, st));
         HBK_TRY(hbk_deferred_flush(&s->v, &s->sh, 0, st));
+        CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
         *launches += 2;
+        CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        CUDA_TRY(cudaEventElapsedTime(&t, s->ctx->evf0, s->ctx->evf1));
+        *flush_ms += t;
+        return HBICG_OK;
     }
     CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
@@ -716,6 +748,7 @@ int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int 
     CUDA_TRY(cudaMemcpyAsync(s->d_b, b, sizeof(double) * n, kin, st));
     CUDA_TRY(cudaEventRecord(ctx->ev0, st));
     int rc = HBICG_OK, launches = 0, flushes = 0;
+    double flush_ms = 0.0;
     int k = 1, n_sw = 0, final_seed = seed, status = HBICG_OK;
     int *sw_k = calloc(m > 0 ? m : 1, sizeof(int)), *sw_seed = calloc(m > 0 ? m : 1, sizeof(int));
     int *conv = calloc(m > 0 ? m : 1, sizeof(int));
@@ -738,7 +771,7 @@ int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int 
         }
         r_final = s->d_r;
     } else {
-        rc = run_fused(s, seed, &launches, &flushes);
+        rc = run_fused(s, seed, &launches, &flushes, &flush_ms);
         if (rc == HBICG_OK) {
             hbk_scalars *h = ctx->h_sc;
             k = h->k;
@@ -796,6 +829,7 @@ int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int 
         stats->basis_flushes = flushes;
         stats->launches = launches;
         stats->solve_ms = ms;
+        stats->flush_ms = flush_ms;
         stats->max_true_residual = maxres;
         stats->bytes_algorithmic = algorithmic_bytes(s, k, act);
         int nl = n_sw < m ? n_sw : m;

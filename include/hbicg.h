@@ -64,6 +64,7 @@ typedef struct {
     int basis_flushes;        /* deferred mode: basis flushes during the solve */
     int launches;             /* kernel launches issued for the solve */
     double solve_ms;          /* device time of init + iterations + final flush (CUDA events) */
+    double flush_ms;          /* deferred mode: device time of the basis flushes */
     double max_true_residual; /* when params.true_residuals */
     double bytes_algorithmic; /* compulsory HBM bytes of the fused schedule for this solve */
     /* optional caller-owned outputs (NULL to skip) */
@@ -97,6 +98,9 @@ unsigned hbicg_matrix_rows(const hbicg_matrix *A);
 unsigned long long hbicg_matrix_nnz(const hbicg_matrix *A);
 /* y = A x (+ sigma x); x, y device or host per `where` */
 int hbicg_matrix_spmv(hbicg_matrix *A, const double *x, double *y, double sigma, int where);
+/* Profiling helper: `iters` back-to-back launches of the SpMV kernel (device
+ * x, y) between CUDA events on the context's stream; *ms = mean per launch. */
+int hbicg_matrix_time_spmv(hbicg_matrix *A, const double *x, double *y, double sigma, int iters, double *ms);
 
 /* Workspace for families of m shifts on A (device vectors, scalar state, graphs). */
 int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_params *p, hbicg_solver **out);

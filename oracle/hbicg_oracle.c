@@ -283,6 +283,7 @@ int hbo_shifted_bicgstab(unsigned n, const unsigned *ptr, const unsigned *col, c
                     }
                 }
                 if (tr && tr->act && k < tr->act_cap) tr->act[k] = active;
+                if (tr && tr->rr_hist && k < tr->hist_cap) tr->rr_hist[k] = rr;
 
                 if (opt->switching && st.done[seed] && n_done < m) {
                     const int t = argmax;
@@ -323,7 +324,14 @@ int hbo_shifted_bicgstab(unsigned n, const unsigned *ptr, const unsigned *col, c
         }
     }
 
-    if (tr) tr->final_seed = seed;
+    if (tr) {
+        tr->final_seed = seed;
+        for (int i = 0; i < k && i < tr->hist_cap; i++) {
+            if (tr->a_hist) tr->a_hist[i] = st.a_hist[i];
+            if (tr->b_hist) tr->b_hist[i] = st.b_hist[i];
+            if (tr->w_hist) tr->w_hist[i] = i ? st.w_hist[i] : 0.0;
+        }
+    }
     free(r_prev); free(r_hat); free(s); free(y); free(q_keep); free(tmp); free(p);
     free(st.alpha); free(st.beta); free(st.omega); free(st.eta); free(st.zeta);
     free(st.a_hist); free(st.b_hist); free(st.w_hist); free(st.pi); free(st.done);

@@ -37,6 +37,11 @@ typedef struct {
     /* conv_k[j] = iteration at which shift j met the test (0 = never) */
     int *conv_k;
     int final_seed;
+    /* optional per-iteration histories, index k = 1..(returned k - 1), capacity
+     * hist_cap: the seed's alpha, beta, omega (as archived, i.e. rescaled after
+     * a switch) and (r, r) at the end of iteration k */
+    double *a_hist, *b_hist, *w_hist, *rr_hist;
+    int hist_cap;
 } hbo_trace;
 
 /* y = A x for a square CSR matrix (32-bit indices): each row summed in stored

@@ -42,7 +42,8 @@ class _Opts(C.Structure):
 
 class _Trace(C.Structure):
     _fields_ = [("sw_k", _PI), ("sw_seed", _PI), ("sw_cap", C.c_int), ("n_sw", C.c_int), ("act", _PI),
-                ("act_cap", C.c_int), ("conv_k", _PI), ("final_seed", C.c_int)]
+                ("act_cap", C.c_int), ("conv_k", _PI), ("final_seed", C.c_int), ("a_hist", _PD), ("b_hist", _PD),
+                ("w_hist", _PD), ("rr_hist", _PD), ("hist_cap", C.c_int)]
 
 
 @dataclass
@@ -54,6 +55,7 @@ class OracleResult:
     act: np.ndarray | None = None      # active non-seed shifts per iteration (index k)
     conv_k: np.ndarray | None = None   # iteration at which each shift converged
     final_seed: int | None = None
+    hist: dict | None = None           # seed alpha/beta/omega and (r,r) per iteration
 
 
 def _p(a, t):
@@ -120,12 +122,47 @@ def solve(a, b, sigma, seed=0, tol=1e-12, max_iter=2000, switching=True, schedul
     sws = np.zeros(cap, dtype=np.int32)
     act = np.zeros(max_iter + 2, dtype=np.int32)
     conv = np.zeros(max(m, 1), dtype=np.int32)
-    tr = _Trace(_p(swk, _PI), _p(sws, _PI), cap, 0, _p(act, _PI), act.shape[0], _p(conv, _PI), 0)
+    hist = {key: np.zeros(max_iter + 2) for key in ("alpha", "beta", "omega", "rr")}
+    tr = _Trace(_p(swk, _PI), _p(sws, _PI), cap, 0, _p(act, _PI), act.shape[0], _p(conv, _PI), 0,
+                _p(hist["alpha"], _PD), _p(hist["beta"], _PD), _p(hist["omega"], _PD), _p(hist["rr"], _PD),
+                max_iter + 2)
     opts = _Opts(float(tol), int(max_iter), 1 if switching else 0, SCHEDULES[schedule])
     k = lib().hbo_shifted_bicgstab(n, _p(ptr, _PU), _p(col, _PU), _p(val, _PD), _p(x, _PD), _p(r, _PD),
                                    _p(sig, _PD), m, int(seed), C.byref(opts), C.byref(tr))
     sw = [(int(swk[i]), int(sws[i])) for i in range(min(tr.n_sw, cap))]
-    return OracleResult(k, x, r, sw, act[:k + 1].copy(), conv[:m].copy(), tr.final_seed)
+    hist = {key: v[:k].copy() for key, v in hist.items()}
+    return OracleResult(k, x, r, sw, act[:k + 1].copy(), conv[:m].copy(), tr.final_seed, hist)
+
+
+def shift_profile(hist, sigma, seed, tol, bb):
+    """Replay the shift recurrences of src/solver_dynamic.c:243-253 from a seed's
+    scalar history (no switching): the iteration at which every shift meets the
+    convergence test (:294) and the number of non-seed shifts each iteration
+    updates.  Used to cost a full multi-shift solve from a seed-only run."""
+    a, b, w, rr = hist["alpha"], hist["beta"], hist["omega"], hist["rr"]
+    kend = len(a)
+    sig = np.asarray(sigma, dtype=np.float64)
+    d = sig[seed] - sig
+    m = len(sig)
+    eta = np.zeros(m)
+    zeta = np.ones(m)
+    pi_prev = np.ones(m)
+    conv = np.zeros(m, dtype=np.int64)
+    act = np.zeros(kend + 1, dtype=np.int64)
+    thr = tol * tol * bb
+    for k in range(1, kend):
+        running = conv == 0
+        act[k] = int(running.sum()) - int(running[seed])
+        c_prev = (b[k - 1] / a[k - 1]) * a[k]
+        eta = c_prev * eta - d * a[k] * pi_prev
+        pi = eta + pi_prev
+        zeta = (1.0 - w[k] * d) * zeta
+        fac = np.abs(1.0 / (zeta * pi))
+        fac[seed] = 1.0
+        newly = running & (fac * fac * rr[k] <= thr)
+        conv[newly] = k
+        pi_prev = pi
+    return conv, act
 
 
 def ref_solve(a, b, sigma, seed=0, tol=1e-12, max_iter=2000, variant="dynamic", switching=True) -> OracleResult:
