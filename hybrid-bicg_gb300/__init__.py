@@ -62,7 +62,7 @@ class INFO_Matrix(C.Structure):
 class Params(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("switching", C.c_int), ("form", C.c_int),
                 ("shift_mode", C.c_int), ("use_graph", C.c_int), ("graph_chunk", C.c_int),
-                ("basis_mem_frac", C.c_double), ("true_residuals", C.c_int)]
+                ("basis_mem_frac", C.c_double), ("true_residuals", C.c_int), ("basis_block", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -71,7 +71,8 @@ class Stats(C.Structure):
                 ("solve_ms", C.c_double), ("flush_ms", C.c_double), ("max_true_residual", C.c_double),
                 ("bytes_algorithmic", C.c_double),
                 ("switch_k", _PI), ("switch_seed", _PI), ("conv_k", _PI), ("active_per_iter", _PI),
-                ("true_residual", _PD)]
+                ("true_residual", _PD), ("seed_alpha", _PD), ("seed_beta", _PD), ("seed_omega", _PD),
+                ("seed_rr", _PD)]
 
 
 _lib = None
@@ -142,7 +143,7 @@ def _ptr(a) -> int:
 
 
 def params(tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="auto", use_graph=True,
-           graph_chunk=0, basis_mem_frac=0.0, true_residuals=False) -> Params:
+           graph_chunk=0, basis_mem_frac=0.0, true_residuals=False, basis_block=0) -> Params:
     p = Params()
     lib().hbicg_params_default(C.byref(p))
     p.tol = float(tol)
@@ -155,6 +156,7 @@ def params(tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="a
     if basis_mem_frac:
         p.basis_mem_frac = float(basis_mem_frac)
     p.true_residuals = 1 if true_residuals else 0
+    p.basis_block = int(basis_block)
     return p
 
 
@@ -190,12 +192,18 @@ def _stats(m: int, max_iter: int):
         "conv_k": np.zeros(max(m, 1), dtype=np.int32),
         "active_per_iter": np.zeros(max_iter + 2, dtype=np.int32),
         "true_residual": np.zeros(max(m, 1)),
+        "seed_alpha": np.zeros(max_iter + 2),
+        "seed_beta": np.zeros(max_iter + 2),
+        "seed_omega": np.zeros(max_iter + 2),
+        "seed_rr": np.zeros(max_iter + 2),
     }
     st.switch_k = bufs["switch_k"].ctypes.data_as(_PI)
     st.switch_seed = bufs["switch_seed"].ctypes.data_as(_PI)
     st.conv_k = bufs["conv_k"].ctypes.data_as(_PI)
     st.active_per_iter = bufs["active_per_iter"].ctypes.data_as(_PI)
     st.true_residual = bufs["true_residual"].ctypes.data_as(_PD)
+    for key in ("seed_alpha", "seed_beta", "seed_omega", "seed_rr"):
+        setattr(st, key, bufs[key].ctypes.data_as(_PD))
     return st, bufs
 
 
@@ -207,7 +215,9 @@ def _result(st: Stats, bufs, m, x, r, want_res) -> SolveResult:
                        shift_mode={1: "incremental", 2: "deferred"}.get(st.shift_mode, "?"), solve_ms=st.solve_ms,
                        flush_ms=st.flush_ms,
                        launches=st.launches, flushes=st.basis_flushes, bytes_algorithmic=st.bytes_algorithmic,
-                       true_residual=bufs["true_residual"][:m].copy() if want_res else None)
+                       true_residual=bufs["true_residual"][:m].copy() if want_res else None,
+                       extra={"hist": {"alpha": bufs["seed_alpha"][:st.k].copy(), "beta": bufs["seed_beta"][:st.k].copy(),
+                                       "omega": bufs["seed_omega"][:st.k].copy(), "rr": bufs["seed_rr"][:st.k].copy()}})
 
 
 def _csr_arrays(a):
@@ -216,7 +226,7 @@ def _csr_arrays(a):
 
 
 def solve(a, b, sigma, seed=0, *, tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="auto",
-          use_graph=True, true_residuals=False, graph_chunk=0, basis_mem_frac=0.0) -> SolveResult:
+          use_graph=True, true_residuals=False, graph_chunk=0, basis_mem_frac=0.0, basis_block=0) -> SolveResult:
     """One-call solve with host (numpy) arrays through hbicg_solve."""
     L = lib()
     ptr, col, val = _csr_arrays(a)
@@ -225,7 +235,8 @@ def solve(a, b, sigma, seed=0, *, tol=1e-12, max_iter=2000, switching=True, form
     sig = np.ascontiguousarray(sigma, dtype=np.float64)
     x = np.zeros((m, n))
     r = np.zeros(n)
-    p = params(tol, max_iter, switching, form, shift_mode, use_graph, graph_chunk, basis_mem_frac, true_residuals)
+    p = params(tol, max_iter, switching, form, shift_mode, use_graph, graph_chunk, basis_mem_frac, true_residuals,
+               basis_block)
     st, bufs = _stats(m, max_iter)
     rc = L.hbicg_solve(n, int(ptr[-1]), _ptr(ptr), _ptr(col), _ptr(val), _ptr(bb), _ptr(sig), m, int(seed),
                        C.byref(p), _ptr(x), _ptr(r), C.byref(st))

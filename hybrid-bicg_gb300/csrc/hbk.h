@@ -34,6 +34,11 @@ extern "C" {
 #define HBK_BLK_TILE 0       /* up to HBK_THREADS short rows, <= HBK_TILE_NNZ nonzeros */
 #define HBK_BLK_LONG 1       /* one long row, reduced by the whole block */
 
+/* SpMV storage formats */
+#define HBK_FMT_TILE 0       /* CSR, row blocks staged in shared memory */
+#define HBK_FMT_SELL 1       /* SELL-32: slices of 32 rows, column-major within a slice */
+#define HBK_SELL_MAX_LEN 64  /* longest row the SELL format takes */
+
 typedef struct {
     unsigned n, nnz;
     const unsigned *ptr, *col; /* device CSR, n+1 and nnz entries */
@@ -42,6 +47,10 @@ typedef struct {
     const unsigned char *blk_kind;
     unsigned nblk;
     int grid;                  /* persistent grid of the SpMV kernels */
+    int fmt;                   /* HBK_FMT_* */
+    const double *sval;        /* SELL: values, slice s at sptr[s], entry e of lane l at +e*32+l */
+    const unsigned *scol;      /* SELL: column indices (padding: the row itself, value 0) */
+    const unsigned long long *sptr; /* SELL: n/32 rounded up + 1 slice offsets */
 } hbk_matrix;
 
 /* Device-resident scalars of one solve. */
@@ -88,6 +97,7 @@ typedef struct {
     unsigned *counters;         /* [8] last-block tickets */
     double *ratio;              /* [kcap] scratch for the switch replay */
     int *lslot;                 /* [m] deferred mode: basis slots in use at a system's last update */
+    double *rr_hist;            /* [kcap] (r, r) at the end of each iteration */
     int m, kcap;
 } hbk_shifts;
 
@@ -125,6 +135,11 @@ int hbk_spmv_accumulate(const hbk_matrix *A, const double *x, double *y, cudaStr
 /* Host: split rows into blocks (counts only when blk_row is NULL). */
 unsigned hbk_plan_rows(unsigned n, const unsigned *ptr_host, unsigned *blk_row, unsigned char *blk_kind);
 int hbk_spmv_grid(unsigned nblk);
+/* SELL-32 build on the device: widths of the ceil(n/32) slices into w ... */
+int hbk_sell_widths(unsigned n, const unsigned *ptr, unsigned *w, cudaStream_t st);
+/* ... then, with sptr = exclusive prefix sum of 32*w (host), fill the arrays */
+int hbk_sell_fill(unsigned n, const unsigned *ptr, const unsigned *col, const double *val,
+                  const unsigned long long *sptr, double *sval, unsigned *scol, cudaStream_t st);
 
 /* ---- fused solver ---- */
 int hbk_fused_init(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, const double *b, int seed,

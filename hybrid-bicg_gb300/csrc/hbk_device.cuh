@@ -86,9 +86,47 @@ struct SpmvSmem {
     double red[2 * NW];
 };
 
+// SELL-32 path: one thread per row, the 32 rows of a slice in one warp.  Entry
+// e of the slice's rows is one 256-byte line of values and one 128-byte line
+// of column indices, so every load is coalesced and no shared memory or
+// barrier is needed; each row is still summed in stored order with FMAs from
+// 0, exactly as in the TILE path (padding entries are skipped by row length).
+template <class Epi>
+__device__ __forceinline__ void spmv_rows_sell(const hbk_matrix &A, const double *__restrict__ x, Epi &epi) {
+    const unsigned *__restrict__ ptr = A.ptr;
+    const double *__restrict__ sval = A.sval;
+    const unsigned *__restrict__ scol = A.scol;
+    const unsigned n = A.n;
+    const unsigned ns = (n + 31) / 32;
+    const unsigned stride = gridDim.x * NT;
+    for (unsigned r0 = blockIdx.x * NT; r0 < n; r0 += stride) {
+        const unsigned r = r0 + threadIdx.x;
+        const unsigned s = r >> 5, lane = r & 31;
+        unsigned long long base = 0;
+        unsigned w = 0;
+        if (s < ns) {
+            base = __ldg(A.sptr + s);
+            w = (unsigned)((__ldg(A.sptr + s + 1) - base) >> 5);
+        }
+        const unsigned len = r < n ? __ldg(ptr + r + 1) - __ldg(ptr + r) : 0;
+        const double *__restrict__ vv = sval + base + lane;
+        const unsigned *__restrict__ cc = scol + base + lane;
+        double acc = 0.0;
+#pragma unroll 4
+        for (unsigned e = 0; e < w; ++e) {
+            if (e < len) acc = fma(__ldg(vv + 32 * (size_t)e), __ldg(x + __ldg(cc + 32 * (size_t)e)), acc);
+        }
+        if (r < n) epi(r, acc);
+    }
+}
+
 template <class Epi>
 __device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__restrict__ x, Epi &epi,
                                           SpmvSmem &sm) {
+    if (A.fmt == HBK_FMT_SELL) {
+        spmv_rows_sell(A, x, epi);
+        return;
+    }
     const unsigned *__restrict__ ptr = A.ptr;
     const unsigned *__restrict__ col = A.col;
     const double *__restrict__ val = A.val;

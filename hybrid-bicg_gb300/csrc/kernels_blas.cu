@@ -102,9 +102,54 @@ __global__ void __launch_bounds__(NT) k_true_res(hbk_matrix A, const double *__r
     }
 }
 
+// SELL-32 build: slice widths, then one thread per row writes its entries
+// (column-major within the slice) and its padding (value 0, column = row).
+__global__ void __launch_bounds__(NT) k_sell_widths(unsigned n, const unsigned *__restrict__ ptr,
+                                                    unsigned *__restrict__ w) {
+    const unsigned ns = (n + 31) / 32;
+    for (unsigned s = blockIdx.x * NT + threadIdx.x; s < ns; s += gridDim.x * NT) {
+        unsigned mx = 0;
+        const unsigned r1 = min(n, 32 * s + 32);
+        for (unsigned r = 32 * s; r < r1; ++r) mx = max(mx, ptr[r + 1] - ptr[r]);
+        w[s] = mx;
+    }
+}
+
+__global__ void __launch_bounds__(NT) k_sell_fill(unsigned n, const unsigned *__restrict__ ptr,
+                                                  const unsigned *__restrict__ col, const double *__restrict__ val,
+                                                  const unsigned long long *__restrict__ sptr,
+                                                  double *__restrict__ sval, unsigned *__restrict__ scol) {
+    const unsigned n32 = (n + 31) / 32 * 32;
+    for (unsigned r = blockIdx.x * NT + threadIdx.x; r < n32; r += gridDim.x * NT) {
+        const unsigned s = r >> 5, lane = r & 31;
+        const unsigned long long base = sptr[s];
+        const unsigned w = (unsigned)((sptr[s + 1] - base) >> 5);
+        const unsigned a = r < n ? ptr[r] : 0, len = r < n ? ptr[r + 1] - ptr[r] : 0;
+        const unsigned self = r < n ? r : 0;
+        for (unsigned e = 0; e < w; ++e) {
+            const size_t o = base + 32 * (size_t)e + lane;
+            sval[o] = e < len ? val[a + e] : 0.0;
+            scol[o] = e < len ? col[a + e] : self;
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+int hbk_sell_widths(unsigned n, const unsigned *ptr, unsigned *w, cudaStream_t st) {
+    if (!n) return 0;
+    k_sell_widths<<<grid_for((n + 31) / 32, 1), NT, 0, st>>>(n, ptr, w);
+    return (int)cudaGetLastError();
+}
+
+int hbk_sell_fill(unsigned n, const unsigned *ptr, const unsigned *col, const double *val,
+                  const unsigned long long *sptr, double *sval, unsigned *scol, cudaStream_t st) {
+    if (!n) return 0;
+    k_sell_fill<<<grid_for(n, 1), NT, 0, st>>>(n, ptr, col, val, sptr, sval, scol);
+    return (int)cudaGetLastError();
+}
 
 int hbk_last_error(void) { return (int)cudaGetLastError(); }
 const char *hbk_error_string(int code) { return cudaGetErrorString((cudaError_t)code); }

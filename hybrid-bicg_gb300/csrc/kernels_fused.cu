@@ -221,6 +221,7 @@ __device__ void seed_step_scalars(const Ctx &c, double rr, double rrh) {
     const int deferred = c.v.deferred;
     if (threadIdx.x == 0) {
         sc->rr = rr;
+        if (k < kcap) S.rr_hist[k] = rr;
         const double bk = mul(dvd(S.a_hist[k], S.w_hist[k]), dvd(rrh, sc->rr_hat_old));
         S.b_hist[k] = bk;
         sc->beta = bk;

@@ -86,6 +86,7 @@ void hbicg_params_default(hbicg_params *p) {
     p->graph_chunk = 0;
     p->basis_mem_frac = 0.6;
     p->true_residuals = 0;
+    p->basis_block = 0;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -134,7 +135,55 @@ struct hbicg_matrix {
     int owns;
     unsigned *d_blk_row;
     unsigned char *d_blk_kind;
+    double *d_sval;
+    unsigned *d_scol;
+    unsigned long long *d_sptr;
 };
+
+/* SELL-32 when every row fits in HBK_SELL_MAX_LEN and padding stays under a
+ * third of the nonzeros (rows are short and regular, as in stencils); the CSR
+ * row-block path otherwise.  HBICG_SPMV_FORMAT=tile|sell overrides. */
+static int build_sell(hbicg_matrix *A, const unsigned *h_ptr, unsigned n, unsigned nnz) {
+    cudaStream_t st = A->ctx->stream;
+    unsigned maxlen = 0;
+    for (unsigned i = 0; i < n; i++)
+        if (h_ptr[i + 1] - h_ptr[i] > maxlen) maxlen = h_ptr[i + 1] - h_ptr[i];
+    const char *env = getenv("HBICG_SPMV_FORMAT");
+    int want = maxlen <= HBK_SELL_MAX_LEN;
+    if (env && !strcmp(env, "tile")) want = 0;
+    if (env && !strcmp(env, "sell")) want = maxlen <= HBK_SELL_MAX_LEN;
+    if (!want || !n) return HBICG_OK;
+    const unsigned ns = (n + 31) / 32;
+    unsigned *d_w = NULL, *h_w = malloc(sizeof(unsigned) * ns);
+    unsigned long long *h_sp = malloc(sizeof(unsigned long long) * ((size_t)ns + 1));
+    if (!h_w || !h_sp) return HBICG_E_NOMEM;
+    CUDA_TRY(cudaMalloc((void **)&d_w, sizeof(unsigned) * ns));
+    HBK_TRY(hbk_sell_widths(n, A->d_ptr, d_w, st));
+    CUDA_TRY(cudaMemcpyAsync(h_w, d_w, sizeof(unsigned) * ns, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    cudaFree(d_w);
+    h_sp[0] = 0;
+    for (unsigned i = 0; i < ns; i++) h_sp[i + 1] = h_sp[i] + 32ull * h_w[i];
+    const unsigned long long padded = h_sp[ns];
+    free(h_w);
+    if (!env && (double)padded > 1.34 * (double)nnz + 4096.0) {
+        free(h_sp);
+        return HBICG_OK;
+    }
+    CUDA_TRY(cudaMalloc((void **)&A->d_sptr, sizeof(unsigned long long) * ((size_t)ns + 1)));
+    CUDA_TRY(cudaMalloc((void **)&A->d_sval, sizeof(double) * (padded + 1)));
+    CUDA_TRY(cudaMalloc((void **)&A->d_scol, sizeof(unsigned) * (padded + 1)));
+    CUDA_TRY(cudaMemcpyAsync(A->d_sptr, h_sp, sizeof(unsigned long long) * ((size_t)ns + 1), cudaMemcpyHostToDevice,
+                             st));
+    HBK_TRY(hbk_sell_fill(n, A->d_ptr, A->d_col, A->d_val, A->d_sptr, A->d_sval, A->d_scol, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    free(h_sp);
+    A->k.fmt = HBK_FMT_SELL;
+    A->k.sval = A->d_sval;
+    A->k.scol = A->d_scol;
+    A->k.sptr = A->d_sptr;
+    return HBICG_OK;
+}
 
 int hbicg_matrix_create(hbicg_context *ctx, unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *col,
                         const double *val, int where, hbicg_matrix **out) {
@@ -191,6 +240,19 @@ int hbicg_matrix_create(hbicg_context *ctx, unsigned n, unsigned nnz, const unsi
     A->k.blk_kind = A->d_blk_kind;
     A->k.nblk = nb;
     A->k.grid = hbk_spmv_grid(nb);
+    A->k.fmt = HBK_FMT_TILE;
+    {
+        unsigned *hp = h_ptr;
+        if (where == HBICG_DEVICE) {
+            hp = malloc(sizeof(unsigned) * ((size_t)n + 1));
+            if (!hp) return HBICG_E_NOMEM;
+            CUDA_TRY(cudaMemcpy(hp, ptr, sizeof(unsigned) * ((size_t)n + 1), cudaMemcpyDeviceToHost));
+        }
+        int rc = build_sell(A, hp, n, nnz);
+        if (where == HBICG_DEVICE) free(hp);
+        if (rc) return rc;
+        if (A->k.fmt == HBK_FMT_SELL) A->k.grid = hbk_spmv_grid((n + HBK_THREADS - 1) / HBK_THREADS);
+    }
     *out = A;
     return HBICG_OK;
 }
@@ -205,6 +267,9 @@ void hbicg_matrix_destroy(hbicg_matrix *A) {
     }
     cudaFree(A->d_blk_row);
     cudaFree(A->d_blk_kind);
+    if (A->d_sval) cudaFree(A->d_sval);
+    if (A->d_scol) cudaFree(A->d_scol);
+    if (A->d_sptr) cudaFree(A->d_sptr);
     free(A);
 }
 
@@ -354,6 +419,7 @@ int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_
         long cap = (long)(budget / (double)vb);
         long want = 2L * s->kcap + 8;
         if (cap > want) cap = want;
+        if (p.basis_block > 0 && cap > 2L * p.basis_block + 3) cap = 2L * p.basis_block + 3;
         if (cap < 8) {
             /* not enough memory for a useful basis: fall back */
             s->mode = HBICG_SHIFTS_INCREMENTAL;
@@ -386,6 +452,7 @@ int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_
     DALLOC(sh->b_hist, sizeof(double) * ((size_t)s->kcap + 1));
     DALLOC(sh->w_hist, sizeof(double) * ((size_t)s->kcap + 1));
     DALLOC(sh->ratio, sizeof(double) * ((size_t)s->kcap + 1));
+    DALLOC(sh->rr_hist, sizeof(double) * ((size_t)s->kcap + 1));
     DALLOC(sh->pi, sizeof(double) * (size_t)mm * ((size_t)s->kcap + 1));
     DALLOC(sh->eta, sizeof(double) * mm);
     DALLOC(sh->zeta, sizeof(double) * mm);
@@ -425,7 +492,7 @@ void hbicg_solver_destroy(hbicg_solver *s) {
     void *ptrs[] = {v->r_hat, v->rbuf[0], v->rbuf[1], v->s, v->q, v->y, v->X, v->P, v->V, v->ps, v->Xc, v->Pc,
                     v->own, v->Pmat, s->d_sc, s->d_sigma, sh->a_hist, sh->b_hist, sh->w_hist, sh->ratio, sh->pi,
                     sh->eta, sh->zeta, sh->done, sh->conv_k, sh->act_list, sh->lslot, sh->coef, sh->sw_k,
-                    sh->sw_seed, sh->act_hist, sh->partials, sh->counters, s->d_b, s->d_res, s->d_dot, s->d_rold,
+                    sh->rr_hist, sh->sw_seed, sh->act_hist, sh->partials, sh->counters, s->d_b, s->d_res, s->d_dot, s->d_rold,
                     s->d_qcopy};
     for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++)
         if (ptrs[i]) cudaFree(ptrs[i]);
@@ -838,6 +905,13 @@ int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int 
         if (stats->conv_k && m > 0) memcpy(stats->conv_k, conv, sizeof(int) * m);
         if (stats->active_per_iter) memcpy(stats->active_per_iter, act, sizeof(int) * ((size_t)s->kcap + 1));
         if (stats->true_residual && h_res) memcpy(stats->true_residual, h_res, sizeof(double) * m);
+        if (s->p.form == HBICG_FORM_FUSED && k > 0) {
+            const size_t nk = (size_t)(k < s->kcap ? k : s->kcap);
+            if (stats->seed_alpha) cudaMemcpy(stats->seed_alpha, s->sh.a_hist, sizeof(double) * nk, cudaMemcpyDeviceToHost);
+            if (stats->seed_beta) cudaMemcpy(stats->seed_beta, s->sh.b_hist, sizeof(double) * nk, cudaMemcpyDeviceToHost);
+            if (stats->seed_omega) cudaMemcpy(stats->seed_omega, s->sh.w_hist, sizeof(double) * nk, cudaMemcpyDeviceToHost);
+            if (stats->seed_rr) cudaMemcpy(stats->seed_rr, s->sh.rr_hist, sizeof(double) * nk, cudaMemcpyDeviceToHost);
+        }
     }
     free(h_res);
     free(h_sigma);

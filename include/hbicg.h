@@ -53,6 +53,8 @@ typedef struct {
     int graph_chunk;       /* iterations per graph launch, 0 = automatic */
     double basis_mem_frac; /* deferred mode: share of free device memory for the basis (default 0.6) */
     int true_residuals;    /* compute ||b-(A+sigma_j I)x_j||/||b|| after the solve (default 0) */
+    int basis_block;       /* deferred mode: iterations per basis block before x_j, p_j are formed
+                              (0 = automatic; bounds how far the coefficient representation is carried) */
 } hbicg_params;
 
 typedef struct {
@@ -73,6 +75,10 @@ typedef struct {
     int *conv_k;              /* [m] iteration at which each shift met the test (0 = never) */
     int *active_per_iter;     /* [max_iter + 1] non-seed shifts updated at iteration k */
     double *true_residual;    /* [m] */
+    double *seed_alpha;       /* [max_iter + 1] the seed's alpha, beta, omega per iteration (as archived) */
+    double *seed_beta;
+    double *seed_omega;
+    double *seed_rr;          /* [max_iter + 1] (r, r) at the end of each iteration */
 } hbicg_stats;
 
 typedef struct hbicg_context hbicg_context;
