@@ -165,42 +165,64 @@ def spmv_bytes(n: int, nnz: int) -> float:
 
 
 # ------------------------------------------------------------- CPU baseline
-def cpu_baseline(f, threads: int | None = None):
-    """The reference's algorithm (its C restatement, oracle/) on the host cores,
-    bounded: (1) the seed system alone to convergence, timed, which also yields
-    the seed's scalar history; (2) every shift's convergence iteration replayed
-    from that history; (3) all shifts for a few iterations, timed, for the cost
-    of one shift update.  Estimate = seed time + per-shift time x the number of
-    shift updates the full solve performs."""
+def load_profile(name: str, f):
+    """Convergence profile of the reference's algorithm on a named workload
+    (tests/golden/<name>_profile.json, made by tests/golden/make_golden.py
+    --profile <name> from the oracle): iterations and the number of non-seed
+    shifts each iteration updates."""
+    p = ROOT / "tests" / "golden" / f"{name}_profile.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    if len(d["conv_k"]) != len(f.sigma):
+        return None
+    d["source"] = f"reference-algorithm profile {p.name}"
+    return d
+
+
+def cpu_baseline(f, profile=None, threads: int | None = None):
+    """The reference's algorithm (its C restatement, oracle/, with the
+    reference's OpenMP layout) on the host cores, on a bounded sample:
+    the seed system alone for 1 and 3 iterations and all shifts for 1 and 3
+    iterations; the differences are steady per-iteration costs with set-up
+    cancelled.  Time-to-solution = iterations x seed cost + shift updates x
+    per-shift cost, with the iteration count and the per-iteration number of
+    running shifts taken from the reference algorithm's convergence profile
+    (committed, or — for workloads without one — the seed system solved to
+    convergence here and the shifts replayed from its scalars)."""
     orc = graft.load_oracle()
     orc.build(ref=False)
     if threads:
         os.environ["OMP_NUM_THREADS"] = str(threads)
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    bb = float(f.b @ f.b)
-    t0 = time.perf_counter()
-    seed_run = orc.solve(f.a, f.b, f.sigma[f.seed:f.seed + 1], seed=0, tol=f.tol, max_iter=f.max_iter)
-    t_seed = time.perf_counter() - t0
-    k_iters = seed_run.k - 1
-    conv, act = orc.shift_profile(seed_run.hist, f.sigma, f.seed, f.tol, bb)
-    shift_updates = int(act.sum())
-    # all shifts for 1 and for 3 iterations: the difference is two steady
-    # iterations with every shift running (set-up cost cancels)
-    times = {}
-    for s_iters in (1, 3):
+    one = f.sigma[f.seed:f.seed + 1]
+
+    def timed(sigma, iters):
         t0 = time.perf_counter()
-        orc.solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=s_iters)
-        times[s_iters] = time.perf_counter() - t0
-    t_iter_all = (times[3] - times[1]) / 2.0
-    t_iter_seed = t_seed / max(k_iters, 1)
-    per_shift = max(t_iter_all - t_iter_seed, 0.0) / max(len(f.sigma) - 1, 1)
-    est = t_seed + per_shift * shift_updates
-    sample = (f"seed system alone to convergence ({k_iters} iterations, {t_seed:.2f} s) + all {len(f.sigma)} "
-              f"shifts for 1 and 3 iterations ({times[1]:.2f} s, {times[3]:.2f} s); estimate = seed time + "
-              f"{per_shift * 1e3:.3f} ms per shift update x {shift_updates} shift updates replayed from the seed's "
-              f"scalar history")
+        orc.solve(f.a, f.b, sigma, seed=0 if len(sigma) == 1 else f.seed, tol=f.tol, max_iter=iters)
+        return time.perf_counter() - t0
+
+    t_seed = {s: timed(one, s) for s in (1, 3)}
+    t_all = {s: timed(f.sigma, s) for s in (1, 3)}
+    per_seed = max(t_seed[3] - t_seed[1], 0.0) / 2.0
+    per_all = max(t_all[3] - t_all[1], 0.0) / 2.0
+    per_shift = max(per_all - per_seed, 0.0) / max(len(f.sigma) - 1, 1)
+    source = profile.get("source", "given profile") if profile else ""
+    if profile is None:
+        bb = float(f.b @ f.b)
+        run = orc.solve(f.a, f.b, one, seed=0, tol=f.tol, max_iter=f.max_iter)
+        conv, act = orc.shift_profile(run.hist, f.sigma, f.seed, f.tol, bb)
+        profile = {"k": int(run.k), "shift_updates": int(act.sum())}
+        source = "seed solved to convergence here"
+    iters = int(profile["k"]) - 1
+    updates = int(profile["shift_updates"])
+    est = iters * per_seed + updates * per_shift + t_seed[1] - per_seed
+    sample = (f"bounded sample: seed system alone for 1 and 3 iterations ({t_seed[1]:.2f} s, {t_seed[3]:.2f} s), "
+              f"all {len(f.sigma)} shifts for 1 and 3 iterations ({t_all[1]:.2f} s, {t_all[3]:.2f} s); "
+              f"estimate = {iters} iterations x {per_seed * 1e3:.1f} ms + {updates} shift updates x "
+              f"{per_shift * 1e3:.2f} ms + set-up ({source})")
     return {"value": est, "unit": "s", "cores": cores, "kind": "port", "sample": sample,
-            "iterations": k_iters + 1, "shift_updates": shift_updates}
+            "iterations": iters + 1, "shift_updates": updates}
 
 
 # ------------------------------------------------------------- our arm
@@ -283,7 +305,11 @@ def run_ours(args, dist: Dist):
 
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(f)
+        prof = load_profile(args.workload, f) if args.scale is None else None
+        if prof is None:
+            # the GPU solve's own profile (same algorithm; within rounding of the reference's)
+            prof = {"k": int(vres.k), "shift_updates": int(np.sum(vres.active)), "source": "the GPU solve's profile"}
+        cpu = cpu_baseline(f, prof)
 
     line = {
         "metric": METRIC, "value": step_max, "unit": "s", "n_gpus": dist.world, "steps": args.steps,
@@ -312,8 +338,9 @@ def run_reference(args, dist: Dist):
     _, f = workload(args.workload, args.scale)
     vals = []
     info = None
+    prof = load_profile(args.workload, f) if args.scale is None else None
     for i in range(max(1, min(args.warmup, 1)) + args.steps):
-        info = cpu_baseline(f)
+        info = cpu_baseline(f, prof)
         if i >= max(1, min(args.warmup, 1)):
             vals.append(info["value"])
     v = float(np.median(vals))

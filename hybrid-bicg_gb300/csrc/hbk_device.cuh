@@ -121,12 +121,8 @@ __device__ __forceinline__ void spmv_rows_sell(const hbk_matrix &A, const double
 }
 
 template <class Epi>
-__device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__restrict__ x, Epi &epi,
-                                          SpmvSmem &sm) {
-    if (A.fmt == HBK_FMT_SELL) {
-        spmv_rows_sell(A, x, epi);
-        return;
-    }
+__device__ __forceinline__ void spmv_rows_tile(const hbk_matrix &A, const double *__restrict__ x, Epi &epi,
+                                               SpmvSmem &sm) {
     const unsigned *__restrict__ ptr = A.ptr;
     const unsigned *__restrict__ col = A.col;
     const double *__restrict__ val = A.val;
@@ -158,6 +154,25 @@ __device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__r
         __syncthreads();
     }
 }
+
+// Format chosen at compile time so the SELL kernels carry no shared-memory
+// tile (full occupancy); launchers pick the instantiation from A.fmt.
+template <int FMT, class Epi>
+__device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__restrict__ x, Epi &epi) {
+    if constexpr (FMT == HBK_FMT_SELL) {
+        spmv_rows_sell(A, x, epi);
+    } else {
+        __shared__ SpmvSmem sm;
+        spmv_rows_tile(A, x, epi, sm);
+    }
+}
+
+// launch helper: kernel<FMT> for the matrix's format
+#define HBK_LAUNCH_FMT(A, kern, grid, block, stream, ...)                                   \
+    do {                                                                                    \
+        if ((A).fmt == HBK_FMT_SELL) kern<HBK_FMT_SELL><<<grid, block, 0, stream>>>(__VA_ARGS__); \
+        else kern<HBK_FMT_TILE><<<grid, block, 0, stream>>>(__VA_ARGS__);                  \
+    } while (0)
 
 inline int grid_for(unsigned n, int per_thread) {
     static int sms = 0;

@@ -56,24 +56,24 @@ struct EpiAccum {
     __device__ void operator()(unsigned r, double acc) const { y[r] += acc; }
 };
 
+template <int FMT>
 __global__ void __launch_bounds__(NT) k_spmv(hbk_matrix A, const double *__restrict__ x, double *__restrict__ y,
                                              double sigma, int add) {
-    __shared__ SpmvSmem sm;
     EpiStore epi{y, x, sigma, add};
-    spmv_rows(A, x, epi, sm);
+    spmv_rows<FMT>(A, x, epi);
 }
 
+template <int FMT>
 __global__ void __launch_bounds__(NT) k_spmv_acc(hbk_matrix A, const double *__restrict__ x, double *__restrict__ y) {
-    __shared__ SpmvSmem sm;
     EpiAccum epi{y};
-    spmv_rows(A, x, epi, sm);
+    spmv_rows<FMT>(A, x, epi);
 }
 
 // out[j] = ||b - (A + sigma_j I) x_j||^2 ; one launch per shift block (grid.y = shift)
+template <int FMT>
 __global__ void __launch_bounds__(NT) k_true_res(hbk_matrix A, const double *__restrict__ X, size_t ld,
                                                  const double *__restrict__ b, const double *__restrict__ sigma,
                                                  double *partials, unsigned *counters, double *out) {
-    __shared__ SpmvSmem sm;
     __shared__ double sh[NW];
     const int j = blockIdx.y;
     const double *xj = X + (size_t)j * ld;
@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(NT) k_true_res(hbk_matrix A, const double *__r
         const double res = b[r] - fma(sg, xj[r], ax);
         acc = fma(res, res, acc);
     };
-    spmv_rows(A, xj, epi, sm);
+    spmv_rows<FMT>(A, xj, epi);
     acc = block_sum(acc, sh);
     double *pj = partials + (size_t)j * gridDim.x;
     if (threadIdx.x == 0) pj[blockIdx.x] = acc;
@@ -200,13 +200,13 @@ int hbk_spmv_grid(unsigned nblk) {
 
 int hbk_spmv(const hbk_matrix *A, const double *x, double *y, double sigma, int sigma_add, cudaStream_t st) {
     if (!A->n) return 0;
-    k_spmv<<<A->grid, NT, 0, st>>>(*A, x, y, sigma, sigma_add);
+    HBK_LAUNCH_FMT(*A, k_spmv, A->grid, NT, st, *A, x, y, sigma, sigma_add);
     return (int)cudaGetLastError();
 }
 
 int hbk_spmv_accumulate(const hbk_matrix *A, const double *x, double *y, cudaStream_t st) {
     if (!A->n) return 0;
-    k_spmv_acc<<<A->grid, NT, 0, st>>>(*A, x, y);
+    HBK_LAUNCH_FMT(*A, k_spmv_acc, A->grid, NT, st, *A, x, y);
     return (int)cudaGetLastError();
 }
 
@@ -215,7 +215,7 @@ int hbk_true_residuals(const hbk_matrix *A, const double *X, const double *b, co
     if (!A->n || m <= 0) return 0;
     size_t ld = ((size_t)A->n + 31) / 32 * 32;
     dim3 grid(A->grid, m);
-    k_true_res<<<grid, NT, 0, st>>>(*A, X, ld, b, sigma, partials, counters, out);
+    HBK_LAUNCH_FMT(*A, k_true_res, grid, NT, st, *A, X, ld, b, sigma, partials, counters, out);
     return (int)cudaGetLastError();
 }
 

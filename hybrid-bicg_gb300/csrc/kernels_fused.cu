@@ -117,8 +117,9 @@ __global__ void __launch_bounds__(NT) k_init_coef(Ctx c) {
 
 // ---------------------------------------------------------------------------
 // K1: s = (A + sigma_s I) p_s and (r^, s)
+template <int FMT>
 __global__ void __launch_bounds__(NT) k_seed_s(Ctx c) {
-    __shared__ SpmvSmem sm;
+    __shared__ double red[2 * NW];
     hbk_scalars *sc = c.sh.sc;
     if (stopped(sc)) return;
     const int seed = sc->seed;
@@ -132,11 +133,11 @@ __global__ void __launch_bounds__(NT) k_seed_s(Ctx c) {
         s[r] = sv;
         acc = fma(rh[r], sv, acc);
     };
-    spmv_rows(c.A, ps, epi, sm);
-    acc = block_sum(acc, sm.red);
+    spmv_rows<FMT>(c.A, ps, epi);
+    acc = block_sum(acc, red);
     if (threadIdx.x == 0) c.sh.partials[blockIdx.x] = acc;
     if (take_ticket(c.sh.counters + 0)) {
-        const double rs = sum_partials(c.sh.partials, gridDim.x, sm.red);
+        const double rs = sum_partials(c.sh.partials, gridDim.x, red);
         if (threadIdx.x == 0) {
             const int k = sc->k;
             const double a = dvd(sc->rr_hat, rs);
@@ -165,8 +166,9 @@ __global__ void __launch_bounds__(NT) k_seed_q(Ctx c) {
 }
 
 // K3: y = (A + sigma_s I) q, (q,q) and (q,y)
+template <int FMT>
 __global__ void __launch_bounds__(NT) k_seed_y(Ctx c) {
-    __shared__ SpmvSmem sm;
+    __shared__ double red[2 * NW];
     hbk_scalars *sc = c.sh.sc;
     if (stopped(sc)) return;
     const double sig = c.sh.sigma[sc->seed];
@@ -180,15 +182,15 @@ __global__ void __launch_bounds__(NT) k_seed_y(Ctx c) {
         acc.x = fma(qr, qr, acc.x);
         acc.y = fma(qr, yv, acc.y);
     };
-    spmv_rows(c.A, q, epi, sm);
-    acc = block_sum2(acc, sm.red);
+    spmv_rows<FMT>(c.A, q, epi);
+    acc = block_sum2(acc, red);
     if (threadIdx.x == 0) {
         c.sh.partials[blockIdx.x] = acc.x;
         c.sh.partials[HBK_MAX_GRID + blockIdx.x] = acc.y;
     }
     if (take_ticket(c.sh.counters + 1)) {
-        const double qq = sum_partials(c.sh.partials, gridDim.x, sm.red);
-        const double qy = sum_partials(c.sh.partials + HBK_MAX_GRID, gridDim.x, sm.red);
+        const double qq = sum_partials(c.sh.partials, gridDim.x, red);
+        const double qy = sum_partials(c.sh.partials + HBK_MAX_GRID, gridDim.x, red);
         if (threadIdx.x == 0) {
             const int k = sc->k;
             const double w = dvd(qq, qy);
@@ -769,9 +771,9 @@ int hbk_fused_init(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *
 int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, cudaStream_t st) {
     Ctx c = make_ctx(A, v, sh);
     const int gv = grid_for(v->n, 2);
-    k_seed_s<<<A->grid, NT, 0, st>>>(c);
+    HBK_LAUNCH_FMT(*A, k_seed_s, A->grid, NT, st, c);
     k_seed_q<<<gv, NT, 0, st>>>(c);
-    k_seed_y<<<A->grid, NT, 0, st>>>(c);
+    HBK_LAUNCH_FMT(*A, k_seed_y, A->grid, NT, st, c);
     k_seed_update<<<gv, NT, 0, st>>>(c);
     if (!v->deferred) {
         k_shift_update<64><<<gv, NT, 0, st>>>(c);

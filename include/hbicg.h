@@ -54,7 +54,7 @@ typedef struct {
     double basis_mem_frac; /* deferred mode: share of free device memory for the basis (default 0.6) */
     int true_residuals;    /* compute ||b-(A+sigma_j I)x_j||/||b|| after the solve (default 0) */
     int basis_block;       /* deferred mode: iterations per basis block before x_j, p_j are formed
-                              (0 = automatic; bounds how far the coefficient representation is carried) */
+                              (0 = automatic, 24; < 0 = as long as memory allows) */
 } hbicg_params;
 
 typedef struct {

@@ -160,5 +160,36 @@ def main() -> None:
     print("mm files:", ", ".join(mm))
 
 
+
+
+def convergence_profile(name: str = "c2") -> None:
+    """Convergence profile of a named workload from the oracle (the reference's
+    algorithm): the seed system alone is solved to convergence, then every
+    shift's convergence iteration is replayed from the seed's scalar history
+    (no switching: the seed is the smallest shift and converges last).  The
+    benchmark's CPU baseline costs a full solve from this profile and a timed
+    bounded sample, so it does not need the hours-long full CPU solve."""
+    import oracle as O
+    import time
+
+    O.build(ref=False)
+    wl = _workloads()
+    f = wl.family(name)
+    t0 = time.perf_counter()
+    seed_run = O.solve(f.a, f.b, f.sigma[f.seed:f.seed + 1], seed=0, tol=f.tol, max_iter=f.max_iter)
+    secs = time.perf_counter() - t0
+    conv, act = O.shift_profile(seed_run.hist, f.sigma, f.seed, f.tol, float(f.b @ f.b))
+    out = {"workload": name, "k": int(seed_run.k), "conv_k": [int(c) for c in conv],
+           "active_per_iter": [int(a) for a in act[:seed_run.k]], "shift_updates": int(act.sum()),
+           "oracle_seconds": secs}
+    import json
+
+    (OUT / f"{name}_profile.json").write_text(json.dumps(out) + "\n")
+    print(f"{name}: k={seed_run.k} shift updates={int(act.sum())} ({secs:.0f} s)")
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 2 and sys.argv[1] == "--profile":
+        convergence_profile(sys.argv[2])
+    else:
+        main()
