@@ -106,6 +106,8 @@ def lib() -> C.CDLL:
         "hbicg_solve": (C.c_int, [C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_int, C.c_int, C.POINTER(Params), C.c_void_p, C.c_void_p, C.POINTER(Stats)]),
         "hbicg_dropin_config": (None, [C.c_double, C.c_int, C.c_int]),
+        "hbicg_true_residuals_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_ulonglong, C.c_void_p, C.c_void_p,
+                                                   C.c_int, C.c_void_p, C.c_void_p]),
         "shifted_lopbicg_dynamic": (C.c_int, [C.POINTER(CSR_Matrix), C.POINTER(CSR_Matrix), C.POINTER(INFO_Matrix),
                                               _PD, _PD, _PD, C.c_int, C.c_int]),
         "shifted_lopbicg_static": (C.c_int, [C.POINTER(CSR_Matrix), C.POINTER(CSR_Matrix), C.POINTER(INFO_Matrix),
@@ -372,6 +374,16 @@ def dropin_solve(variant: str, a, b, sigma, seed=0, tol=1e-12, max_iter=2000, sw
            sig.ctypes.data_as(_PD), m, int(seed))
     L.hbicg_dropin_config(1e-12, 2000, 1)
     return k, x, r
+
+
+def true_residuals_noalloc(matrix: "Matrix", x, b, sigma, res, stream: int = 0) -> None:
+    """hbicg_true_residuals_noalloc: res[j] = ||b - (A + sigma_j I) x_j|| / ||b||
+    for device tensors x [m, ldx], b [n], sigma [m] and res [m], queued on
+    `stream` without allocating device memory (at most 64 shifts)."""
+    m = int(sigma.shape[0])
+    ldx = int(x.stride(0)) if m else matrix.n
+    _check(lib().hbicg_true_residuals_noalloc(matrix.h, _ptr(x), ldx, _ptr(b), _ptr(sigma), m, _ptr(res),
+                                              C.c_void_p(stream)), "hbicg_true_residuals_noalloc")
 
 
 def dropin_raw(variant: str, ptr, col, val, x, r, sigma, seed=0, tol=1e-12, max_iter=2000, switching=True) -> int:

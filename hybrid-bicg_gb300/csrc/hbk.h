@@ -151,6 +151,10 @@ int hbk_deferred_flush(const hbk_vectors *v, const hbk_shifts *sh, int keep_p, c
 int hbk_true_residuals(const hbk_matrix *A, const double *X, const double *b, const double *sigma, int m,
                        double *partials, unsigned *counter, double *out, cudaStream_t st);
 
+/* the same with an explicit leading dimension of X and at most grid_cap blocks */
+int hbk_true_residuals_ld(const hbk_matrix *A, const double *X, size_t ldx, const double *b, const double *sigma,
+                          int m, int grid_cap, double *partials, unsigned *counters, double *out, cudaStream_t st);
+
 int hbk_last_error(void);
 const char *hbk_error_string(int code);
 int hbk_device_sm_count(void);

@@ -219,6 +219,15 @@ int hbk_true_residuals(const hbk_matrix *A, const double *X, const double *b, co
     return (int)cudaGetLastError();
 }
 
+int hbk_true_residuals_ld(const hbk_matrix *A, const double *X, size_t ldx, const double *b, const double *sigma,
+                          int m, int grid_cap, double *partials, unsigned *counters, double *out, cudaStream_t st) {
+    if (!A->n || m <= 0) return 0;
+    const int g = A->grid < grid_cap ? A->grid : grid_cap;
+    dim3 grid(g, m);
+    HBK_LAUNCH_FMT(*A, k_true_res, grid, NT, st, *A, X, ldx, b, sigma, partials, counters, out);
+    return (int)cudaGetLastError();
+}
+
 // Row blocks: consecutive short rows are packed while the block stays within
 // NT rows and HBK_TILE_NNZ nonzeros; a row longer than HBK_TILE_NNZ / 8 gets a
 // block of its own and is reduced by the whole CTA.

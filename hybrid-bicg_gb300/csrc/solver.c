@@ -39,6 +39,8 @@ static void set_msg(const char *fmt, ...) {
 
 const char *hbicg_last_message(void) { return g_msg; }
 
+void hbicg__set_message(const char *msg) { set_msg("%s", msg); }
+
 const char *hbicg_status_string(int s) {
     switch (s) {
     case HBICG_OK: return "ok";
@@ -272,6 +274,8 @@ void hbicg_matrix_destroy(hbicg_matrix *A) {
     if (A->d_sptr) cudaFree(A->d_sptr);
     free(A);
 }
+
+const hbk_matrix *hbicg__matrix_kernel_view(const hbicg_matrix *A) { return &A->k; }
 
 unsigned hbicg_matrix_rows(const hbicg_matrix *A) { return A->k.n; }
 unsigned long long hbicg_matrix_nnz(const hbicg_matrix *A) { return A->k.nnz; }

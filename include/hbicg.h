@@ -117,6 +117,22 @@ void hbicg_solver_destroy(hbicg_solver *s);
 int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int seed, int in_where, double *x,
                      double *r_out, int out_where, hbicg_stats *stats);
 
+/* True relative residuals ||b - (A + sigma_j I) x_j|| / ||b|| into res[0..m)
+ * without allocating anything.  No counterpart in the reference.  For callers
+ * that cannot call cudaMalloc where they check a solve (another component owns
+ * the device memory budget, a latency-bound loop cannot take cudaMalloc's
+ * implicit synchronisation, a host callback may not allocate).  All pointers
+ * are device pointers; x is m rows of ldx doubles; work is queued on `stream`
+ * (a cudaStream_t, 0 = legacy default) and the call does not wait for it.
+ * Scratch is one static device array of about 1 MiB in the library, held by
+ * every GPU that loads it until exit: at most HBICG_NOALLOC_MAX_SHIFTS shifts
+ * (larger m returns HBICG_E_ARG), and calls that overlap on the GPU race on
+ * the shared scratch.  The first call on a device looks the array up with
+ * cudaGetSymbolAddress; make it before any stream capture. */
+#define HBICG_NOALLOC_MAX_SHIFTS 64
+int hbicg_true_residuals_noalloc(hbicg_matrix *A, const double *x, unsigned long long ldx, const double *b,
+                                 const double *sigma, int m, double *res, void *stream);
+
 /* One-call form with host pointers (creates and frees everything). */
 int hbicg_solve(unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *col, const double *val,
                 const double *b, const double *sigma, int m, int seed, const hbicg_params *p, double *x,
