@@ -31,6 +31,7 @@ _PI = C.POINTER(C.c_int)
 HOST, DEVICE = 0, 1
 FORMS = {"plain": 0, "fused": 1}
 SHIFT_MODES = {"auto": 0, "incremental": 1, "deferred": 2}
+FLUSH_MODES = {"auto": 0, "fp64": 1, "tensor": 2}
 STATUS = {0: "ok", 1: "not square", 2: "no diagonal", 3: "breakdown", 4: "max_iter", 5: "cuda", 6: "timeout",
           7: "argument", 8: "out of memory", 9: "io"}
 
@@ -62,7 +63,8 @@ class INFO_Matrix(C.Structure):
 class Params(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("switching", C.c_int), ("form", C.c_int),
                 ("shift_mode", C.c_int), ("use_graph", C.c_int), ("graph_chunk", C.c_int),
-                ("basis_mem_frac", C.c_double), ("true_residuals", C.c_int), ("basis_block", C.c_int)]
+                ("basis_mem_frac", C.c_double), ("true_residuals", C.c_int), ("basis_block", C.c_int),
+                ("flush_mode", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -145,7 +147,7 @@ def _ptr(a) -> int:
 
 
 def params(tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="auto", use_graph=True,
-           graph_chunk=0, basis_mem_frac=0.0, true_residuals=False, basis_block=0) -> Params:
+           graph_chunk=0, basis_mem_frac=0.0, true_residuals=False, basis_block=0, flush="auto") -> Params:
     p = Params()
     lib().hbicg_params_default(C.byref(p))
     p.tol = float(tol)
@@ -159,6 +161,7 @@ def params(tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="a
         p.basis_mem_frac = float(basis_mem_frac)
     p.true_residuals = 1 if true_residuals else 0
     p.basis_block = int(basis_block)
+    p.flush_mode = FLUSH_MODES[flush]
     return p
 
 
@@ -228,7 +231,8 @@ def _csr_arrays(a):
 
 
 def solve(a, b, sigma, seed=0, *, tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="auto",
-          use_graph=True, true_residuals=False, graph_chunk=0, basis_mem_frac=0.0, basis_block=0) -> SolveResult:
+          use_graph=True, true_residuals=False, graph_chunk=0, basis_mem_frac=0.0, basis_block=0,
+          flush="auto") -> SolveResult:
     """One-call solve with host (numpy) arrays through hbicg_solve."""
     L = lib()
     ptr, col, val = _csr_arrays(a)
@@ -238,7 +242,7 @@ def solve(a, b, sigma, seed=0, *, tol=1e-12, max_iter=2000, switching=True, form
     x = np.zeros((m, n))
     r = np.zeros(n)
     p = params(tol, max_iter, switching, form, shift_mode, use_graph, graph_chunk, basis_mem_frac, true_residuals,
-               basis_block)
+               basis_block, flush)
     st, bufs = _stats(m, max_iter)
     rc = L.hbicg_solve(n, int(ptr[-1]), _ptr(ptr), _ptr(col), _ptr(val), _ptr(bb), _ptr(sig), m, int(seed),
                        C.byref(p), _ptr(x), _ptr(r), C.byref(st))

@@ -151,6 +151,18 @@ int hbk_deferred_flush(const hbk_vectors *v, const hbk_shifts *sh, int keep_p, c
 int hbk_true_residuals(const hbk_matrix *A, const double *X, const double *b, const double *sigma, int m,
                        double *partials, unsigned *counter, double *out, cudaStream_t st);
 
+/* basis flush on the tensor cores (flush_tc.cu): x_j += xi_j Pmat_j + Xc_j . V,
+ * p_j = rho_j Pmat_j + Pc_j . V over the first L <= hbk_flush_tc_max_slots()
+ * slots, FP64-accurate; ws of hbk_flush_tc_workspace_bytes(m) bytes; *err set
+ * on a bounded-wait timeout.  No reset (see hbk_deferred_reset). */
+size_t hbk_flush_tc_workspace_bytes(int m);
+int hbk_flush_tc_max_slots(void);
+int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
+                     const double *own, int m, double *X, double *Pmat, int keep_p, void *ws, int *err,
+                     cudaStream_t st);
+/* after a flush: zero the coefficients, own = (0, keep_p), basis slot 0 = r_{k-1} */
+int hbk_deferred_reset(const hbk_vectors *v, const hbk_shifts *sh, int keep_p, cudaStream_t st);
+
 /* the same with an explicit leading dimension of X and at most grid_cap blocks */
 int hbk_true_residuals_ld(const hbk_matrix *A, const double *X, size_t ldx, const double *b, const double *sigma,
                           int m, int grid_cap, double *partials, unsigned *counters, double *out, cudaStream_t st);

@@ -790,10 +790,16 @@ int hbk_deferred_flush(const hbk_vectors *v, const hbk_shifts *sh, int keep_p, c
     Ctx c = make_ctx(&A0, v, sh);
     const int groups = (sh->m + GROUP - 1) / GROUP;
     dim3 grid(grid_for(v->n, 1), groups);
-    // p first (it reads the old Pmat that the x update also reads): write into X
-    // before Pmat is overwritten
+    // x first: it reads the old Pmat, which the p pass then overwrites
     k_flush<<<grid, NT, 0, st>>>(c, keep_p, 0);
     if (keep_p) k_flush<<<grid, NT, 0, st>>>(c, keep_p, 1);
+    k_flush_reset<<<grid_for(v->n, 2), NT, 0, st>>>(c, keep_p);
+    return (int)cudaGetLastError();
+}
+
+int hbk_deferred_reset(const hbk_vectors *v, const hbk_shifts *sh, int keep_p, cudaStream_t st) {
+    hbk_matrix A0 = {};
+    Ctx c = make_ctx(&A0, v, sh);
     k_flush_reset<<<grid_for(v->n, 2), NT, 0, st>>>(c, keep_p);
     return (int)cudaGetLastError();
 }

@@ -89,6 +89,7 @@ void hbicg_params_default(hbicg_params *p) {
     p->basis_mem_frac = 0.6;
     p->true_residuals = 0;
     p->basis_block = 0;
+    p->flush_mode = HBICG_FLUSH_AUTO;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -363,6 +364,8 @@ struct hbicg_solver {
     /* fused form graphs */
     cudaGraphExec_t graph;
     int chunk;
+    void *tc_ws;      /* tensor-core flush workspace (deferred mode) */
+    int *d_tc_err;    /* set by the tensor-core flush on a bounded-wait timeout */
     int launches_per_iter;
 };
 
@@ -447,6 +450,11 @@ int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_
             DALLOC(v->Xc, sizeof(double) * (size_t)mm * (size_t)cap);
             DALLOC(v->Pc, sizeof(double) * (size_t)mm * (size_t)cap);
             DALLOC(v->own, sizeof(double) * 2 * (size_t)mm);
+            if (p.flush_mode != HBICG_FLUSH_FP64) {
+                DALLOC(s->tc_ws, hbk_flush_tc_workspace_bytes(mm));
+                DALLOC(s->d_tc_err, sizeof(int));
+                CUDA_TRY(cudaMemset(s->d_tc_err, 0, sizeof(int)));
+            }
         }
     }
 
@@ -504,7 +512,7 @@ void hbicg_solver_destroy(hbicg_solver *s) {
                     v->own, v->Pmat, s->d_sc, s->d_sigma, sh->a_hist, sh->b_hist, sh->w_hist, sh->ratio, sh->pi,
                     sh->eta, sh->zeta, sh->done, sh->conv_k, sh->act_list, sh->lslot, sh->coef, sh->sw_k,
                     sh->rr_hist, sh->sw_seed, sh->act_hist, sh->partials, sh->counters, s->d_b, s->d_res, s->d_dot, s->d_rold,
-                    s->d_qcopy};
+                    s->d_qcopy, s->tc_ws, s->d_tc_err};
     for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++)
         if (ptrs[i]) cudaFree(ptrs[i]);
     free(s);
@@ -725,6 +733,22 @@ static int ensure_pmat(hbicg_solver *s) {
     return HBICG_OK;
 }
 
+/* Form x_j (and p_j) from the L basis slots in use: on the tensor cores when
+ * the basis fits one K = 64 operand, else with the FP64 kernel; then reset. */
+static int do_flush(hbicg_solver *s, int keep_p, int L, int *launches) {
+    cudaStream_t st = s->ctx->stream;
+    if (s->tc_ws && L >= 1 && L <= hbk_flush_tc_max_slots()) {
+        HBK_TRY(hbk_flush_tc_run(s->v.V, s->ld, s->A->k.n, L, s->v.Xc, s->v.Pc, s->v.slot_cap, s->v.own, s->m, s->v.X,
+                                 s->v.Pmat, keep_p, s->tc_ws, s->d_tc_err, st));
+        HBK_TRY(hbk_deferred_reset(&s->v, &s->sh, keep_p, st));
+        *launches += 4;
+    } else {
+        HBK_TRY(hbk_deferred_flush(&s->v, &s->sh, keep_p, st));
+        *launches += keep_p ? 3 : 2;
+    }
+    return HBICG_OK;
+}
+
 static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, double *flush_ms) {
     cudaStream_t st = s->ctx->stream;
     hbk_scalars *h = s->ctx->h_sc;
@@ -762,12 +786,12 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, dou
             if (rc) return rc;
             float t = 0.f;
             CUDA_TRY(cudaEventRecord(s->ctx->evf0, st));
-            HBK_TRY(hbk_deferred_flush(&s->v, &s->sh, 1, st));
+            rc = do_flush(s, 1, h->slots, launches);
+            if (rc) return rc;
             CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
             CUDA_TRY(cudaEventSynchronize(s->ctx->evf1));
             CUDA_TRY(cudaEventElapsedTime(&t, s->ctx->evf0, s->ctx->evf1));
             *flush_ms += t;
-            *launches += 3;
             (*flushes)++;
             continue;
         }
@@ -776,13 +800,19 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, dou
     if (s->v.deferred) {
         float t = 0.f;
         CUDA_TRY(cudaEventRecord(s->ctx->evf0, st));
-        HBK_TRY(hbk_deferred_flush(&s->v, &s->sh, 0, st));
+        int rc = do_flush(s, 0, h->slots, launches);
+        if (rc) return rc;
         CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
-        *launches += 2;
         CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
+        int tc_err = 0;
+        if (s->d_tc_err) CUDA_TRY(cudaMemcpyAsync(&tc_err, s->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         CUDA_TRY(cudaEventElapsedTime(&t, s->ctx->evf0, s->ctx->evf1));
         *flush_ms += t;
+        if (tc_err) {
+            set_msg("tensor-core flush: an mbarrier wait timed out");
+            return HBICG_E_TIMEOUT;
+        }
         return HBICG_OK;
     }
     CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));

@@ -55,7 +55,14 @@ typedef struct {
     int true_residuals;    /* compute ||b-(A+sigma_j I)x_j||/||b|| after the solve (default 0) */
     int basis_block;       /* deferred mode: iterations per basis block before x_j, p_j are formed
                               (0 = automatic, 24; < 0 = as long as memory allows) */
+    int flush_mode;        /* deferred mode: hbicg_flush_mode (default AUTO) */
 } hbicg_params;
+
+typedef enum {
+    HBICG_FLUSH_AUTO = 0,   /* tensor cores when the basis block fits one K = 64 operand */
+    HBICG_FLUSH_FP64 = 1,   /* FP64 CUDA-core kernel */
+    HBICG_FLUSH_TENSOR = 2  /* tensor cores (BF16 digit products, FP64-accurate) */
+} hbicg_flush_mode;
 
 typedef struct {
     int k;                    /* the reference's return value: iterations + 1 on convergence */
