@@ -234,7 +234,8 @@ def run_ours(args, dist: Dist):
     n, nnz, m = f.a.n, f.a.nnz, len(f.sigma)
     form = "plain" if args.mode == "static" else "fused"
     use_graph = args.mode != "normal"
-    kw = dict(tol=f.tol, max_iter=f.max_iter, form=form, shift_mode=args.shift_mode, use_graph=use_graph)
+    kw = dict(tol=f.tol, max_iter=f.max_iter, form=form, shift_mode=args.shift_mode, use_graph=use_graph,
+              flush=args.flush, basis_block=args.basis_block)
     ctx = pkg.Context()
     ptr = torch.from_numpy(f.a.ptr.astype(np.int32)).cuda()
     col = torch.from_numpy(f.a.col.astype(np.int32)).cuda()
@@ -362,6 +363,8 @@ def main(argv=None):
     ap.add_argument("--scale", type=int, default=None, help="grid side override (smaller case of the same shape)")
     ap.add_argument("--mode", default="dynamic", choices=["dynamic", "static", "normal"])
     ap.add_argument("--shift-mode", default="auto", choices=["auto", "incremental", "deferred"])
+    ap.add_argument("--flush", default="auto", choices=["auto", "fp64", "tensor"])
+    ap.add_argument("--basis-block", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args(argv)

@@ -150,6 +150,21 @@ __device__ __forceinline__ double i128_scaled(__int128 T, int k) {
     return __longlong_as_double((long long)bits);
 }
 
+// exact FP64 of v * 2^e for |v| < 2^53, built from bits (no FP64 instruction)
+__device__ __forceinline__ double i64_scaled(long long v, int e) {
+    if (v == 0) return 0.0;
+    const bool neg = v < 0;
+    const uint64_t u = neg ? (uint64_t)(-v) : (uint64_t)v;
+    const int p = 63 - __clzll((long long)u);
+    const uint64_t mant = u << (52 - p);
+    const int eb = p + e + 1023;
+    if (eb >= 2047) return neg ? -INFINITY : INFINITY;
+    if (eb <= 0) return neg ? -0.0 : 0.0;  // below the normal range: negligible here
+    return __longlong_as_double((long long)(((uint64_t)neg << 63) | ((uint64_t)eb << 52) | (mant & ((1ull << 52) - 1))));
+}
+
+constexpr int SROW = TC_N + 1;  // staged row stride in doubles (avoids bank conflicts)
+
 struct TcArgs {
     const double *V;      // basis [slots][ld]
     size_t ld;
@@ -338,14 +353,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
         // ---- MMAs: diagonal d into accumulator columns [48 d, 48 d + 48)
         if (tid == 0) {
             tc_fence_after();
-            const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+            const uint64_t ad0 = umma_desc(smem_u32(sA)), bd0 = umma_desc(smem_u32(sB));
             for (int d = 0; d < NDIAG; ++d) {
                 bool first = true;
                 for (int s = max(0, d - (NDIG - 1)); s <= min(d, NDIG - 1); ++s) {
                     const int tt = d - s;
                     for (int kk = 0; kk < TC_K / 16; ++kk) {
-                        const uint64_t ad = umma_desc(a0 + s * A_SLICE + kk * 256);
-                        const uint64_t bd = umma_desc(b0 + tt * B_SLICE + kk * 256);
+                        // start-address field: (offset >> 4) adds without carry (smem < 256 KB)
+                        const uint64_t ad = ad0 + (uint64_t)((s * A_SLICE + kk * 256) >> 4);
+                        const uint64_t bd = bd0 + (uint64_t)((tt * B_SLICE + kk * 256) >> 4);
                         const uint32_t acc = first ? 0u : 1u;
                         asm volatile(
                             "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
@@ -369,15 +385,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
         __syncthreads();
         if (*(volatile int *)s_fail) break;
 
-        // ---- epilogue: warp w reads lanes 32 (w % 4) .. +31, columns 24 (w / 4) .. +23
+        // ---- epilogue.  The x and p tiles of the group (64 rows x 48 columns)
+        // are staged in shared memory (the digit buffer is free once the MMAs
+        // are done) with coalesced loads; warp w then reads TMEM lanes
+        // 32 (w % 4) .. +31 (one output row per thread), columns 24 (w / 4) .. +23.
+        double *sXo = reinterpret_cast<double *>(sB);
+        double *sPo = sXo + 64 * SROW;
+        const int jbase = g * 64;
+        const int rows = min(64, a.m - jbase);
+        for (int e = tid; e < 64 * TC_N; e += TC_THREADS) {
+            const int jj = e / TC_N, cc = e % TC_N;
+            const unsigned ii = i0 + cc;
+            const bool in = jj < rows && ii < n;
+            const size_t o = (size_t)(jbase + jj) * ld + ii;
+            sXo[jj * SROW + cc] = in ? a.X[o] : 0.0;
+            sPo[jj * SROW + cc] = (in && a.Pmat) ? a.Pmat[o] : 0.0;
+        }
+        __syncthreads();
         const int lq = warp & 3, ch = warp >> 2;
         const int r = 32 * lq + lane;
-        const int which = r >> 6, j = g * 64 + (r & 63);
-        const bool live = j < a.m && (which == 0 || a.keep_p);
+        const int which = r >> 6, jj = r & 63;
+        const bool live = jj < rows && (which == 0 || a.keep_p);
         const int E = s_rowexp[r];
         const double own = s_rown[r];
-        double *xrow = a.X + (size_t)(j < a.m ? j : 0) * ld;
-        double *prow = a.Pmat ? a.Pmat + (size_t)(j < a.m ? j : 0) * ld : nullptr;
         for (int c = 0; c < 3; ++c) {
             const int col0 = 24 * ch + 8 * c;
             uint32_t dv[NDIAG][8];
@@ -391,32 +421,44 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                     : "r"(taddr));
             }
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            // inputs first (an x row reads the old Pmat that a p row rewrites)
-            double xo[8], po[8];
+            double pn[8];
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
-                const unsigned ii = i0 + col0 + u;
-                xo[u] = (live && which == 0 && ii < n) ? xrow[ii] : 0.0;
-                po[u] = (live && prow && ii < n) ? prow[ii] : 0.0;
-            }
-            __syncthreads();
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const unsigned ii = i0 + col0 + u;
-                if (!live || ii >= n) continue;
-                const int F = s_colexp[col0 + u];
+                const int cc = col0 + u;
+                const int F = s_colexp[cc];
                 double G = 0.0;
                 if (E != EXP_NONE && F != EXP_NONE) {
-                    __int128 T = 0;
+                    // T = sum_d D_d 2^(7 (8 - d)) as hi * 2^35 + lo, both exact in int64
+                    long long hi = __float2int_rz(__uint_as_float(dv[0][u]));
 #pragma unroll
-                    for (int d = 0; d < NDIAG; ++d) {
-                        const long long D = (long long)__uint_as_float(dv[d][u]);
-                        T += (__int128)D * (__int128)(1ll << (7 * (NDIAG - 1 - d)));
-                    }
-                    G = i128_scaled(T, E + F - 70);
+                    for (int d = 1; d < 4; ++d) hi = hi * 128 + __float2int_rz(__uint_as_float(dv[d][u]));
+                    long long lo = __float2int_rz(__uint_as_float(dv[4][u]));
+#pragma unroll
+                    for (int d = 5; d < NDIAG; ++d) lo = lo * 128 + __float2int_rz(__uint_as_float(dv[d][u]));
+                    const long long q = lo >> 35;            // floor(lo / 2^35)
+                    const long long th = hi + q;             // T = th 2^35 + tl, 0 <= tl < 2^35
+                    const long long tl = lo - q * (1ll << 35);
+                    const int k = E + F - 70;
+                    G = i64_scaled(th, k + 35) + i64_scaled(tl, k);  // one rounding
                 }
-                if (which == 0) xrow[ii] = (prow ? fma(own, po[u], xo[u]) : xo[u]) + G;
-                else prow[ii] = prow ? fma(own, po[u], G) : G;
+                // x rows write now (they read the old p); p rows wait for the barrier
+                if (live && which == 0) sXo[jj * SROW + cc] = fma(own, sPo[jj * SROW + cc], sXo[jj * SROW + cc]) + G;
+                pn[u] = fma(own, sPo[jj * SROW + cc], G);
+            }
+            __syncthreads();
+            if (live && which == 1) {
+#pragma unroll
+                for (int u = 0; u < 8; ++u) sPo[jj * SROW + col0 + u] = pn[u];
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < 64 * TC_N; e += TC_THREADS) {
+            const int jr = e / TC_N, cc = e % TC_N;
+            const unsigned ii = i0 + cc;
+            if (jr < rows && ii < n) {
+                const size_t o = (size_t)(jbase + jr) * ld + ii;
+                a.X[o] = sXo[jr * SROW + cc];
+                if (a.keep_p) a.Pmat[o] = sPo[jr * SROW + cc];
             }
         }
         tc_fence_before();
