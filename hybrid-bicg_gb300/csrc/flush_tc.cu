@@ -3,26 +3,30 @@
 // tcgen05 MMAs.
 //
 // GB300 runs FP64 at ~1.2 TFLOP/s, so the FP64 form of this product is the
-// solver's bottleneck.  Here each FP64 operand is cut into nine signed 7-bit
-// integer digits (63 bits) against a power-of-two scale — per output row for
-// the coefficients, per vector element for the basis, after normalising every
-// basis slot by a power of two — so that every digit is exact in BF16.  A
-// digit product summed over K = 64 slots stays below 2^24 even when all pairs
-// of one diagonal (s + t = d) are summed together, so each diagonal
-// d = 0..8 accumulates exactly in its own FP32 TMEM accumulator.  Diagonals
-// past 8 are dropped (their total is below 2^-53 of the row/element scale,
-// the accuracy of an FP64 dot product of the same length).  The epilogue joins
-// the nine exact diagonal sums in 128-bit integer arithmetic and rounds once
-// to FP64; only the own-vector terms use the FP64 pipe.  (The digit splitting
-// is the error-free splitting of Ozaki, Ogita, Oishi and Rump for matrix
-// products, arranged here so that the exact sums fit TMEM.)
+// solver's bottleneck.  Here each FP64 operand becomes a signed 62-bit fixed
+// point integer against a power-of-two scale — per output row for the
+// coefficients, per vector element for the basis, after normalising every
+// basis slot by a power of two — cut into nine balanced 7-bit digits in
+// [-64, 64], each exact in BF16.  A digit product is at most 2^12, so the sum
+// over K = 64 slots of all pairs of one diagonal (s + t = d, at most nine
+// pairs) stays below 2^22: each diagonal d = 0..8 accumulates exactly in its
+// own FP32 TMEM accumulator and converts to an integer with one FP32 add.
+// Diagonals past 8 are dropped (their total is below 2^-54 of the
+// row/element scale, the accuracy of an FP64 dot product of the same length).
+// The epilogue joins the nine exact diagonal sums in 64-bit integer arithmetic
+// and rounds once to FP64; only the own-vector terms use the FP64 pipe.  (The
+// digit splitting is the error-free splitting of Ozaki, Ogita, Oishi and Rump
+// for matrix products, arranged here so that the exact sums fit TMEM.)
 //
-// One CTA per SM (205 KB of shared memory), persistent over tiles of 48
-// vector elements; 128 output rows per group of 64 shifts (x rows, then p
-// rows).  Per tile: build the basis digits in shared memory, one thread
-// issues 45 x 4 MMAs (M=128, N=48, K=16) into nine accumulators, the warps
-// read TMEM back and write x and p.  Every wait is bounded: a timeout sets an
-// error flag, the CTA skips its remaining work and still frees its TMEM.
+// One CTA per SM (203 KB of shared memory), persistent over tiles of 48
+// vector elements; 128 output rows per group of 64 shifts, ordered so that
+// TMEM lanes 32q..32q+15 hold the x rows of shifts 16q..16q+15 and lanes
+// 32q+16..32q+31 their p rows.  Warps 0-3 make the basis digits of a tile
+// and thread 0 issues its MMAs (M=128, N up to 256, K=16; 52 per tile) into
+// nine accumulators; warps 4-15 empty the accumulators into registers first, so
+// that the next tile's MMAs run while they round, add the own-vector terms
+// and write x and p.  Every wait is bounded: a timeout sets an error flag,
+// the CTA skips its remaining work and still frees its TMEM.
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdint.h>
@@ -42,12 +46,30 @@ constexpr int A_SLICE = TC_M * TC_K * 2;  // 16384 B
 constexpr int B_SLICE = TC_N * TC_K * 2;  // 6144 B
 constexpr int A_BYTES = NDIG * A_SLICE;   // 147456 B
 constexpr int B_BYTES = NDIG * B_SLICE;   // 55296 B
-constexpr int TC_THREADS = 256;
+constexpr int BUILD_WARPS = 4;            // warps 0-3: basis digits + MMA issue
+constexpr int EPI_WARPS = 12;             // warps 4-15: epilogue
+constexpr int TC_THREADS = 32 * (BUILD_WARPS + EPI_WARPS);
+constexpr int BUILD_THREADS = 32 * BUILD_WARPS;
+constexpr int EPI_COLS = TC_N / (EPI_WARPS / 4);  // 16 columns per epilogue thread
+constexpr int ITEMS = (TC_K / 8) * TC_N;          // (slot octet, element) pairs per tile
+constexpr int ITEMS_PER = ITEMS / BUILD_THREADS;  // 3
 constexpr int TMEM_COLS = 512;
-constexpr int SMEM_MISC = 4096;
+constexpr int SMEM_MISC = 6144;
 constexpr int SMEM_BYTES = A_BYTES + B_BYTES + SMEM_MISC;
 constexpr long long WAIT_LIMIT = 1ll << 26;  // polls of an mbarrier before giving up
 constexpr int EXP_NONE = -100000;            // exponent of an all-zero row or column
+// sum_s 64 * 2^(56 - 7 s): adding it to a 62-bit signed value makes every
+// 7-bit field of the sum the balanced digit + 64
+constexpr uint64_t DIGIT_BIAS = 0x4081020408102040ull;
+// magic FP32 1.5 * 2^23: for |D| < 2^22, bits(D + MAGIC) = MAGIC_BITS + D
+constexpr float MAGIC = 12582912.0f;
+constexpr uint32_t MAGIC_BITS = 0x4B400000u;
+constexpr uint64_t HI_BIAS = (uint64_t)MAGIC_BITS * 2113665ull;    // * (2^21 + 2^14 + 2^7 + 1)
+constexpr uint64_t LO_BIAS = (uint64_t)MAGIC_BITS * 270549121ull;  // * (2^28 + 2^21 + 2^14 + 2^7 + 1)
+
+static_assert(ITEMS % BUILD_THREADS == 0, "builder items");
+static_assert(EPI_COLS % 4 == 0 && TC_N % 8 == 0, "epilogue columns");
+static_assert(NDIAG * TC_N <= TMEM_COLS, "accumulators fit TMEM");
 
 // byte offset of element (row, k) in a K-major, no-swizzle UMMA operand:
 // core matrices of 8 rows x 16 bytes; K-adjacent core matrices 128 B apart
@@ -78,6 +100,10 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -88,11 +114,14 @@ __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// bounded wait; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// bounded wait; false on timeout or when another warp has already failed
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, const int *fail) {
     for (long long i = 0; i < WAIT_LIMIT; ++i) {
         if (mbar_try(bar, parity)) return true;
-        if (i > 64) __nanosleep(64);
+        if (i > 64) {
+            if ((i & 1023) == 0 && *(const volatile int *)fail) return false;
+            __nanosleep(64);
+        }
     }
     return false;
 }
@@ -108,33 +137,61 @@ __device__ __forceinline__ int exp_of_bits(uint64_t bits) {
     return (64 - __clzll((long long)frac)) - 1074;
 }
 
-// 63-bit magnitude of |v| * 2^(63 - scale) (truncated), v given by its bits
-__device__ __forceinline__ uint64_t fixed63(uint64_t bits, int scale) {
+// v * 2^(62 - scale) truncated toward zero, as a two's complement integer
+// (|v| < 2^scale, so the result is below 2^62), plus DIGIT_BIAS
+__device__ __forceinline__ uint64_t biased62(uint64_t bits, int scale) {
     const int eb = (int)((bits >> 52) & 0x7ff);
     const uint64_t frac = bits & ((1ull << 52) - 1);
     const uint64_t M = eb ? (frac | (1ull << 52)) : frac;
-    const int e2 = (eb ? eb : 1) - 1075;
-    const int sh = e2 + 63 - scale;
-    if (M == 0 || sh <= -64) return 0;
-    return sh >= 0 ? (M << sh) : (M >> (-sh));
+    const int sh = (eb ? eb : 1) - 1075 + 62 - scale;
+    uint64_t q = 0;
+    if (sh >= 0)
+        q = M << sh;
+    else if (sh > -64)
+        q = M >> (-sh);
+    if ((int64_t)bits < 0) q = 0 - q;
+    return q + DIGIT_BIAS;
 }
 
-// round-to-nearest FP64 of T * 2^k, T an exact 128-bit integer
-__device__ __forceinline__ double i128_scaled(__int128 T, int k) {
-    if (T == 0) return 0.0;
-    const bool neg = T < 0;
-    unsigned __int128 U = neg ? (unsigned __int128)(-T) : (unsigned __int128)T;
-    const uint64_t hi = (uint64_t)(U >> 64), lo = (uint64_t)U;
-    int p = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+// balanced digit s (weight 2^(56 - 7 s)) of a biased value, as an exact float
+template <int S>
+__device__ __forceinline__ float digit(uint64_t U) {
+    const uint32_t e = S == 0 ? (uint32_t)(U >> 56) : ((uint32_t)(U >> (56 - 7 * S)) & 127u);
+    return __uint_as_float(0x4B000000u | e) - 8388672.0f;  // (2^23 + e) - (2^23 + 64)
+}
+
+template <int S>
+__device__ __forceinline__ uint32_t digit_pair(uint64_t U0, uint64_t U1) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(digit<S>(U0), digit<S>(U1));
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// 8 consecutive slots of one element (Us[0..7]) -> one 16-byte row of a core
+// matrix in every digit slice
+template <int S>
+__device__ __forceinline__ void store_digits(unsigned char *sB, uint32_t off, const uint64_t *Us) {
+    uint4 w;
+    w.x = digit_pair<S>(Us[0], Us[1]);
+    w.y = digit_pair<S>(Us[2], Us[3]);
+    w.z = digit_pair<S>(Us[4], Us[5]);
+    w.w = digit_pair<S>(Us[6], Us[7]);
+    *reinterpret_cast<uint4 *>(sB + S * B_SLICE + off) = w;
+    if constexpr (S + 1 < NDIG) store_digits<S + 1>(sB, off, Us);
+}
+
+// round-to-nearest FP64 of W * 2^e, |W| < 2^63, built from bits (no FP64 op)
+__device__ __forceinline__ double i64_round(long long W, int e) {
+    if (W == 0) return 0.0;
+    const bool neg = W < 0;
+    const uint64_t u = neg ? (uint64_t)(-W) : (uint64_t)W;
+    int p = 63 - __clzll((long long)u);
     uint64_t mant;
     if (p <= 52) {
-        mant = (uint64_t)(U << (52 - p));
+        mant = u << (52 - p);
     } else {
         const int s = p - 52;
-        const unsigned __int128 m = U >> s;
-        const unsigned __int128 rem = U - (m << s);
-        const unsigned __int128 half = (unsigned __int128)1 << (s - 1);
-        mant = (uint64_t)m;
+        mant = u >> s;
+        const uint64_t rem = u & ((1ull << s) - 1), half = 1ull << (s - 1);
         if (rem > half || (rem == half && (mant & 1))) {
             ++mant;
             if (mant == (1ull << 53)) {
@@ -143,27 +200,22 @@ __device__ __forceinline__ double i128_scaled(__int128 T, int k) {
             }
         }
     }
-    const int eb = p + k + 1023;
-    if (eb >= 2047) return neg ? -INFINITY : INFINITY;
-    if (eb <= 0) return neg ? -0.0 : 0.0;  // below the normal range: negligible here
-    const uint64_t bits = ((uint64_t)neg << 63) | ((uint64_t)eb << 52) | (mant & ((1ull << 52) - 1));
-    return __longlong_as_double((long long)bits);
-}
-
-// exact FP64 of v * 2^e for |v| < 2^53, built from bits (no FP64 instruction)
-__device__ __forceinline__ double i64_scaled(long long v, int e) {
-    if (v == 0) return 0.0;
-    const bool neg = v < 0;
-    const uint64_t u = neg ? (uint64_t)(-v) : (uint64_t)v;
-    const int p = 63 - __clzll((long long)u);
-    const uint64_t mant = u << (52 - p);
     const int eb = p + e + 1023;
     if (eb >= 2047) return neg ? -INFINITY : INFINITY;
     if (eb <= 0) return neg ? -0.0 : 0.0;  // below the normal range: negligible here
     return __longlong_as_double((long long)(((uint64_t)neg << 63) | ((uint64_t)eb << 52) | (mant & ((1ull << 52) - 1))));
 }
 
-constexpr int SROW = TC_N + 1;  // staged row stride in doubles (avoids bank conflicts)
+// the exact sum T = hs 2^35 + ls (|T| < 2^79) times 2^k, rounded to FP64
+// (a 62-bit window of T, then one rounding: error below 0.51 ulp)
+__device__ __forceinline__ double join_diagonals(long long hs, long long ls, int k) {
+    const long long th = hs + (ls >> 35);            // T = th 2^35 + tl, 0 <= tl < 2^35
+    const long long tl = ls & ((1ll << 35) - 1);
+    const int bl = 64 - __clzll(th ^ (th >> 63));    // bits of |th| (|th| < 2^45)
+    const int s = min(35, 62 - bl);
+    const long long W = (long long)((unsigned long long)th << s) + (tl >> (35 - s));
+    return i64_round(W, k + 35 - s);
+}
 
 struct TcArgs {
     const double *V;      // basis [slots][ld]
@@ -187,7 +239,7 @@ __global__ void __launch_bounds__(NT) k_slot_max(const double *__restrict__ V, s
     const double *v = V + (size_t)l * ld;
     unsigned long long mx = 0;
     for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
-        const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(v[i]));
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v[i]) & 0x7FFFFFFFFFFFFFFFull;
         mx = b > mx ? b : mx;
     }
 #pragma unroll
@@ -198,6 +250,10 @@ __global__ void __launch_bounds__(NT) k_slot_max(const double *__restrict__ V, s
     if ((threadIdx.x & 31) == 0 && mx) atomicMax(slot_max + l, mx);
 }
 
+// TMEM lane / A row r of a group -> (x or p, shift within the group)
+__device__ __forceinline__ int row_which(int r) { return (r >> 4) & 1; }
+__device__ __forceinline__ int row_shift(int r) { return ((r >> 5) << 4) | (r & 15); }
+
 // ---- coefficient digits: one block per output row, one thread per slot
 __global__ void __launch_bounds__(TC_K) k_flush_prep(const double *__restrict__ Xc, const double *__restrict__ Pc,
                                                      int cap, const double *__restrict__ own, int m, int L,
@@ -205,7 +261,7 @@ __global__ void __launch_bounds__(TC_K) k_flush_prep(const double *__restrict__ 
                                                      unsigned char *aimg, int *rowexp, double *rown) {
     __shared__ unsigned long long s_max[2];
     const int r = blockIdx.x, g = blockIdx.y, l = threadIdx.x;
-    const int which = r >> 6, j = g * 64 + (r & 63);
+    const int which = row_which(r), j = g * 64 + row_shift(r);
     double a = 0.0;
     if (j < m && l < L) {
         const double c = (which ? Pc : Xc)[(size_t)j * cap + l];
@@ -222,16 +278,14 @@ __global__ void __launch_bounds__(TC_K) k_flush_prep(const double *__restrict__ 
     __syncthreads();
     const unsigned long long rmax = s_max[0] > s_max[1] ? s_max[0] : s_max[1];
     const int E = rmax ? exp_of_bits(rmax) : EXP_NONE;
-    const uint64_t Q = rmax ? fixed63((uint64_t)__double_as_longlong(a), E) : 0;
-    const bool neg = a < 0.0;
+    const uint64_t U = (rmax && a != 0.0) ? biased62((uint64_t)__double_as_longlong(a), E) : DIGIT_BIAS;
     unsigned char *img = aimg + (size_t)g * A_BYTES;
     const uint32_t off = umma_off(r, l);
+    const float d[NDIG] = {digit<0>(U), digit<1>(U), digit<2>(U), digit<3>(U), digit<4>(U),
+                           digit<5>(U), digit<6>(U), digit<7>(U), digit<8>(U)};
 #pragma unroll
-    for (int s = 0; s < NDIG; ++s) {
-        const int dgt = (int)((Q >> (56 - 7 * s)) & 127);
-        const __nv_bfloat16 h = __float2bfloat16_rn((float)(neg ? -dgt : dgt));
-        *reinterpret_cast<__nv_bfloat16 *>(img + (size_t)s * A_SLICE + off) = h;
-    }
+    for (int s = 0; s < NDIG; ++s)
+        *reinterpret_cast<__nv_bfloat16 *>(img + (size_t)s * A_SLICE + off) = __float2bfloat16_rn(d[s]);
     if (l == 0) {
         rowexp[g * TC_M + r] = E;
         rown[g * TC_M + r] = (j < m) ? own[2 * (size_t)j + which] : 0.0;
@@ -244,21 +298,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
     unsigned char *sA = smem;
     unsigned char *sB = smem + A_BYTES;
     unsigned char *misc = smem + A_BYTES + B_BYTES;
-    uint64_t *bar_a = reinterpret_cast<uint64_t *>(misc);
-    uint64_t *bar_mma = reinterpret_cast<uint64_t *>(misc + 8);
-    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(misc + 16);
-    int *s_fail = reinterpret_cast<int *>(misc + 20);
-    int *s_slotexp = reinterpret_cast<int *>(misc + 64);                // [64]
-    int *s_colexp = reinterpret_cast<int *>(misc + 64 + 256);           // [4][48]
-    int *s_rowexp = reinterpret_cast<int *>(misc + 64 + 256 + 768);     // [128]
-    double *s_rown = reinterpret_cast<double *>(misc + 64 + 256 + 768 + 512);  // [128]
+    uint64_t *bar_a = reinterpret_cast<uint64_t *>(misc);           // coefficient digits landed
+    uint64_t *bar_full = reinterpret_cast<uint64_t *>(misc + 8);     // basis digits of a tile written
+    uint64_t *bar_mma = reinterpret_cast<uint64_t *>(misc + 16);     // MMAs of a tile done
+    uint64_t *bar_ready = reinterpret_cast<uint64_t *>(misc + 24);   // MMAs issued (orders s_F for the epilogue)
+    uint64_t *bar_tfree = reinterpret_cast<uint64_t *>(misc + 32);   // accumulators read out
+    uint64_t *bar_cexp = reinterpret_cast<uint64_t *>(misc + 40);    // builders' partial exponents written
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(misc + 48);
+    int *s_fail = reinterpret_cast<int *>(misc + 52);
+    int *s_slotexp = reinterpret_cast<int *>(misc + 64);             // [64]
+    int *s_cexp = reinterpret_cast<int *>(misc + 320);               // [2][8][48] per slot octet
+    int *s_F = reinterpret_cast<int *>(misc + 3392);                 // [4][48] element exponents, ring
+    int *s_rowexp = reinterpret_cast<int *>(misc + 4160);            // [128]
+    double *s_rown = reinterpret_cast<double *>(misc + 4672);        // [128]
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int g = blockIdx.y;
 
     if (tid == 0) {
         mbar_init(bar_a, 1);
+        mbar_init(bar_full, BUILD_THREADS);
         mbar_init(bar_mma, 1);
+        mbar_init(bar_ready, 1);
+        mbar_init(bar_tfree, EPI_WARPS);
+        mbar_init(bar_cexp, BUILD_THREADS);
         *s_fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -280,194 +343,254 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
     tc_fence_after();
     const uint32_t tmem = *s_tmem;
 
-    // the coefficient digits of this group: one bulk copy per slice
-    if (tid == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar_a)),
-                     "r"((uint32_t)A_BYTES)
-                     : "memory");
-        const unsigned char *src = a.aimg + (size_t)g * A_BYTES;
-        for (int s = 0; s < NDIG; ++s)
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                    smem_u32(sA + s * A_SLICE)),
-                "l"(src + (size_t)s * A_SLICE), "r"((uint32_t)A_SLICE), "r"(smem_u32(bar_a))
-                : "memory");
-    }
-    bool a_ok = mbar_wait(bar_a, 0);
-    if (!a_ok) atomicExch(s_fail, 1);
-    __syncthreads();
-
     const unsigned n = a.n;
     const unsigned ntiles = (n + TC_N - 1) / TC_N;
     const size_t ld = a.ld;
-    uint32_t phase = 0;
-    bool mma_pending = false;
-    for (unsigned t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        if (*(volatile int *)s_fail) break;
-        const unsigned i0 = t * TC_N;
-        // ---- basis digits: thread (column i, quarter q) covers slots 16q..16q+15
-        uint64_t vb[16];
-        const int i = tid % TC_N, q = tid / TC_N;
-        const bool builder = tid < 4 * TC_N;
-        int emax = EXP_NONE;
-        if (builder) {
-#pragma unroll
-            for (int u = 0; u < 16; ++u) {
-                const int l = 16 * q + u;
-                double v = 0.0;
-                if (l < a.L && i0 + i < n) v = a.V[(size_t)l * ld + i0 + i];
-                vb[u] = (uint64_t)__double_as_longlong(v);
-                if (v != 0.0) emax = max(emax, exp_of_bits(vb[u]) - s_slotexp[l]);
-            }
-            s_colexp[q * TC_N + i] = emax;
+    bool a_ok = true;
+    int issued = 0;  // thread 0: MMA batches committed
+
+    if (warp < BUILD_WARPS) {
+        // the coefficient digits of this group: one bulk copy per slice
+        if (tid == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar_a)),
+                         "r"((uint32_t)A_BYTES)
+                         : "memory");
+            const unsigned char *src = a.aimg + (size_t)g * A_BYTES;
+            for (int s = 0; s < NDIG; ++s)
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32(sA + s * A_SLICE)),
+                    "l"(src + (size_t)s * A_SLICE), "r"((uint32_t)A_SLICE), "r"(smem_u32(bar_a))
+                    : "memory");
+            a_ok = mbar_wait(bar_a, 0, s_fail);
+            if (!a_ok) atomicExch(s_fail, 1);
         }
-        __syncthreads();
-        if (builder) {
-            int F = s_colexp[i];
-            F = max(F, s_colexp[TC_N + i]);
-            F = max(F, s_colexp[2 * TC_N + i]);
-            F = max(F, s_colexp[3 * TC_N + i]);
+        // item (octet o, element i): slots 8o..8o+7 of element i0 + i
+        int io[ITEMS_PER], ii[ITEMS_PER];
 #pragma unroll
-            for (int u = 0; u < 16; u += 2) {
-                const int l = 16 * q + u;
-                const uint64_t Q0 = vb[u] && F != EXP_NONE ? fixed63(vb[u], F + s_slotexp[l]) : 0;
-                const uint64_t Q1 = vb[u + 1] && F != EXP_NONE ? fixed63(vb[u + 1], F + s_slotexp[l + 1]) : 0;
-                const bool n0 = (int64_t)vb[u] < 0, n1 = (int64_t)vb[u + 1] < 0;
-                const uint32_t off = umma_off(i, l);
+        for (int u = 0; u < ITEMS_PER; ++u) {
+            const int it = tid + BUILD_THREADS * u;
+            io[u] = it / TC_N;
+            ii[u] = it % TC_N;
+        }
+        double v[ITEMS_PER][8];
+        auto load_tile = [&](unsigned t) {
+            const unsigned i0 = t * TC_N;
 #pragma unroll
-                for (int s = 0; s < NDIG; ++s) {
-                    const int d0 = (int)((Q0 >> (56 - 7 * s)) & 127), d1 = (int)((Q1 >> (56 - 7 * s)) & 127);
-                    __nv_bfloat162 h;
-                    h.x = __float2bfloat16_rn((float)(n0 ? -d0 : d0));
-                    h.y = __float2bfloat16_rn((float)(n1 ? -d1 : d1));
-                    *reinterpret_cast<__nv_bfloat162 *>(sB + s * B_SLICE + off) = h;
+            for (int u = 0; u < ITEMS_PER; ++u)
+#pragma unroll
+                for (int w = 0; w < 8; ++w) {
+                    const int l = 8 * io[u] + w;
+                    v[u][w] = (l < a.L && i0 + ii[u] < n) ? __ldcs(a.V + (size_t)l * ld + i0 + ii[u]) : 0.0;
+                }
+        };
+        const uint64_t ad0 = umma_desc(smem_u32(sA)), bd0 = umma_desc(smem_u32(sB));
+        int it = 0;
+        if (blockIdx.x < ntiles) load_tile(blockIdx.x);
+        for (unsigned t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+            if (*(volatile int *)s_fail) break;
+            // phase A (overlaps the previous tile's MMAs): element exponents and
+            // fixed-point values; s_cexp alternates between two buffers
+            int *cexp = s_cexp + (it & 1) * ITEMS;
+            int em[ITEMS_PER];
+#pragma unroll
+            for (int u = 0; u < ITEMS_PER; ++u) {
+                int e = EXP_NONE;
+#pragma unroll
+                for (int w = 0; w < 8; ++w) {
+                    const uint64_t bits = (uint64_t)__double_as_longlong(v[u][w]);
+                    if (bits << 1) e = max(e, exp_of_bits(bits) - s_slotexp[8 * io[u] + w]);
+                }
+                em[u] = e;
+                cexp[io[u] * TC_N + ii[u]] = e;
+            }
+            // (an mbarrier, not a named barrier: a builder that gave up must not hang the others)
+            mbar_arrive(bar_cexp);
+            if (!mbar_wait(bar_cexp, it & 1, s_fail)) {
+                atomicExch(s_fail, 1);
+                break;
+            }
+            int Fv[ITEMS_PER];
+            uint64_t U[ITEMS_PER][8];
+#pragma unroll
+            for (int u = 0; u < ITEMS_PER; ++u) {
+                int F = em[u];
+#pragma unroll
+                for (int o = 0; o < TC_K / 8; ++o) F = max(F, cexp[o * TC_N + ii[u]]);
+                Fv[u] = F;
+#pragma unroll
+                for (int w = 0; w < 8; ++w) {
+                    const uint64_t bits = (uint64_t)__double_as_longlong(v[u][w]);
+                    U[u][w] = ((bits << 1) && F != EXP_NONE) ? biased62(bits, F + s_slotexp[8 * io[u] + w]) : DIGIT_BIAS;
                 }
             }
-        }
-        // digits written by threads must be visible to the tensor core (async proxy)
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (builder && q == 0) s_colexp[i] = max(max(s_colexp[i], s_colexp[TC_N + i]),
-                                                 max(s_colexp[2 * TC_N + i], s_colexp[3 * TC_N + i]));
-
-        // ---- MMAs: diagonal d into accumulator columns [48 d, 48 d + 48)
-        if (tid == 0) {
-            tc_fence_after();
-            const uint64_t ad0 = umma_desc(smem_u32(sA)), bd0 = umma_desc(smem_u32(sB));
-            for (int d = 0; d < NDIAG; ++d) {
-                bool first = true;
-                for (int s = max(0, d - (NDIG - 1)); s <= min(d, NDIG - 1); ++s) {
-                    const int tt = d - s;
-                    for (int kk = 0; kk < TC_K / 16; ++kk) {
-                        // start-address field: (offset >> 4) adds without carry (smem < 256 KB)
-                        const uint64_t ad = ad0 + (uint64_t)((s * A_SLICE + kk * 256) >> 4);
-                        const uint64_t bd = bd0 + (uint64_t)((tt * B_SLICE + kk * 256) >> 4);
-                        const uint32_t acc = first ? 0u : 1u;
-                        asm volatile(
-                            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-                            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem + d * TC_N),
-                            "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
-                            : "memory");
-                        first = false;
+            // phase B: the digit buffer is free once the previous tile's MMAs are done
+            if (it > 0 && !mbar_wait(bar_mma, (it - 1) & 1, s_fail)) {
+                atomicExch(s_fail, 1);
+                break;
+            }
+#pragma unroll
+            for (int u = 0; u < ITEMS_PER; ++u) {
+                if (io[u] == 0) s_F[(it & 3) * TC_N + ii[u]] = Fv[u];
+                store_digits<0>(sB, umma_off(ii[u], 8 * io[u]), U[u]);
+            }
+            // digits written by threads must be visible to the tensor core (async proxy)
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(bar_full);
+            // the next tile's basis values are in flight during this tile's MMAs
+            if (t + gridDim.x < ntiles) load_tile(t + gridDim.x);
+            if (tid == 0) {
+                bool ok = a_ok && mbar_wait(bar_full, it & 1, s_fail);
+                // the previous tile's accumulators must have been read out
+                if (ok && it > 0) ok = mbar_wait(bar_tfree, (it - 1) & 1, s_fail);
+                if (!ok) {
+                    atomicExch(s_fail, 1);
+                    break;
+                }
+                tc_fence_after();
+                // diagonal d accumulates in columns [48 d, 48 d + 48).  The basis
+                // digit slices lie one after another along N, so one MMA of
+                // coefficient slice s against basis rows 0 .. 48 (9 - s) - 1,
+                // written from column 48 s on, adds A_s B_t to diagonal s + t
+                // for every t <= 8 - s (in two MMAs where N would pass 256).
+#pragma unroll
+                for (int kk = 0; kk < TC_K / 16; ++kk) {
+#pragma unroll
+                    for (int s = 0; s < NDIG; ++s) {
+                        const int ntot = TC_N * (NDIG - s);
+#pragma unroll
+                        for (int part = 0; part * 256 < ntot; ++part) {
+                            const int nn = ntot - part * 256 < 256 ? ntot - part * 256 : 256;
+                            const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nn >> 3) << 17) |
+                                                   ((uint32_t)(TC_M >> 4) << 24);
+                            // start-address field: (offset >> 4) adds without carry (smem < 256 KB)
+                            const uint64_t ad = ad0 + (uint64_t)((s * A_SLICE + kk * 256) >> 4);
+                            const uint64_t bd = bd0 + (uint64_t)((part * 256 / 8 * 1024 + kk * 256) >> 4);
+                            const uint32_t acc = (kk | s) ? 1u : 0u;
+                            asm volatile(
+                                "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                                    tmem + (uint32_t)(TC_N * s + 256 * part)),
+                                "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                                : "memory");
+                        }
                     }
                 }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(bar_mma))
+                             : "memory");
+                ++issued;
+                mbar_arrive(bar_ready);
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(bar_mma))
-                         : "memory");
         }
-        if (!mbar_wait(bar_mma, phase)) {
-            atomicExch(s_fail, 1);
-            mma_pending = true;
-        }
-        phase ^= 1;
-        tc_fence_after();
-        __syncthreads();
-        if (*(volatile int *)s_fail) break;
-
-        // ---- epilogue.  The x and p tiles of the group (64 rows x 48 columns)
-        // are staged in shared memory (the digit buffer is free once the MMAs
-        // are done) with coalesced loads; warp w then reads TMEM lanes
-        // 32 (w % 4) .. +31 (one output row per thread), columns 24 (w / 4) .. +23.
-        double *sXo = reinterpret_cast<double *>(sB);
-        double *sPo = sXo + 64 * SROW;
-        const int jbase = g * 64;
-        const int rows = min(64, a.m - jbase);
-        for (int e = tid; e < 64 * TC_N; e += TC_THREADS) {
-            const int jj = e / TC_N, cc = e % TC_N;
-            const unsigned ii = i0 + cc;
-            const bool in = jj < rows && ii < n;
-            const size_t o = (size_t)(jbase + jj) * ld + ii;
-            sXo[jj * SROW + cc] = in ? a.X[o] : 0.0;
-            sPo[jj * SROW + cc] = (in && a.Pmat) ? a.Pmat[o] : 0.0;
-        }
-        __syncthreads();
-        const int lq = warp & 3, ch = warp >> 2;
-        const int r = 32 * lq + lane;
-        const int which = r >> 6, jj = r & 63;
-        const bool live = jj < rows && (which == 0 || a.keep_p);
+    } else {
+        // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, columns
+        // 16 c .. 16 c + 15 with c = (w - 4) / 4; lane u < 16 holds the x row
+        // of shift 16 (w % 4) + u, lane u + 16 its p row.
+        const int q = warp & 3, cg = (warp - BUILD_WARPS) >> 2;
+        const int r = 32 * q + lane;
+        const int which = row_which(r);
+        const int j = g * 64 + row_shift(r);
+        const bool live = j < a.m;
+        const bool store = live && (which == 0 || a.keep_p);
         const int E = s_rowexp[r];
         const double own = s_rown[r];
-        for (int c = 0; c < 3; ++c) {
-            const int col0 = 24 * ch + 8 * c;
-            uint32_t dv[NDIAG][8];
-#pragma unroll
-            for (int d = 0; d < NDIAG; ++d) {
-                const uint32_t taddr = tmem + ((uint32_t)(32 * lq) << 16) + (uint32_t)(d * TC_N + col0);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                    : "=r"(dv[d][0]), "=r"(dv[d][1]), "=r"(dv[d][2]), "=r"(dv[d][3]), "=r"(dv[d][4]), "=r"(dv[d][5]),
-                      "=r"(dv[d][6]), "=r"(dv[d][7])
-                    : "r"(taddr));
+        double *const prim = which ? a.Pmat : a.X;  // the row this lane loads and writes
+        const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(cg * EPI_COLS);
+        int it = 0;
+        for (unsigned t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+            // the warp decides as one: tcgen05.ld and the shuffles below are warp-collective
+            bool bad = *(volatile int *)s_fail != 0;
+            if (!bad) bad = !mbar_wait(bar_ready, it & 1, s_fail) || !mbar_wait(bar_mma, it & 1, s_fail);
+            if (__any_sync(0xffffffffu, bad)) {
+                if (lane == 0) atomicExch(s_fail, 1);
+                break;
             }
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            double pn[8];
+            tc_fence_after();
+            // exact diagonal sums -> T = hs 2^35 + ls
+            long long hs[EPI_COLS], ls[EPI_COLS];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int cc = col0 + u;
-                const int F = s_colexp[cc];
-                double G = 0.0;
-                if (E != EXP_NONE && F != EXP_NONE) {
-                    // T = sum_d D_d 2^(7 (8 - d)) as hi * 2^35 + lo, both exact in int64
-                    long long hi = __float2int_rz(__uint_as_float(dv[0][u]));
+            for (int c4 = 0; c4 < EPI_COLS / 4; ++c4) {
+                uint32_t dv[NDIAG][4];
 #pragma unroll
-                    for (int d = 1; d < 4; ++d) hi = hi * 128 + __float2int_rz(__uint_as_float(dv[d][u]));
-                    long long lo = __float2int_rz(__uint_as_float(dv[4][u]));
+                for (int d = 0; d < NDIAG; ++d)
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                                 : "=r"(dv[d][0]), "=r"(dv[d][1]), "=r"(dv[d][2]), "=r"(dv[d][3])
+                                 : "r"(tbase + (uint32_t)(d * TC_N + 4 * c4)));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                    for (int d = 5; d < NDIAG; ++d) lo = lo * 128 + __float2int_rz(__uint_as_float(dv[d][u]));
-                    const long long q = lo >> 35;            // floor(lo / 2^35)
-                    const long long th = hi + q;             // T = th 2^35 + tl, 0 <= tl < 2^35
-                    const long long tl = lo - q * (1ll << 35);
-                    const int k = E + F - 70;
-                    G = i64_scaled(th, k + 35) + i64_scaled(tl, k);  // one rounding
+                for (int u = 0; u < 4; ++u) {
+                    uint32_t B[NDIAG];
+#pragma unroll
+                    for (int d = 0; d < NDIAG; ++d) B[d] = __float_as_uint(__uint_as_float(dv[d][u]) + MAGIC);
+                    const uint64_t h = (uint64_t)B[0] * (1u << 21) + (uint64_t)B[1] * (1u << 14) +
+                                       (uint64_t)B[2] * (1u << 7) + (uint64_t)B[3];
+                    const uint64_t l = (uint64_t)B[4] * (1u << 28) + (uint64_t)B[5] * (1u << 21) +
+                                       (uint64_t)B[6] * (1u << 14) + (uint64_t)B[7] * (1u << 7) + (uint64_t)B[8];
+                    hs[4 * c4 + u] = (long long)(h - HI_BIAS);
+                    ls[4 * c4 + u] = (long long)(l - LO_BIAS);
                 }
-                // x rows write now (they read the old p); p rows wait for the barrier
-                if (live && which == 0) sXo[jj * SROW + cc] = fma(own, sPo[jj * SROW + cc], sXo[jj * SROW + cc]) + G;
-                pn[u] = fma(own, sPo[jj * SROW + cc], G);
             }
-            __syncthreads();
-            if (live && which == 1) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar_tfree);
+
+            // x lanes load X, p lanes load Pmat (before the join, to hide the
+            // latency); x lanes take the old Pmat from their p lane before it
+            // is overwritten
+            const unsigned c0 = t * TC_N + cg * EPI_COLS;
+            const bool full = c0 + EPI_COLS <= n;
+            double pv[EPI_COLS];
+            const double *src = prim ? prim + (size_t)j * ld + c0 : nullptr;
+            if (live && src && full) {
 #pragma unroll
-                for (int u = 0; u < 8; ++u) sPo[jj * SROW + col0 + u] = pn[u];
+                for (int u = 0; u < EPI_COLS; u += 2) {
+                    const double2 w2 = __ldcs(reinterpret_cast<const double2 *>(src + u));
+                    pv[u] = w2.x;
+                    pv[u + 1] = w2.y;
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < EPI_COLS; ++u) pv[u] = (live && src && c0 + u < n) ? src[u] : 0.0;
+            }
+            const int *Fc = s_F + (it & 3) * TC_N + cg * EPI_COLS;
+            double G[EPI_COLS];
+#pragma unroll
+            for (int u = 0; u < EPI_COLS; ++u) {
+                const int F = Fc[u];
+                G[u] = (E != EXP_NONE && F != EXP_NONE) ? join_diagonals(hs[u], ls[u], E + F - 68) : 0.0;
+            }
+            const bool have_p = a.Pmat != nullptr;
+            double out[EPI_COLS];
+#pragma unroll
+            for (int u = 0; u < EPI_COLS; ++u) {
+                const double po = __shfl_xor_sync(0xffffffffu, pv[u], 16);
+                const double pold = which ? pv[u] : (have_p ? po : 0.0);
+                const double y = fma(own, pold, G[u]);
+                out[u] = which ? y : pv[u] + y;
+            }
+            if (store) {
+                double *dst = prim + (size_t)j * ld + c0;
+                if (full) {
+#pragma unroll
+                    for (int u = 0; u < EPI_COLS; u += 2)
+                        __stcs(reinterpret_cast<double2 *>(dst + u), make_double2(out[u], out[u + 1]));
+                } else {
+#pragma unroll
+                    for (int u = 0; u < EPI_COLS; ++u)
+                        if (c0 + u < n) dst[u] = out[u];
+                }
             }
         }
-        __syncthreads();
-        for (int e = tid; e < 64 * TC_N; e += TC_THREADS) {
-            const int jr = e / TC_N, cc = e % TC_N;
-            const unsigned ii = i0 + cc;
-            if (jr < rows && ii < n) {
-                const size_t o = (size_t)(jbase + jr) * ld + ii;
-                a.X[o] = sXo[jr * SROW + cc];
-                if (a.keep_p) a.Pmat[o] = sPo[jr * SROW + cc];
-            }
-        }
-        tc_fence_before();
-        __syncthreads();
     }
     // every path ends here: let copies and MMAs still in flight after a
     // timeout finish (bounded), then free TMEM
-    if (!a_ok) mbar_wait(bar_a, 0);
-    if (mma_pending) mbar_wait(bar_mma, phase ^ 1);
+    __syncthreads();
+    if (tid == 0 && *(volatile int *)s_fail) {
+        int dummy = 0;
+        if (!a_ok) mbar_wait(bar_a, 0, &dummy);
+        if (issued > 0) mbar_wait(bar_mma, (issued - 1) & 1, &dummy);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -491,7 +614,7 @@ int hbk_flush_tc_max_slots(void) { return TC_K; }
 int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
                      const double *own, int m, double *X, double *Pmat, int keep_p, void *ws, int *err,
                      cudaStream_t st) {
-    if (L > TC_K || L < 1 || m < 1 || n == 0) return (int)cudaErrorInvalidValue;
+    if (L > TC_K || L < 1 || m < 1 || n == 0 || (ld & 1)) return (int)cudaErrorInvalidValue;
     const int groups = (m + 63) / 64;
     unsigned char *w = (unsigned char *)ws;
     unsigned long long *slot_max = (unsigned long long *)(w + 256);
@@ -503,14 +626,14 @@ int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double
     dim3 gs(grid_for(n, 16) < 64 ? grid_for(n, 16) : 64, L);
     k_slot_max<<<gs, NT, 0, st>>>(V, ld, n, L, slot_max);
     k_flush_prep<<<dim3(TC_M, groups), TC_K, 0, st>>>(Xc, Pc, cap, own, m, L, slot_max, aimg, rowexp, rown);
-    static int attr_set = 0;
-    if (!attr_set) {
-        e = cudaFuncSetAttribute(k_flush_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-        if (e) return (int)e;
-        attr_set = 1;
-    }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
+    static unsigned attr_set = 0;  // one bit per device
+    if (dev < 32 && !(attr_set & (1u << dev))) {
+        e = cudaFuncSetAttribute(k_flush_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        if (e) return (int)e;
+        attr_set |= 1u << dev;
+    }
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const unsigned ntiles = (n + TC_N - 1) / TC_N;
     const unsigned gx = ntiles < (unsigned)sms ? ntiles : (unsigned)sms;
