@@ -138,18 +138,18 @@ __device__ __forceinline__ int exp_of_bits(uint64_t bits) {
 }
 
 // v * 2^(62 - scale) truncated toward zero, as a two's complement integer
-// (|v| < 2^scale, so the result is below 2^62), plus DIGIT_BIAS
+// (|v| < 2^scale, so the result is below 2^62), plus DIGIT_BIAS.  The
+// significand M < 2^53 is placed at M 2^10 and shifted right by
+// r = 1023 + scale - max(eb, 1) >= 0 (|v| < 2^scale bounds the left shift
+// M 2^(62 - scale + eb - 1075) by 2^10).
 __device__ __forceinline__ uint64_t biased62(uint64_t bits, int scale) {
     const int eb = (int)((bits >> 52) & 0x7ff);
     const uint64_t frac = bits & ((1ull << 52) - 1);
     const uint64_t M = eb ? (frac | (1ull << 52)) : frac;
-    const int sh = (eb ? eb : 1) - 1075 + 62 - scale;
-    uint64_t q = 0;
-    if (sh >= 0)
-        q = M << sh;
-    else if (sh > -64)
-        q = M >> (-sh);
-    if ((int64_t)bits < 0) q = 0 - q;
+    const int r = 1023 + scale - (eb ? eb : 1);
+    uint64_t q = r < 64 ? (M << 10) >> r : 0;
+    const uint64_t sg = (uint64_t)((int64_t)bits >> 63);  // 0 or all ones
+    q = (q ^ sg) - sg;
     return q + DIGIT_BIAS;
 }
 
@@ -179,42 +179,53 @@ __device__ __forceinline__ void store_digits(unsigned char *sB, uint32_t off, co
     if constexpr (S + 1 < NDIG) store_digits<S + 1>(sB, off, Us);
 }
 
-// round-to-nearest FP64 of W * 2^e, |W| < 2^63, built from bits (no FP64 op)
-__device__ __forceinline__ double i64_round(long long W, int e) {
-    if (W == 0) return 0.0;
-    const bool neg = W < 0;
-    const uint64_t u = neg ? (uint64_t)(-W) : (uint64_t)W;
-    int p = 63 - __clzll((long long)u);
-    uint64_t mant;
-    if (p <= 52) {
-        mant = u << (52 - p);
-    } else {
-        const int s = p - 52;
-        mant = u >> s;
-        const uint64_t rem = u & ((1ull << s) - 1), half = 1ull << (s - 1);
-        if (rem > half || (rem == half && (mant & 1))) {
-            ++mant;
-            if (mant == (1ull << 53)) {
-                mant >>= 1;
-                ++p;
-            }
-        }
-    }
-    const int eb = p + e + 1023;
-    if (eb >= 2047) return neg ? -INFINITY : INFINITY;
-    if (eb <= 0) return neg ? -0.0 : 0.0;  // below the normal range: negligible here
-    return __longlong_as_double((long long)(((uint64_t)neg << 63) | ((uint64_t)eb << 52) | (mant & ((1ull << 52) - 1))));
+// 32 x 32 + 64 -> 64-bit multiply-add
+__device__ __forceinline__ uint64_t madw(uint32_t a, uint32_t b, uint64_t c) {
+    uint64_t d;
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+    return d;
 }
 
 // the exact sum T = hs 2^35 + ls (|T| < 2^79) times 2^k, rounded to FP64
-// (a 62-bit window of T, then one rounding: error below 0.51 ulp)
+// (round half up on a 64-bit window of |T| whose leading bit is bit 63;
+// bits of |T| below the window only break exact ties: error <= 0.5 ulp + 2^-64)
 __device__ __forceinline__ double join_diagonals(long long hs, long long ls, int k) {
-    const long long th = hs + (ls >> 35);            // T = th 2^35 + tl, 0 <= tl < 2^35
-    const long long tl = ls & ((1ll << 35) - 1);
-    const int bl = 64 - __clzll(th ^ (th >> 63));    // bits of |th| (|th| < 2^45)
-    const int s = min(35, 62 - bl);
-    const long long W = (long long)((unsigned long long)th << s) + (tl >> (35 - s));
-    return i64_round(W, k + 35 - s);
+    const long long sg = (hs + (ls >> 35)) >> 63;  // sign of T = sign of floor(T / 2^35)
+    hs = (hs ^ sg) - sg;
+    ls = (ls ^ sg) - sg;
+    const unsigned long long th = (unsigned long long)(hs + (ls >> 35));  // |T| = th 2^35 + tl, th < 2^45
+    const unsigned long long tl = (unsigned long long)ls & ((1ull << 35) - 1);
+    unsigned long long W;
+    int lead;  // position of the leading bit of |T|
+    if (th >> 28) {
+        const int bl = 64 - __clzll((long long)th);  // 29..45
+        W = (th << (64 - bl)) | (tl >> (bl - 29));
+        lead = bl + 34;
+    } else {
+        const unsigned long long t64 = (th << 35) | tl;  // |T| < 2^63
+        if (t64 == 0) return 0.0;
+        const int z = __clzll((long long)t64);
+        W = t64 << z;
+        lead = 63 - z;
+    }
+    const unsigned long long mant = (W >> 11) + ((W >> 10) & 1);  // 2^52 .. 2^53 (carries into the exponent)
+    const int ebm1 = lead + k + 1022;                               // biased exponent - 1
+    if ((unsigned)ebm1 > 2044u) {
+        if (ebm1 < 0) return sg ? -0.0 : 0.0;  // below the normal range: negligible here
+        return sg ? -INFINITY : INFINITY;
+    }
+    const unsigned long long bits = ((unsigned long long)ebm1 << 52) + mant;
+    return __longlong_as_double((long long)(bits | ((unsigned long long)sg << 63)));
+}
+
+// one 32-byte sector per lane and instruction (x and p rows are read and
+// written 4 doubles at a time; 16-byte pieces of a sector written by separate
+// instructions cost partial-sector traffic)
+__device__ __forceinline__ void ld_sector(const double *p, double &a, double &b, double &c, double &d) {
+    asm volatile("ld.global.v4.f64 {%0,%1,%2,%3}, [%4];" : "=d"(a), "=d"(b), "=d"(c), "=d"(d) : "l"(p));
+}
+__device__ __forceinline__ void st_sector(double *p, double a, double b, double c, double d) {
+    asm volatile("st.global.v4.f64 [%0], {%1,%2,%3,%4};" ::"l"(p), "d"(a), "d"(b), "d"(c), "d"(d) : "memory");
 }
 
 struct TcArgs {
@@ -398,8 +409,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                 int e = EXP_NONE;
 #pragma unroll
                 for (int w = 0; w < 8; ++w) {
-                    const uint64_t bits = (uint64_t)__double_as_longlong(v[u][w]);
-                    if (bits << 1) e = max(e, exp_of_bits(bits) - s_slotexp[8 * io[u] + w]);
+                    // |v| < 2^(eb - 1022) for every v, zero and subnormals included
+                    const int eb = (int)((uint64_t)__double_as_longlong(v[u][w]) >> 52) & 0x7ff;
+                    e = max(e, eb - 1022 - s_slotexp[8 * io[u] + w]);
                 }
                 em[u] = e;
                 cexp[io[u] * TC_N + ii[u]] = e;
@@ -421,7 +433,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
 #pragma unroll
                 for (int w = 0; w < 8; ++w) {
                     const uint64_t bits = (uint64_t)__double_as_longlong(v[u][w]);
-                    U[u][w] = ((bits << 1) && F != EXP_NONE) ? biased62(bits, F + s_slotexp[8 * io[u] + w]) : DIGIT_BIAS;
+                    U[u][w] = biased62(bits, F + s_slotexp[8 * io[u] + w]);
                 }
             }
             // phase B: the digit buffer is free once the previous tile's MMAs are done
@@ -497,6 +509,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
         const double own = s_rown[r];
         double *const prim = which ? a.Pmat : a.X;  // the row this lane loads and writes
         const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(cg * EPI_COLS);
+        constexpr uint32_t m7 = 1u << 7, m14 = 1u << 14, m21 = 1u << 21, m28 = 1u << 28;
         int it = 0;
         for (unsigned t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
             // the warp decides as one: tcgen05.ld and the shuffles below are warp-collective
@@ -523,10 +536,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                     uint32_t B[NDIAG];
 #pragma unroll
                     for (int d = 0; d < NDIAG; ++d) B[d] = __float_as_uint(__uint_as_float(dv[d][u]) + MAGIC);
-                    const uint64_t h = (uint64_t)B[0] * (1u << 21) + (uint64_t)B[1] * (1u << 14) +
-                                       (uint64_t)B[2] * (1u << 7) + (uint64_t)B[3];
-                    const uint64_t l = (uint64_t)B[4] * (1u << 28) + (uint64_t)B[5] * (1u << 21) +
-                                       (uint64_t)B[6] * (1u << 14) + (uint64_t)B[7] * (1u << 7) + (uint64_t)B[8];
+                    const uint64_t h = madw(B[0], m21, madw(B[1], m14, madw(B[2], m7, (uint64_t)B[3])));
+                    const uint64_t l =
+                        madw(B[4], m28, madw(B[5], m21, madw(B[6], m14, madw(B[7], m7, (uint64_t)B[8]))));
                     hs[4 * c4 + u] = (long long)(h - HI_BIAS);
                     ls[4 * c4 + u] = (long long)(l - LO_BIAS);
                 }
@@ -536,49 +548,43 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
             if (lane == 0) mbar_arrive(bar_tfree);
 
             // x lanes load X, p lanes load Pmat (before the join, to hide the
-            // latency); x lanes take the old Pmat from their p lane before it
-            // is overwritten
+            // latency; 32-byte rows pieces, aligned since ld % 4 == 0 and
+            // c0 % 4 == 0); x lanes take the old Pmat from their p lane before
+            // it is overwritten
             const unsigned c0 = t * TC_N + cg * EPI_COLS;
             const bool full = c0 + EPI_COLS <= n;
             double pv[EPI_COLS];
             const double *src = prim ? prim + (size_t)j * ld + c0 : nullptr;
             if (live && src && full) {
 #pragma unroll
-                for (int u = 0; u < EPI_COLS; u += 2) {
-                    const double2 w2 = __ldcs(reinterpret_cast<const double2 *>(src + u));
-                    pv[u] = w2.x;
-                    pv[u + 1] = w2.y;
-                }
+                for (int u = 0; u < EPI_COLS; u += 4) ld_sector(src + u, pv[u], pv[u + 1], pv[u + 2], pv[u + 3]);
             } else {
 #pragma unroll
                 for (int u = 0; u < EPI_COLS; ++u) pv[u] = (live && src && c0 + u < n) ? src[u] : 0.0;
             }
             const int *Fc = s_F + (it & 3) * TC_N + cg * EPI_COLS;
-            double G[EPI_COLS];
-#pragma unroll
-            for (int u = 0; u < EPI_COLS; ++u) {
-                const int F = Fc[u];
-                G[u] = (E != EXP_NONE && F != EXP_NONE) ? join_diagonals(hs[u], ls[u], E + F - 68) : 0.0;
-            }
             const bool have_p = a.Pmat != nullptr;
-            double out[EPI_COLS];
+            double *dst = store ? prim + (size_t)j * ld + c0 : nullptr;
+            // one pass per four columns: join, own-vector terms, store
 #pragma unroll
-            for (int u = 0; u < EPI_COLS; ++u) {
-                const double po = __shfl_xor_sync(0xffffffffu, pv[u], 16);
-                const double pold = which ? pv[u] : (have_p ? po : 0.0);
-                const double y = fma(own, pold, G[u]);
-                out[u] = which ? y : pv[u] + y;
-            }
-            if (store) {
-                double *dst = prim + (size_t)j * ld + c0;
-                if (full) {
+            for (int u = 0; u < EPI_COLS; u += 4) {
+                double o4[4];
 #pragma unroll
-                    for (int u = 0; u < EPI_COLS; u += 2)
-                        __stcs(reinterpret_cast<double2 *>(dst + u), make_double2(out[u], out[u + 1]));
-                } else {
+                for (int h = 0; h < 4; ++h) {
+                    const double G = E != EXP_NONE ? join_diagonals(hs[u + h], ls[u + h], E + Fc[u + h] - 68) : 0.0;
+                    const double po = __shfl_xor_sync(0xffffffffu, pv[u + h], 16);
+                    const double pold = which ? pv[u + h] : (have_p ? po : 0.0);
+                    const double y = fma(own, pold, G);
+                    o4[h] = which ? y : pv[u + h] + y;
+                }
+                if (dst) {
+                    if (full)
+                        st_sector(dst + u, o4[0], o4[1], o4[2], o4[3]);
+                    else {
 #pragma unroll
-                    for (int u = 0; u < EPI_COLS; ++u)
-                        if (c0 + u < n) dst[u] = out[u];
+                        for (int h = 0; h < 4; ++h)
+                            if (c0 + u + h < n) dst[u + h] = o4[h];
+                    }
                 }
             }
         }
@@ -614,7 +620,9 @@ int hbk_flush_tc_max_slots(void) { return TC_K; }
 int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
                      const double *own, int m, double *X, double *Pmat, int keep_p, void *ws, int *err,
                      cudaStream_t st) {
-    if (L > TC_K || L < 1 || m < 1 || n == 0 || (ld & 1)) return (int)cudaErrorInvalidValue;
+    // x and p rows are accessed in 32-byte sectors: 32-byte aligned rows
+    if (L > TC_K || L < 1 || m < 1 || n == 0 || (ld & 3) || ((uintptr_t)X & 31) || ((uintptr_t)Pmat & 31))
+        return (int)cudaErrorInvalidValue;
     const int groups = (m + 63) / 64;
     unsigned char *w = (unsigned char *)ws;
     unsigned long long *slot_max = (unsigned long long *)(w + 256);
