@@ -47,6 +47,14 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def peaks_bf16():
+    """Dense BF16 tensor peak (TFLOP/s): the measured burst figure, else the fallback."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["bf16_tflops"])
+    return 1900.0
+
+
 # ------------------------------------------------------------- distributed
 class Dist:
     """Replica bookkeeping: barrier and max/sum reductions over ranks."""
@@ -164,6 +172,30 @@ def spmv_bytes(n: int, nnz: int) -> float:
     return 12.0 * nnz + 4.0 * (n + 1) + 16.0 * n
 
 
+# DRAM bytes (read + write) that ncu measured for one tensor-core flush launch,
+# per algorithmic byte (basis slots once, x_j read and written, Pmat_j read and
+# written): n = 2,097,152, 64 shifts, 51 slots (profiles/k_flush_tc_2M.md).
+FLUSH_TRAFFIC_PER_ALGORITHMIC_BYTE = 5.097 / 5.151
+
+
+def flush_roofline(bytes_per_launch: float, ms_per_launch: float, n: int, m: int, hbm: float, peak_kind: str):
+    """Roofline of the basis flush (the solve's dominant kernel in deferred
+    mode): its compulsory HBM bytes per launch over its device time per launch
+    (CUDA events around every flush of the timed solves, the small
+    slot-maximum and coefficient-digit kernels included).  The tensor-core
+    work behind it is reported beside: 45 digit-pair products over K = 64 per
+    48-element tile and group of 64 shifts, M = 128."""
+    achieved = bytes_per_launch / (ms_per_launch * 1e-3) / 1e9
+    tiles = -(-n // 48) * -(-m // 64)
+    tflop = tiles * 2.0 * 128 * 48 * 45 * 64 / 1e12
+    ratio = FLUSH_TRAFFIC_PER_ALGORITHMIC_BYTE
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": bytes_per_launch * ratio if ratio else None,
+            "kernel": "k_flush_tc (basis -> x_j, p_j on tcgen05 BF16 digit products)",
+            "bytes_per_launch": bytes_per_launch, "ms_per_launch": ms_per_launch, "peak_kind": peak_kind,
+            "tensor_tflops": tflop / (ms_per_launch * 1e-3), "tensor_peak_tflops": peaks_bf16()}
+
+
 # ------------------------------------------------------------- CPU baseline
 def load_profile(name: str, f):
     """Convergence profile of the reference's algorithm on a named workload
@@ -253,6 +285,8 @@ def run_ours(args, dist: Dist):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches = 0
     flush_ms = 0.0
+    flush_bytes = 0.0
+    flush_launches = 0
     with Clocks(dist.local) as clk:
         torch.cuda.synchronize()
         ev0.record(stream)
@@ -260,6 +294,9 @@ def run_ours(args, dist: Dist):
             res = solver.run(b, sig, seed=f.seed, x=x)
             launches += res.launches
             flush_ms += res.flush_ms
+            flush_bytes += res.flush_bytes
+            # mid-solve flushes plus the final one
+            flush_launches += (res.flushes + 1) if res.shift_mode == "deferred" else 0
         ev1.record(stream)
         torch.cuda.synchronize()
     dist.barrier()
@@ -280,6 +317,9 @@ def run_ours(args, dist: Dist):
     spmv = {"bound": "hbm", "achieved": sb / (spmv_ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
             "frac": sb / (spmv_ms * 1e-3) / 1e9 / hbm, "traffic": None, "kernel": "k_spmv",
             "bytes_per_launch": sb, "ms_per_launch": spmv_ms, "peak_kind": peak_kind}
+    roofline = spmv
+    if flush_launches and flush_ms > 0:
+        roofline = flush_roofline(flush_bytes / flush_launches, flush_ms / flush_launches, n, m, hbm, peak_kind)
 
     # e2e through the reference-facing C ABI with pinned host buffers
     e2e = None
@@ -323,7 +363,7 @@ def run_ours(args, dist: Dist):
         "iterations": res.k, "switches": res.switches, "max_true_residual": vres.max_true_residual,
         "all_converged": bool(np.all(vres.conv_k > 0)),
         "solve_breakdown_ms": {"flush": flush_ms / args.steps},
-        "roofline": spmv, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu,
+        "roofline": roofline, "roofline_spmv": spmv, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }
     solver.close()

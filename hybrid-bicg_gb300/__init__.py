@@ -71,7 +71,7 @@ class Stats(C.Structure):
     _fields_ = [("k", C.c_int), ("status", C.c_int), ("n_switches", C.c_int), ("final_seed", C.c_int),
                 ("shift_mode", C.c_int), ("basis_flushes", C.c_int), ("launches", C.c_int),
                 ("solve_ms", C.c_double), ("flush_ms", C.c_double), ("max_true_residual", C.c_double),
-                ("bytes_algorithmic", C.c_double),
+                ("bytes_algorithmic", C.c_double), ("flush_bytes", C.c_double),
                 ("switch_k", _PI), ("switch_seed", _PI), ("conv_k", _PI), ("active_per_iter", _PI),
                 ("true_residual", _PD), ("seed_alpha", _PD), ("seed_beta", _PD), ("seed_omega", _PD),
                 ("seed_rr", _PD)]
@@ -181,6 +181,7 @@ class SolveResult:
     launches: int
     flushes: int
     bytes_algorithmic: float
+    flush_bytes: float = 0.0
     true_residual: np.ndarray | None = None
     extra: dict = field(default_factory=dict)
 
@@ -220,6 +221,7 @@ def _result(st: Stats, bufs, m, x, r, want_res) -> SolveResult:
                        shift_mode={1: "incremental", 2: "deferred"}.get(st.shift_mode, "?"), solve_ms=st.solve_ms,
                        flush_ms=st.flush_ms,
                        launches=st.launches, flushes=st.basis_flushes, bytes_algorithmic=st.bytes_algorithmic,
+                       flush_bytes=st.flush_bytes,
                        true_residual=bufs["true_residual"][:m].copy() if want_res else None,
                        extra={"hist": {"alpha": bufs["seed_alpha"][:st.k].copy(), "beta": bufs["seed_beta"][:st.k].copy(),
                                        "omega": bufs["seed_omega"][:st.k].copy(), "rr": bufs["seed_rr"][:st.k].copy()}})

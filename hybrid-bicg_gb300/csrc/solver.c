@@ -367,6 +367,7 @@ struct hbicg_solver {
     void *tc_ws;      /* tensor-core flush workspace (deferred mode) */
     int *d_tc_err;    /* set by the tensor-core flush on a bounded-wait timeout */
     int launches_per_iter;
+    double flush_bytes; /* compulsory HBM bytes of this solve's basis flushes */
 };
 
 static int pick_mode(const hbicg_params *p, unsigned n, int m) {
@@ -737,6 +738,8 @@ static int ensure_pmat(hbicg_solver *s) {
  * the basis fits one K = 64 operand, else with the FP64 kernel; then reset. */
 static int do_flush(hbicg_solver *s, int keep_p, int L, int *launches) {
     cudaStream_t st = s->ctx->stream;
+    /* basis slots read once; x_j read and written; Pmat_j read (and written) */
+    s->flush_bytes += 8.0 * s->A->k.n * ((double)L + (keep_p ? 4.0 : 3.0) * s->m);
     if (s->tc_ws && L >= 1 && L <= hbk_flush_tc_max_slots()) {
         HBK_TRY(hbk_flush_tc_run(s->v.V, s->ld, s->A->k.n, L, s->v.Xc, s->v.Pc, s->v.slot_cap, s->v.own, s->m, s->v.X,
                                  s->v.Pmat, keep_p, s->tc_ws, s->d_tc_err, st));
@@ -857,6 +860,7 @@ int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int 
     CUDA_TRY(cudaEventRecord(ctx->ev0, st));
     int rc = HBICG_OK, launches = 0, flushes = 0;
     double flush_ms = 0.0;
+    s->flush_bytes = 0.0;
     int k = 1, n_sw = 0, final_seed = seed, status = HBICG_OK;
     int *sw_k = calloc(m > 0 ? m : 1, sizeof(int)), *sw_seed = calloc(m > 0 ? m : 1, sizeof(int));
     int *conv = calloc(m > 0 ? m : 1, sizeof(int));
@@ -940,6 +944,7 @@ int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int 
         stats->flush_ms = flush_ms;
         stats->max_true_residual = maxres;
         stats->bytes_algorithmic = algorithmic_bytes(s, k, act);
+        stats->flush_bytes = s->flush_bytes;
         int nl = n_sw < m ? n_sw : m;
         if (stats->switch_k) memcpy(stats->switch_k, sw_k, sizeof(int) * nl);
         if (stats->switch_seed) memcpy(stats->switch_seed, sw_seed, sizeof(int) * nl);

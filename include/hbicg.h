@@ -76,6 +76,7 @@ typedef struct {
     double flush_ms;          /* deferred mode: device time of the basis flushes */
     double max_true_residual; /* when params.true_residuals */
     double bytes_algorithmic; /* compulsory HBM bytes of the fused schedule for this solve */
+    double flush_bytes;       /* deferred mode: compulsory HBM bytes of the basis flushes (in flush_ms) */
     /* optional caller-owned outputs (NULL to skip) */
     int *switch_k;            /* [m] iteration of each switch */
     int *switch_seed;         /* [m] seed chosen at each switch */
