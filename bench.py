@@ -174,7 +174,7 @@ def spmv_bytes(n: int, nnz: int) -> float:
 
 # DRAM bytes (read + write) that ncu measured for one tensor-core flush launch,
 # per algorithmic byte (basis slots once, x_j read and written, Pmat_j read and
-# written): n = 2,097,152, 64 shifts, 51 slots (profiles/k_flush_tc_2M.md).
+# written), on `bench.py --kernel flush --n 2097152` (64 shifts, 51 slots).
 FLUSH_TRAFFIC_PER_ALGORITHMIC_BYTE = 5.097 / 5.151
 
 
@@ -393,6 +393,60 @@ def run_reference(args, dist: Dist):
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_flush_kernel(args):
+    """The basis flush alone (hbk_flush_tc_run: slot maxima, coefficient
+    digits, the tensor-core kernel) on random FP64 data of a solve's shape:
+    n elements, 64 shifts, 51 basis slots, p kept.  CUDA events around
+    `--steps` calls after `--warmup`; algorithmic bytes 8 n (L + 4 m)."""
+    import ctypes as C
+
+    import torch
+
+    pkg = graft.load_package()
+    lib = pkg.lib()
+    fn = lib.hbk_flush_tc_run
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.c_size_t, C.c_uint, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                   C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.hbk_flush_tc_workspace_bytes.restype = C.c_size_t
+    lib.hbk_flush_tc_workspace_bytes.argtypes = [C.c_int]
+    n, m, L, cap = args.n, 64, 51, 72
+    ld = (n + 31) // 32 * 32
+    g = torch.Generator(device="cuda").manual_seed(0)
+    V = torch.randn(L, ld, dtype=torch.float64, device="cuda", generator=g)
+    X = torch.randn(m, ld, dtype=torch.float64, device="cuda", generator=g)
+    P = torch.randn(m, ld, dtype=torch.float64, device="cuda", generator=g)
+    Xc = torch.randn(m, cap, dtype=torch.float64, device="cuda", generator=g)
+    Pc = torch.randn(m, cap, dtype=torch.float64, device="cuda", generator=g)
+    own = torch.randn(m, 2, dtype=torch.float64, device="cuda", generator=g)
+    ws = torch.zeros(int(lib.hbk_flush_tc_workspace_bytes(m)) // 8 + 1, dtype=torch.float64, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        rc = fn(V.data_ptr(), ld, n, L, Xc.data_ptr(), Pc.data_ptr(), cap, own.data_ptr(), m, X.data_ptr(),
+                P.data_ptr(), 1, ws.data_ptr(), err.data_ptr(), st)
+        if rc:
+            raise RuntimeError(f"hbk_flush_tc_run returned {rc}")
+
+    for _ in range(args.warmup):
+        call()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        call()
+    e1.record()
+    torch.cuda.synchronize()
+    if int(err.item()):
+        raise RuntimeError("tensor-core flush reported a wait timeout")
+    ms = e0.elapsed_time(e1) / args.steps
+    byt = 8.0 * n * (L + 4 * m)
+    hbm, kind = peaks()
+    return {"kernel": "k_flush_tc", "n": n, "shifts": m, "slots": L, "ms_per_launch": ms, "bytes_per_launch": byt,
+            "achieved_gbs": byt / (ms * 1e-3) / 1e9, "frac": byt / (ms * 1e-3) / 1e9 / hbm, "peak_kind": kind}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -407,7 +461,13 @@ def main(argv=None):
     ap.add_argument("--basis-block", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel", default=None, choices=["flush"],
+                    help="time one kernel alone on random data instead of the solve")
+    ap.add_argument("--n", type=int, default=2097152, help="elements for --kernel")
     args = ap.parse_args(argv)
+    if args.kernel == "flush":
+        print(json.dumps(run_flush_kernel(args)), flush=True)
+        return
     if args.impl == "ours" and args.warmup < 3:
         args.warmup = 3
     dist = Dist()
