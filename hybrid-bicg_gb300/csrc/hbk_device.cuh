@@ -174,6 +174,29 @@ __device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__r
         else kern<HBK_FMT_TILE><<<grid, block, 0, stream>>>(__VA_ARGS__);                  \
     } while (0)
 
+// number of SMs of the current device (cached: one device type per process)
+inline int sm_count() {
+    static const int sms = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
+    return sms;
+}
+
+// At most one wave of a grid-stride kernel K: the blocks of NT threads that
+// are resident on all SMs at once (more blocks only add a partial second wave).
+template <auto K>
+inline int wave_grid(int want) {
+    static const int one_wave = [] {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, K, NT, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+        return per_sm * sm_count();
+    }();
+    return want < one_wave ? want : one_wave;
+}
+
 inline int grid_for(unsigned n, int per_thread) {
     static int sms = 0;
     if (!sms) {

@@ -771,16 +771,23 @@ int hbk_fused_init(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *
 int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, cudaStream_t st) {
     Ctx c = make_ctx(A, v, sh);
     const int gv = grid_for(v->n, 2);
-    HBK_LAUNCH_FMT(*A, k_seed_s, A->grid, NT, st, c);
-    k_seed_q<<<gv, NT, 0, st>>>(c);
-    HBK_LAUNCH_FMT(*A, k_seed_y, A->grid, NT, st, c);
-    k_seed_update<<<gv, NT, 0, st>>>(c);
-    if (!v->deferred) {
-        k_shift_update<64><<<gv, NT, 0, st>>>(c);
+    // every kernel here is a grid-stride loop: launch at most one wave of it
+    if (A->fmt == HBK_FMT_SELL) {
+        k_seed_s<HBK_FMT_SELL><<<wave_grid<k_seed_s<HBK_FMT_SELL>>(A->grid), NT, 0, st>>>(c);
+        k_seed_q<<<wave_grid<k_seed_q>(gv), NT, 0, st>>>(c);
+        k_seed_y<HBK_FMT_SELL><<<wave_grid<k_seed_y<HBK_FMT_SELL>>(A->grid), NT, 0, st>>>(c);
     } else {
-        k_seed_p_deferred<<<gv, NT, 0, st>>>(c);
+        k_seed_s<HBK_FMT_TILE><<<wave_grid<k_seed_s<HBK_FMT_TILE>>(A->grid), NT, 0, st>>>(c);
+        k_seed_q<<<wave_grid<k_seed_q>(gv), NT, 0, st>>>(c);
+        k_seed_y<HBK_FMT_TILE><<<wave_grid<k_seed_y<HBK_FMT_TILE>>(A->grid), NT, 0, st>>>(c);
+    }
+    k_seed_update<<<wave_grid<k_seed_update>(gv), NT, 0, st>>>(c);
+    if (!v->deferred) {
+        k_shift_update<64><<<wave_grid<k_shift_update<64>>(gv), NT, 0, st>>>(c);
+    } else {
+        k_seed_p_deferred<<<wave_grid<k_seed_p_deferred>(gv), NT, 0, st>>>(c);
         k_coef_update<<<grid_for((unsigned)((size_t)sh->m * v->slot_cap), 1), NT, 0, st>>>(c);
-        k_materialize_ps<<<gv, NT, 0, st>>>(c);
+        k_materialize_ps<<<wave_grid<k_materialize_ps>(gv), NT, 0, st>>>(c);
     }
     return (int)cudaGetLastError();
 }
