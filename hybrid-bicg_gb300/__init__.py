@@ -77,6 +77,11 @@ class Stats(C.Structure):
                 ("seed_rr", _PD)]
 
 
+class Coo(C.Structure):
+    _fields_ = [("rows", C.c_uint), ("cols", C.c_uint), ("nnz", C.c_ulonglong), ("field", C.c_int),
+                ("symmetry", C.c_int), ("expanded", C.c_int), ("row", _PU), ("col", _PU), ("val", _PD)]
+
+
 _lib = None
 
 
@@ -98,6 +103,14 @@ def lib() -> C.CDLL:
         "hbicg_matrix_create": (C.c_int, [C.c_void_p, C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                           C.POINTER(C.c_void_p)]),
         "hbicg_matrix_destroy": (None, [C.c_void_p]),
+        "hbicg_matrix_rows": (C.c_uint, [C.c_void_p]),
+        "hbicg_matrix_nnz": (C.c_ulonglong, [C.c_void_p]),
+        "hbicg_mm_read": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(Coo)]),
+        "hbicg_coo_free": (None, [C.POINTER(Coo)]),
+        "hbicg_matrix_from_coo": (C.c_int, [C.c_void_p, C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_int, C.POINTER(C.c_void_p)]),
+        "hbicg_matrix_load_mm": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
+        "hbicg_matrix_get_csr": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
         "hbicg_matrix_spmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
         "hbicg_matrix_time_spmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
                                              C.POINTER(C.c_double)]),
@@ -277,6 +290,46 @@ class Context:
 class Matrix:
     """Device CSR + SpMV schedule.  ptr/col/val: numpy (copied) or torch CUDA tensors (used in place)."""
 
+    @classmethod
+    def _wrap(cls, ctx: Context, h) -> "Matrix":
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self._keep = ()
+        self.h = h
+        self.n = int(lib().hbicg_matrix_rows(h))
+        self.nnz = int(lib().hbicg_matrix_nnz(h))
+        return self
+
+    @classmethod
+    def from_coo(cls, ctx: Context, n: int, row, col, val) -> "Matrix":
+        """CSR built on the GPU from triplets (numpy host arrays or torch CUDA
+        tensors): row order, entries of a row in their given order."""
+        where = HOST if isinstance(row, np.ndarray) else DEVICE
+        if where == HOST:
+            row = np.ascontiguousarray(row, dtype=np.uint32)
+            col = np.ascontiguousarray(col, dtype=np.uint32)
+            val = np.ascontiguousarray(val, dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib().hbicg_matrix_from_coo(ctx.h, int(n), int(row.shape[0]), _ptr(row), _ptr(col), _ptr(val), where,
+                                           C.byref(h)), "hbicg_matrix_from_coo")
+        return cls._wrap(ctx, h)
+
+    @classmethod
+    def load_mm(cls, ctx: Context, path: str, expand_symmetric: bool = False) -> "Matrix":
+        """Matrix Market file -> device CSR (parallel parse, GPU COO -> CSR)."""
+        h = C.c_void_p()
+        _check(lib().hbicg_matrix_load_mm(ctx.h, str(path).encode(), int(bool(expand_symmetric)), C.byref(h)),
+               "hbicg_matrix_load_mm")
+        return cls._wrap(ctx, h)
+
+    def csr(self):
+        """(ptr, col, val) copied to numpy."""
+        ptr = np.zeros(self.n + 1, dtype=np.uint32)
+        col = np.zeros(self.nnz, dtype=np.uint32)
+        val = np.zeros(self.nnz, dtype=np.float64)
+        _check(lib().hbicg_matrix_get_csr(self.h, _ptr(ptr), _ptr(col), _ptr(val), HOST), "hbicg_matrix_get_csr")
+        return ptr, col, val
+
     def __init__(self, ctx: Context, ptr, col, val):
         self.ctx = ctx
         self._keep = (ptr, col, val)
@@ -425,6 +478,24 @@ def mult(a, x, y=None) -> np.ndarray:
     yy = np.zeros(n) if y is None else np.ascontiguousarray(y, dtype=np.float64)
     L.mult(C.byref(A), xx.ctypes.data_as(_PD), yy.ctypes.data_as(_PD))
     return yy
+
+
+def read_mm(path: str, expand_symmetric: bool = False, threads: int = 0) -> dict:
+    """Parallel Matrix Market read (hbicg_mm_read) -> dict of numpy arrays
+    row, col (0-based), val in file order, plus rows, cols, field, symmetry."""
+    c = Coo()
+    _check(lib().hbicg_mm_read(str(path).encode(), int(bool(expand_symmetric)), int(threads), C.byref(c)),
+           "hbicg_mm_read")
+    try:
+        nnz = int(c.nnz)
+        out = {"rows": int(c.rows), "cols": int(c.cols), "field": ["real", "integer", "pattern"][c.field],
+               "symmetry": ["general", "symmetric", "skew-symmetric"][c.symmetry], "expanded": bool(c.expanded),
+               "row": np.ctypeslib.as_array(c.row, shape=(nnz,)).copy() if nnz else np.zeros(0, np.uint32),
+               "col": np.ctypeslib.as_array(c.col, shape=(nnz,)).copy() if nnz else np.zeros(0, np.uint32),
+               "val": np.ctypeslib.as_array(c.val, shape=(nnz,)).copy() if nnz else np.zeros(0)}
+    finally:
+        lib().hbicg_coo_free(C.byref(c))
+    return out
 
 
 def load_matrix_market(path: str):

@@ -155,6 +155,10 @@ int hbk_true_residuals(const hbk_matrix *A, const double *X, const double *b, co
  * p_j = rho_j Pmat_j + Pc_j . V over the first L <= hbk_flush_tc_max_slots()
  * slots, FP64-accurate; ws of hbk_flush_tc_workspace_bytes(m) bytes; *err set
  * on a bounded-wait timeout.  No reset (see hbk_deferred_reset). */
+/* COO -> CSR on the device, stable within rows (csrc/coo_csr.cu) */
+size_t hbk_coo_to_csr_tmp_bytes(unsigned nnz);
+int hbk_coo_to_csr(unsigned n, unsigned nnz, const unsigned *row, const unsigned *col, const double *val,
+                   unsigned *ptr, unsigned *col_out, double *val_out, void *tmp, int *err, cudaStream_t st);
 size_t hbk_flush_tc_workspace_bytes(int m);
 int hbk_flush_tc_max_slots(void);
 int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,

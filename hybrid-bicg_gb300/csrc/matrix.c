@@ -77,19 +77,22 @@ static void read_entry(FILE *f, MM_typecode code, unsigned *row, unsigned *col, 
     *val = v;
 }
 
+/* The reference's loader (src/matrix.c:26-94): same entries, same values,
+ * same exit on a bad file; the parsing runs on all host cores
+ * (hbicg_mm_read).  Returns whether the file is stored as symmetric. */
 int coo_load_matrix(char *filename, COO_Matrix *coo) {
-    MM_typecode code;
-    int M, N, nz;
-    FILE *f = open_mtx(filename, &code, &M, &N, &nz);
-    coo->rows = (unsigned)M;
-    coo->cols = (unsigned)N;
-    coo->nz = (unsigned)nz;
-    coo->val = malloc(sizeof(double) * ((size_t)nz + 1));
-    coo->row = malloc(sizeof(unsigned) * ((size_t)nz + 1));
-    coo->col = malloc(sizeof(unsigned) * ((size_t)nz + 1));
-    for (int i = 0; i < nz; i++) read_entry(f, code, &coo->row[i], &coo->col[i], &coo->val[i]);
-    fclose(f);
-    return mm_is_symmetric(code);
+    hbicg_coo c;
+    if (hbicg_mm_read(filename, 0, 0, &c) != HBICG_OK) {
+        fprintf(stderr, "ERROR: %s\n", hbicg_last_message());
+        exit(EXIT_FAILURE);
+    }
+    coo->rows = c.rows;
+    coo->cols = c.cols;
+    coo->nz = (unsigned)c.nnz;
+    coo->val = c.val;
+    coo->row = c.row;
+    coo->col = c.col;
+    return c.symmetry == 1;
 }
 
 void coo_copy(COO_Matrix *in, COO_Matrix *out) {

@@ -116,6 +116,38 @@ int hbicg_matrix_spmv(hbicg_matrix *A, const double *x, double *y, double sigma,
  * x, y) between CUDA events on the context's stream; *ms = mean per launch. */
 int hbicg_matrix_time_spmv(hbicg_matrix *A, const double *x, double *y, double sigma, int iters, double *ms);
 
+/* Coordinate (triplet) matrix in host memory, 0-based, as read from a file. */
+typedef struct {
+    unsigned rows, cols;
+    unsigned long long nnz;
+    int field;     /* 0 real, 1 integer, 2 pattern (values 1.0) */
+    int symmetry;  /* 0 general, 1 symmetric, 2 skew-symmetric */
+    int expanded;  /* mirrored off-diagonal entries appended after the stored ones */
+    unsigned *row, *col;
+    double *val;
+} hbicg_coo;
+
+/* Parallel Matrix Market reader (replaces src/matrix.c:26-94 / src/mmio.c's
+ * one-fscanf-per-entry loop): `threads` host threads (0 = all cores), entries
+ * in file order, values converted exactly as fscanf("%lg") does.  Symmetric
+ * and skew-symmetric files are returned as stored unless expand_symmetric.
+ * Errors (I/O, bad banner, bad entry, entry count) return HBICG_E_IO with a
+ * message; nothing exits.  Free with hbicg_coo_free. */
+int hbicg_mm_read(const char *path, int expand_symmetric, int threads, hbicg_coo *out);
+void hbicg_coo_free(hbicg_coo *coo);
+
+/* Square CSR matrix from COO triplets, built on the GPU: entries are ordered
+ * by row with the order of entries inside a row kept (the ordering of the
+ * reference's coo2csr, src/matrix.c:206-242).  row/col/val are host or device
+ * pointers per `where`; indices must be < n (else HBICG_E_ARG). */
+int hbicg_matrix_from_coo(hbicg_context *ctx, unsigned n, unsigned nnz, const unsigned *row, const unsigned *col,
+                          const double *val, int where, hbicg_matrix **out);
+/* Copy the matrix's CSR arrays out (ptr [n+1], col and val [nnz]) to host or
+ * device memory per `where`. */
+int hbicg_matrix_get_csr(const hbicg_matrix *A, unsigned *ptr, unsigned *col, double *val, int where);
+/* hbicg_mm_read + hbicg_matrix_from_coo (the file must be square). */
+int hbicg_matrix_load_mm(hbicg_context *ctx, const char *path, int expand_symmetric, hbicg_matrix **out);
+
 /* Workspace for families of m shifts on A (device vectors, scalar state, graphs). */
 int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_params *p, hbicg_solver **out);
 void hbicg_solver_destroy(hbicg_solver *s);
