@@ -447,6 +447,107 @@ def run_flush_kernel(args):
             "achieved_gbs": byt / (ms * 1e-3) / 1e9, "frac": byt / (ms * 1e-3) / 1e9 / hbm, "peak_kind": kind}
 
 
+def run_coo2csr_kernel(args):
+    """COO -> CSR of a workload's matrix (its triplets in a random order) on
+    the GPU (hbk_coo_to_csr: stable radix sort by row, row pointers, gather;
+    device buffers, CUDA events) beside the reference's host algorithm (a
+    stable counting sort by row, then the row cut: coo2csr, one core)."""
+    import ctypes as C
+
+    import torch
+
+    pkg, f = workload(args.workload, args.scale)
+    a = f.a
+    n, nnz = a.n, a.nnz
+    rng = np.random.default_rng(0)
+    perm = rng.permutation(nnz)
+    row = np.repeat(np.arange(n, dtype=np.uint32), np.diff(a.ptr.astype(np.int64)))[perm]
+    col = a.col.astype(np.uint32)[perm]
+    val = a.val[perm]
+    lib = pkg.lib()
+    lib.hbk_coo_to_csr_tmp_bytes.restype = C.c_size_t
+    lib.hbk_coo_to_csr_tmp_bytes.argtypes = [C.c_uint]
+    fn = lib.hbk_coo_to_csr
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_uint, C.c_uint] + [C.c_void_p] * 8 + [C.c_void_p]
+    d_row = torch.from_numpy(row.astype(np.int32)).cuda()
+    d_col = torch.from_numpy(col.astype(np.int32)).cuda()
+    d_val = torch.from_numpy(val).cuda()
+    ptr = torch.empty(n + 1, dtype=torch.int32, device="cuda")
+    col_o = torch.empty(nnz, dtype=torch.int32, device="cuda")
+    val_o = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    tmp = torch.empty(int(lib.hbk_coo_to_csr_tmp_bytes(nnz)), dtype=torch.uint8, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        rc = fn(n, nnz, d_row.data_ptr(), d_col.data_ptr(), d_val.data_ptr(), ptr.data_ptr(), col_o.data_ptr(),
+                val_o.data_ptr(), tmp.data_ptr(), err.data_ptr(), st)
+        if rc:
+            raise RuntimeError(f"hbk_coo_to_csr returned {rc}")
+
+    for _ in range(args.warmup):
+        call()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        call()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    ok = int(err.item()) == 0 and np.array_equal(ptr.cpu().numpy().astype(np.uint32), a.ptr.astype(np.uint32))
+    # the reference's host algorithm on the same triplets
+    coo = pkg.COO_Matrix()
+    coo.val = val.ctypes.data_as(C.POINTER(C.c_double))
+    coo.row = row.ctypes.data_as(C.POINTER(C.c_uint))
+    coo.col = col.ctypes.data_as(C.POINTER(C.c_uint))
+    coo.nz, coo.rows, coo.cols = nnz, n, n
+    out = pkg.CSR_Matrix()
+    t0 = time.perf_counter()
+    lib.coo2csr(C.byref(coo), C.byref(out))
+    host_s = time.perf_counter() - t0
+    same = (np.array_equal(np.ctypeslib.as_array(out.ptr, shape=(n + 1,)), ptr.cpu().numpy().astype(np.uint32))
+            and np.array_equal(np.ctypeslib.as_array(out.col, shape=(nnz,)), col_o.cpu().numpy().astype(np.uint32))
+            and np.array_equal(np.ctypeslib.as_array(out.val, shape=(nnz,)), val_o.cpu().numpy()))
+    lib.csr_free_matrix(C.byref(out))
+    byt = 28.0 * nnz + 4.0 * (n + 1)  # triplets read once, col/val written once, ptr written
+    hbm, kind = peaks()
+    return {"kernel": "hbk_coo_to_csr", "workload": args.workload, "n": n, "nnz": nnz, "ms": ms,
+            "entries_per_s": nnz / (ms * 1e-3), "algorithmic_gbs": byt / (ms * 1e-3) / 1e9,
+            "frac": byt / (ms * 1e-3) / 1e9 / hbm, "peak_kind": kind, "error_flag": int(err.item()),
+            "host_reference_algorithm_s": host_s, "identical_to_host": bool(same and ok)}
+
+
+def run_mmread(args):
+    """Matrix Market read of a workload's matrix: the parallel reader on all
+    host cores beside the same reader on one core (the reference reads with one
+    fscanf per entry on one core)."""
+    import tempfile
+
+    pkg, f = workload(args.workload, args.scale)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "a.mtx")
+        t0 = time.perf_counter()
+        pkg.workloads.write_matrix_market(path, f.a)
+        write_s = time.perf_counter() - t0
+        size = os.path.getsize(path)
+        times = {}
+        for th in (1, 0):
+            best = None
+            for _ in range(max(1, args.steps)):
+                t0 = time.perf_counter()
+                c = pkg.read_mm(path, threads=th)
+                dt = time.perf_counter() - t0
+                best = dt if best is None else min(best, dt)
+            times["all_cores" if th == 0 else "one_core"] = best
+        same = len(c["val"]) == f.a.nnz
+    return {"kernel": "hbicg_mm_read", "workload": args.workload, "n": f.a.n, "nnz": f.a.nnz, "file_bytes": size,
+            "s_all_cores": times["all_cores"], "s_one_core": times["one_core"], "cores": os.cpu_count(),
+            "speedup": times["one_core"] / times["all_cores"], "MB_per_s": size / times["all_cores"] / 1e6,
+            "write_s": write_s, "entries_ok": bool(same)}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -461,12 +562,13 @@ def main(argv=None):
     ap.add_argument("--basis-block", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel", default=None, choices=["flush"],
+    ap.add_argument("--kernel", default=None, choices=["flush", "coo2csr", "mmread"],
                     help="time one kernel alone on random data instead of the solve")
     ap.add_argument("--n", type=int, default=2097152, help="elements for --kernel")
     args = ap.parse_args(argv)
-    if args.kernel == "flush":
-        print(json.dumps(run_flush_kernel(args)), flush=True)
+    if args.kernel:
+        run = {"flush": run_flush_kernel, "coo2csr": run_coo2csr_kernel, "mmread": run_mmread}[args.kernel]
+        print(json.dumps(run(args)), flush=True)
         return
     if args.impl == "ours" and args.warmup < 3:
         args.warmup = 3

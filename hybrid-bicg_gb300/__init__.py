@@ -49,6 +49,11 @@ def build(jobs: int | None = None, quiet: bool = True) -> Path:
 
 
 # ---------------------------------------------------------------- ctypes types
+class COO_Matrix(C.Structure):
+    """src/matrix.h:11-18"""
+    _fields_ = [("val", _PD), ("row", _PU), ("col", _PU), ("nz", C.c_uint), ("rows", C.c_uint), ("cols", C.c_uint)]
+
+
 class CSR_Matrix(C.Structure):
     """src/matrix.h:19-26"""
     _fields_ = [("val", _PD), ("col", _PU), ("ptr", _PU), ("nz", C.c_uint), ("rows", C.c_uint), ("cols", C.c_uint)]
@@ -136,6 +141,7 @@ def lib() -> C.CDLL:
         "MPI_csr_load_matrix_block": (None, [C.c_char_p, C.POINTER(CSR_Matrix), C.POINTER(CSR_Matrix),
                                              C.POINTER(INFO_Matrix)]),
         "csr_free_matrix": (None, [C.POINTER(CSR_Matrix)]),
+        "coo2csr": (None, [C.POINTER(COO_Matrix), C.POINTER(CSR_Matrix)]),
         "csr_init_matrix": (None, [C.POINTER(CSR_Matrix)]),
     }
     for name, (res, args) in sig.items():
