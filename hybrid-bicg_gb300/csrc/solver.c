@@ -15,11 +15,17 @@
  * seed's Krylov basis and formed once at the end by an FP64 GEMM-like kernel
  * (deferred), which cuts the FP64 work per shift per iteration by three.
  */
+#define _GNU_SOURCE
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+
+#include <fcntl.h>
+#include <pthread.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <cuda_runtime.h>
 
@@ -98,11 +104,21 @@ struct hbicg_context {
     cudaEvent_t ev0, ev1, evf0, evf1;
     hbk_scalars *h_sc; /* pinned */
     double *h_dbl;     /* pinned scratch */
+    int refs;          /* the caller's handle + one per live matrix or solver */
 };
+
+static void ctx_retain(hbicg_context *c) { __atomic_add_fetch(&c->refs, 1, __ATOMIC_RELAXED); }
+static void ctx_free(hbicg_context *c);
+/* the context is freed when its handle and every matrix and solver made on it
+ * are gone, in whatever order a caller (or a garbage collector) destroys them */
+static void ctx_release(hbicg_context *c) {
+    if (__atomic_sub_fetch(&c->refs, 1, __ATOMIC_ACQ_REL) == 0) ctx_free(c);
+}
 
 int hbicg_context_create(hbicg_context **out) {
     hbicg_context *c = calloc(1, sizeof *c);
     if (!c) return HBICG_E_NOMEM;
+    c->refs = 1;
     CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreate(&c->ev0));
     CUDA_TRY(cudaEventCreate(&c->ev1));
@@ -115,7 +131,10 @@ int hbicg_context_create(hbicg_context **out) {
 }
 
 void hbicg_context_destroy(hbicg_context *c) {
-    if (!c) return;
+    if (c) ctx_release(c);
+}
+
+static void ctx_free(hbicg_context *c) {
     cudaStreamSynchronize(c->stream);
     cudaFreeHost(c->h_sc);
     cudaFreeHost(c->h_dbl);
@@ -146,12 +165,12 @@ struct hbicg_matrix {
 /* SELL-32 when every row fits in HBK_SELL_MAX_LEN and padding stays under a
  * third of the nonzeros (rows are short and regular, as in stencils); the CSR
  * row-block path otherwise.  HBICG_SPMV_FORMAT=tile|sell overrides. */
-static int build_sell(hbicg_matrix *A, const unsigned *h_ptr, unsigned n, unsigned nnz) {
+static int build_sell(hbicg_matrix *A, const unsigned *h_ptr, unsigned n, unsigned nnz, int force) {
     cudaStream_t st = A->ctx->stream;
     unsigned maxlen = 0;
     for (unsigned i = 0; i < n; i++)
         if (h_ptr[i + 1] - h_ptr[i] > maxlen) maxlen = h_ptr[i + 1] - h_ptr[i];
-    const char *env = getenv("HBICG_SPMV_FORMAT");
+    const char *env = force ? "sell" : getenv("HBICG_SPMV_FORMAT");
     int want = maxlen <= HBK_SELL_MAX_LEN;
     if (env && !strcmp(env, "tile")) want = 0;
     if (env && !strcmp(env, "sell")) want = maxlen <= HBK_SELL_MAX_LEN;
@@ -251,11 +270,12 @@ int hbicg_matrix_create(hbicg_context *ctx, unsigned n, unsigned nnz, const unsi
             if (!hp) return HBICG_E_NOMEM;
             CUDA_TRY(cudaMemcpy(hp, ptr, sizeof(unsigned) * ((size_t)n + 1), cudaMemcpyDeviceToHost));
         }
-        int rc = build_sell(A, hp, n, nnz);
+        int rc = build_sell(A, hp, n, nnz, 0);
         if (where == HBICG_DEVICE) free(hp);
         if (rc) return rc;
         if (A->k.fmt == HBK_FMT_SELL) A->k.grid = hbk_spmv_grid((n + HBK_THREADS - 1) / HBK_THREADS);
     }
+    ctx_retain(ctx);
     *out = A;
     return HBICG_OK;
 }
@@ -387,7 +407,9 @@ void hbicg_matrix_destroy(hbicg_matrix *A) {
     if (A->d_sval) cudaFree(A->d_sval);
     if (A->d_scol) cudaFree(A->d_scol);
     if (A->d_sptr) cudaFree(A->d_sptr);
+    hbicg_context *ctx = A->ctx;
     free(A);
+    ctx_release(ctx);
 }
 
 const hbk_matrix *hbicg__matrix_kernel_view(const hbicg_matrix *A) { return &A->k; }
@@ -426,6 +448,156 @@ int hbicg_matrix_time_spmv(hbicg_matrix *A, const double *x, double *y, double s
     float t = 0.f;
     CUDA_TRY(cudaEventElapsedTime(&t, A->ctx->ev0, A->ctx->ev1));
     *ms = (double)t / iters;
+    return HBICG_OK;
+}
+
+int hbicg_matrix_format(const hbicg_matrix *A) { return A->k.fmt == HBK_FMT_SELL ? HBICG_SPMV_SELL : HBICG_SPMV_TILE; }
+
+static unsigned *host_ptr_copy(hbicg_matrix *A) {
+    const size_t n = A->k.n;
+    unsigned *hp = malloc(sizeof(unsigned) * (n + 1));
+    if (!hp) return NULL;
+    if (cudaMemcpy(hp, A->d_ptr, sizeof(unsigned) * (n + 1), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        free(hp);
+        return NULL;
+    }
+    return hp;
+}
+
+int hbicg_matrix_set_format(hbicg_matrix *A, int fmt) {
+    if (!A || (fmt != HBICG_SPMV_TILE && fmt != HBICG_SPMV_SELL)) return HBICG_E_ARG;
+    if (fmt == HBICG_SPMV_TILE) {
+        A->k.fmt = HBK_FMT_TILE;
+        A->k.grid = hbk_spmv_grid(A->k.nblk);
+        return HBICG_OK;
+    }
+    if (!A->d_sval) {
+        unsigned *hp = host_ptr_copy(A);
+        if (!hp) return HBICG_E_NOMEM;
+        int rc = build_sell(A, hp, A->k.n, A->k.nnz, 1);
+        free(hp);
+        if (rc) return rc;
+        if (!A->d_sval) {
+            set_msg("a row is longer than %d entries: no SELL-32 form", HBK_SELL_MAX_LEN);
+            return HBICG_E_ARG;
+        }
+    }
+    A->k.fmt = HBK_FMT_SELL;
+    A->k.sval = A->d_sval;
+    A->k.scol = A->d_scol;
+    A->k.sptr = A->d_sptr;
+    A->k.grid = hbk_spmv_grid((A->k.n + HBK_THREADS - 1) / HBK_THREADS);
+    return HBICG_OK;
+}
+
+/* Signature of a sparsity pattern for the autotune cache: log2 of n, the
+ * longest row, and the share of rows in each power-of-two row-length class
+ * (0, 1, 2-3, 4-7, ..., >= 8192), in sixteenths. */
+static void pattern_signature(const unsigned *hp, unsigned n, char *key, size_t cap) {
+    unsigned long long cls[15] = {0};
+    unsigned maxlen = 0;
+    for (unsigned i = 0; i < n; i++) {
+        const unsigned len = hp[i + 1] - hp[i];
+        if (len > maxlen) maxlen = len;
+        int c = 0;
+        for (unsigned v = len; v && c < 14; v >>= 1) ++c;
+        cls[c]++;
+    }
+    int lg = 0;
+    for (unsigned v = n; v > 1; v >>= 1) ++lg;
+    int o = snprintf(key, cap, "n2^%d:max%u:", lg, maxlen);
+    for (int c = 0; c < 15 && o < (int)cap; ++c) {
+        const unsigned q = n ? (unsigned)((16ull * cls[c] + n / 2) / n) : 0u;
+        o += snprintf(key + o, cap - (size_t)o, "%x", q > 15 ? 15u : q);
+    }
+}
+
+static pthread_mutex_t g_tune_lock = PTHREAD_MUTEX_INITIALIZER;
+
+/* cached choice for key: 0 tile, 1 sell, -1 none */
+static int tune_lookup(const char *path, const char *key, double *tile_ms, double *sell_ms) {
+    FILE *f = fopen(path, "r");
+    if (!f) return -1;
+    char line[512], k[256], fmt[16];
+    int found = -1;
+    while (fgets(line, sizeof line, f)) {
+        double t, sl;
+        if (line[0] == '#') continue;
+        if (sscanf(line, "%255s %15s %lf %lf", k, fmt, &t, &sl) == 4 && !strcmp(k, key)) {
+            found = !strcmp(fmt, "sell") ? 1 : 0;
+            *tile_ms = t;
+            *sell_ms = sl;
+        }
+    }
+    fclose(f);
+    return found;
+}
+
+int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, double *tile_ms, double *sell_ms) {
+    if (!A) return HBICG_E_ARG;
+    unsigned *hp = host_ptr_copy(A);
+    if (!hp) return HBICG_E_NOMEM;
+    char key[256];
+    pattern_signature(hp, A->k.n, key, sizeof key);
+    free(hp);
+    double t_tile = -1.0, t_sell = -1.0;
+    int pick = -1;
+    if (cache_path && *cache_path) {
+        pthread_mutex_lock(&g_tune_lock);
+        pick = tune_lookup(cache_path, key, &t_tile, &t_sell);
+        pthread_mutex_unlock(&g_tune_lock);
+    }
+    if (pick < 0) {
+        /* time both forms of y = A x (10 launches each after a warm-up) */
+        const size_t n = A->k.n ? A->k.n : 1;
+        double *x = NULL, *y = NULL;
+        CUDA_TRY(cudaMalloc((void **)&x, sizeof(double) * n));
+        CUDA_TRY(cudaMalloc((void **)&y, sizeof(double) * n));
+        CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, A->ctx->stream));
+        int rc = hbicg_matrix_set_format(A, HBICG_SPMV_TILE);
+        if (!rc) rc = hbicg_matrix_time_spmv(A, x, y, 0.0, 10, &t_tile);
+        if (!rc && hbicg_matrix_set_format(A, HBICG_SPMV_SELL) == HBICG_OK)
+            rc = hbicg_matrix_time_spmv(A, x, y, 0.0, 10, &t_sell);
+        cudaFree(x);
+        cudaFree(y);
+        if (rc) return rc;
+        pick = (t_sell >= 0.0 && t_sell < t_tile) ? 1 : 0;
+        if (cache_path && *cache_path) {
+            char line[512];
+            const int len = snprintf(line, sizeof line, "%s %s %.6f %.6f\n", key, pick ? "sell" : "tile", t_tile, t_sell);
+            pthread_mutex_lock(&g_tune_lock);
+            const int fd = open(cache_path, O_WRONLY | O_CREAT | O_APPEND, 0644);
+            if (fd >= 0) {
+                struct stat sb;
+                if (fstat(fd, &sb) == 0 && sb.st_size == 0) {
+                    static const char head[] = "# hbicg autotune cache v1: signature format tile_ms sell_ms\n";
+                    if (write(fd, head, sizeof head - 1) < 0) { /* best effort */
+                    }
+                }
+                if (write(fd, line, (size_t)len) < 0) { /* a cache that cannot be written is only slower */
+                }
+                close(fd);
+            }
+            pthread_mutex_unlock(&g_tune_lock);
+        }
+    }
+    int rc = hbicg_matrix_set_format(A, pick ? HBICG_SPMV_SELL : HBICG_SPMV_TILE);
+    if (rc) return rc;
+    if (!pick && A->d_sval) { /* the SELL copy is not used: give its memory back */
+        cudaStreamSynchronize(A->ctx->stream);
+        cudaFree(A->d_sval);
+        cudaFree(A->d_scol);
+        cudaFree(A->d_sptr);
+        A->d_sval = NULL;
+        A->d_scol = NULL;
+        A->d_sptr = NULL;
+        A->k.sval = NULL;
+        A->k.scol = NULL;
+        A->k.sptr = NULL;
+    }
+    if (chosen) *chosen = pick ? HBICG_SPMV_SELL : HBICG_SPMV_TILE;
+    if (tile_ms) *tile_ms = t_tile;
+    if (sell_ms) *sell_ms = t_sell;
     return HBICG_OK;
 }
 
@@ -613,6 +785,7 @@ int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_
     }
     s->chunk = p.graph_chunk > 0 ? p.graph_chunk : (n >= (1u << 22) ? 2 : (n >= (1u << 18) ? 4 : 16));
     s->launches_per_iter = s->mode == HBICG_SHIFTS_DEFERRED ? 7 : 5;
+    ctx_retain(ctx);
     *out = s;
     return HBICG_OK;
 }
@@ -630,7 +803,9 @@ void hbicg_solver_destroy(hbicg_solver *s) {
                     s->d_qcopy, s->tc_ws, s->d_tc_err};
     for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++)
         if (ptrs[i]) cudaFree(ptrs[i]);
+    hbicg_context *ctx = s->ctx;
     free(s);
+    ctx_release(ctx);
 }
 
 /* ------------------------------------------------------------------------ */
