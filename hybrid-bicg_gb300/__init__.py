@@ -87,6 +87,15 @@ class Coo(C.Structure):
                 ("symmetry", C.c_int), ("expanded", C.c_int), ("row", _PU), ("col", _PU), ("val", _PD)]
 
 
+class Family(C.Structure):
+    """hbicg_family (include/hbicg.h)"""
+    _fields_ = [("n", C.c_uint), ("nnz", C.c_uint), ("ptr", _PU), ("col", _PU), ("val", _PD), ("b", _PD),
+                ("sigma", _PD), ("m", C.c_int), ("seed", C.c_int), ("autotune", C.c_int), ("x", _PD), ("r", _PD),
+                ("true_residual", _PD), ("status", C.c_int), ("k", C.c_int), ("n_switches", C.c_int),
+                ("final_seed", C.c_int), ("spmv_format", C.c_int), ("solve_ms", C.c_double),
+                ("wall_ms", C.c_double), ("max_true_residual", C.c_double)]
+
+
 _lib = None
 
 
@@ -116,6 +125,12 @@ def lib() -> C.CDLL:
                                             C.c_int, C.POINTER(C.c_void_p)]),
         "hbicg_matrix_load_mm": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
         "hbicg_matrix_get_csr": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+        "hbicg_matrix_format": (C.c_int, [C.c_void_p]),
+        "hbicg_matrix_set_format": (C.c_int, [C.c_void_p, C.c_int]),
+        "hbicg_matrix_autotune": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double)]),
+        "hbicg_batch_solve": (C.c_int, [C.POINTER(Family), C.c_int, C.POINTER(Params), C.c_int, C.c_char_p,
+                                        C.POINTER(C.c_double)]),
         "hbicg_matrix_spmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
         "hbicg_matrix_time_spmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
                                              C.POINTER(C.c_double)]),
@@ -272,6 +287,57 @@ def solve(a, b, sigma, seed=0, *, tol=1e-12, max_iter=2000, switching=True, form
     return _result(st, bufs, m, x, r, true_residuals)
 
 
+@dataclass
+class FamilyResult:
+    status: int
+    k: int
+    x: np.ndarray
+    switches: int
+    final_seed: int
+    spmv_format: str
+    solve_ms: float
+    wall_ms: float
+    max_true_residual: float
+    true_residual: np.ndarray | None
+
+
+def batch_solve(families, workers: int = 8, autotune: bool = False, autotune_cache: str | None = None,
+                **kw) -> tuple[list, float]:
+    """hbicg_batch_solve over workloads.Family-like objects (a, b, sigma,
+    seed): every family solved with the same parameters (kw as params()).
+    Returns ([FamilyResult], wall seconds)."""
+    p = params(**kw)
+    want_res = bool(kw.get("true_residuals", False))
+    arr = (Family * max(len(families), 1))()
+    keep = []
+    for i, f in enumerate(families):
+        ptr, col, val = _csr_arrays(f.a)
+        b = np.ascontiguousarray(f.b, dtype=np.float64)
+        sig = np.ascontiguousarray(f.sigma, dtype=np.float64)
+        n, m = int(ptr.shape[0] - 1), len(sig)
+        x = np.zeros((m, n))
+        res = np.zeros(max(m, 1))
+        keep.append((ptr, col, val, b, sig, x, res))
+        fa = arr[i]
+        fa.n, fa.nnz = n, int(ptr[-1])
+        fa.ptr, fa.col, fa.val = ptr.ctypes.data_as(_PU), col.ctypes.data_as(_PU), val.ctypes.data_as(_PD)
+        fa.b, fa.sigma = b.ctypes.data_as(_PD), sig.ctypes.data_as(_PD)
+        fa.m, fa.seed, fa.autotune = m, int(f.seed), 1 if autotune else 0
+        fa.x = x.ctypes.data_as(_PD)
+        fa.true_residual = res.ctypes.data_as(_PD) if want_res else None
+    wall = C.c_double()
+    lib().hbicg_batch_solve(arr, len(families), C.byref(p), int(workers),
+                            str(autotune_cache).encode() if autotune_cache else None, C.byref(wall))
+    out = []
+    for i in range(len(families)):
+        fa = arr[i]
+        out.append(FamilyResult(status=fa.status, k=fa.k, x=keep[i][5], switches=fa.n_switches,
+                                final_seed=fa.final_seed, spmv_format="sell" if fa.spmv_format == 1 else "tile",
+                                solve_ms=fa.solve_ms, wall_ms=fa.wall_ms, max_true_residual=fa.max_true_residual,
+                                true_residual=keep[i][6][:len(keep[i][4])].copy() if want_res else None))
+    return out, wall.value / 1e3
+
+
 class Context:
     def __init__(self):
         self.h = C.c_void_p()
@@ -327,6 +393,20 @@ class Matrix:
         _check(lib().hbicg_matrix_load_mm(ctx.h, str(path).encode(), int(bool(expand_symmetric)), C.byref(h)),
                "hbicg_matrix_load_mm")
         return cls._wrap(ctx, h)
+
+    @property
+    def format(self) -> str:
+        return "sell" if lib().hbicg_matrix_format(self.h) == 1 else "tile"
+
+    def set_format(self, fmt: str) -> None:
+        _check(lib().hbicg_matrix_set_format(self.h, {"tile": 0, "sell": 1}[fmt]), "hbicg_matrix_set_format")
+
+    def autotune(self, cache: str | None = None) -> dict:
+        """Time both SpMV forms (or read the cached choice) and keep the faster."""
+        ch, t1, t2 = C.c_int(), C.c_double(), C.c_double()
+        _check(lib().hbicg_matrix_autotune(self.h, str(cache).encode() if cache else None, C.byref(ch), C.byref(t1),
+                                           C.byref(t2)), "hbicg_matrix_autotune")
+        return {"format": "sell" if ch.value == 1 else "tile", "tile_ms": t1.value, "sell_ms": t2.value}
 
     def csr(self):
         """(ptr, col, val) copied to numpy."""

@@ -189,6 +189,35 @@ int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int 
 int hbicg_true_residuals_noalloc(hbicg_matrix *A, const double *x, unsigned long long ldx, const double *b,
                                  const double *sigma, int m, double *res, void *stream);
 
+/* Batched families: independent shifted families, each a complete solve with
+ * the reference's semantics, run concurrently by `workers` host threads (each
+ * with its own context and stream; 0 = 8), largest nnz * m first, so the GPU
+ * interleaves the kernels of several small families.  Replaces the
+ * reference's hard-coded sweep drivers (src/main_seed_diff.c:113-155).
+ * All pointers are host memory.  Per-family status in fams[i].status; the
+ * call returns the first failing status, or HBICG_OK.  autotune_cache: path
+ * of the SpMV-form cache used by families with autotune set (may be NULL). */
+typedef struct {
+    /* inputs */
+    unsigned n, nnz;
+    const unsigned *ptr, *col;
+    const double *val;
+    const double *b;
+    const double *sigma;
+    int m, seed;
+    int autotune;             /* run hbicg_matrix_autotune before the solve */
+    /* outputs */
+    double *x;                /* [m*n], shift-major */
+    double *r;                /* [n] final seed residual (optional) */
+    double *true_residual;    /* [m] when params.true_residuals (optional) */
+    int status, k, n_switches, final_seed, spmv_format;
+    double solve_ms;          /* device time of the solve */
+    double wall_ms;           /* host time of matrix set-up + solve + copies */
+    double max_true_residual;
+} hbicg_family;
+int hbicg_batch_solve(hbicg_family *fams, int count, const hbicg_params *p, int workers, const char *autotune_cache,
+                      double *wall_ms);
+
 /* One-call form with host pointers (creates and frees everything). */
 int hbicg_solve(unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *col, const double *val,
                 const double *b, const double *sigma, int m, int seed, const hbicg_params *p, double *x,

@@ -1,0 +1,110 @@
+"""Batched families (hbicg_batch_solve) and the SpMV-form autotuner on the
+GPU: every family of a concurrent batch gets exactly the solve it gets alone;
+a failing family fails alone; the autotune cache is written once and read
+back; the manifest runner end to end."""
+import json
+
+import numpy as np
+import pytest
+from conftest import ROOT
+
+pytestmark = pytest.mark.gpu
+
+
+def _families(pkg, count=10, seed=0):
+    return pkg.workloads.batched_families(count, n_lo=500, n_hi=6000, seed=seed)
+
+
+def test_batch_equals_individual_solves(cuda, pkg):
+    fams = _families(pkg)
+    res, wall = pkg.batch_solve(fams, workers=4, tol=1e-10, max_iter=10000, true_residuals=True)
+    assert wall > 0
+    for f, r in zip(fams, res):
+        one = pkg.solve(f.a, f.b, f.sigma, seed=f.seed, tol=1e-10, max_iter=10000)
+        assert r.status == 0 and r.k == one.k and r.switches == len(one.switches)
+        assert np.array_equal(r.x, one.x)  # same kernels, same order: bit for bit
+
+
+def test_batch_failure_stays_with_its_family(cuda, pkg):
+    fams = _families(pkg, count=4, seed=1)
+    bad = fams[2]
+    bad.seed = len(bad.sigma) + 3  # out of range
+    res, _ = pkg.batch_solve(fams, workers=3, tol=1e-10, max_iter=10000)
+    assert res[2].status != 0
+    for i in (0, 1, 3):
+        assert res[i].status == 0 and res[i].k > 1
+
+
+def test_autotune_cache_written_once_and_reused(cuda, pkg, tmp_path):
+    cache = tmp_path / "tune.txt"
+    a = pkg.workloads.stencil_cd3d(24)
+    ctx = pkg.Context()
+    A1 = pkg.Matrix(ctx, a.ptr, a.col, a.val)
+    r1 = A1.autotune(str(cache))
+    assert r1["format"] in ("tile", "sell") and r1["tile_ms"] > 0 and r1["sell_ms"] > 0
+    assert A1.format == r1["format"]
+    lines = cache.read_text().splitlines()
+    assert lines[0].startswith("#") and len(lines) == 2
+    A2 = pkg.Matrix(ctx, a.ptr, a.col, a.val)
+    r2 = A2.autotune(str(cache))  # same pattern: read, not timed again (times kept to 6 decimals)
+    assert r2["format"] == r1["format"] and len(cache.read_text().splitlines()) == 2
+    assert abs(r2["tile_ms"] - r1["tile_ms"]) < 1e-6 and abs(r2["sell_ms"] - r1["sell_ms"]) < 1e-6
+    # both forms give the same product
+    x = np.random.default_rng(0).standard_normal(a.n)
+    y1, y2 = np.zeros(a.n), np.zeros(a.n)
+    A2.set_format("tile")
+    A2.spmv(x, y1, 0.25)
+    A2.set_format("sell")
+    A2.spmv(x, y2, 0.25)
+    assert np.allclose(y1, y2, rtol=1e-14, atol=1e-14)
+    A1.close()
+    A2.close()
+
+
+def test_autotune_long_rows_keep_tile(cuda, pkg, tmp_path):
+    a = pkg.workloads.irregular_powerlaw(20000, seed=1)
+    ctx = pkg.Context()
+    A = pkg.Matrix(ctx, a.ptr, a.col, a.val)
+    r = A.autotune(str(tmp_path / "t.txt"))
+    if int(np.max(np.diff(a.ptr.astype(np.int64)))) > 64:
+        assert r["format"] == "tile" and r["sell_ms"] < 0
+        with pytest.raises(RuntimeError, match="SELL"):
+            A.set_format("sell")
+    A.close()
+
+
+def test_manifest_runner_end_to_end(cuda, pkg, tmp_path):
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("run_manifest", ROOT / "hybrid-bicg_gb300" / "run_manifest.py")
+    rm = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(rm)
+    a = pkg.workloads.stencil_cd3d(12)
+    pkg.workloads.write_matrix_market(str(tmp_path / "a.mtx"), a)
+    man = {"params": {"tol": 1e-10, "max_iter": 5000, "true_residuals": True}, "workers": 3,
+           "autotune_cache": "tune.txt",
+           "families": [{"name": "file", "matrix": "a.mtx", "shifts": {"linspace": [0.0, 0.15, 16]},
+                         "seeds": [0, 7], "out": "x"},
+                        {"name": "gen", "matrix": {"generator": "stencil_cd2d", "args": [40]},
+                         "shifts": {"geomspace": [1e-3, 1.0, 12]}, "rhs": {"normal": 1}}]}
+    (tmp_path / "m.json").write_text(json.dumps(man))
+
+    class Sink:
+        def __init__(self):
+            self.lines = []
+
+        def write(self, s):
+            self.lines.append(s)
+
+        def flush(self):
+            pass
+
+    lines = rm.run(man, tmp_path, stream=Sink())
+    assert [(l["name"], l["seed"]) for l in lines] == [("file", 0), ("file", 7), ("gen", 0)]
+    for l in lines:
+        assert l["status"] == 0 and l["max_true_residual"] <= 1e-10 * 1.01
+    b = np.full(a.n, 1.0 / np.sqrt(a.n))
+    one = pkg.solve(a, b, np.linspace(0.0, 0.15, 16), seed=7, tol=1e-10, max_iter=5000)
+    x = np.load(tmp_path / "x" / "file_seed7.npy")
+    assert abs(lines[1]["k"] - one.k) <= 1 and np.max(np.abs(x - one.x)) <= 1e-9 * np.max(np.abs(one.x))
+    assert (tmp_path / "tune.txt").exists()
