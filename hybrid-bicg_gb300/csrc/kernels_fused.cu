@@ -245,9 +245,15 @@ __device__ void seed_step_scalars(const Ctx &c, double rr, double rrh) {
     for (int j = threadIdx.x; j < m; j += NT) {
         double *co = S.coef + (size_t)j * HBK_NCOEF;
         if (j == seed) {
-            // the seed as a system of its own (deferred mode): pi = zeta = 1, shift 0
-            co[0] = wk;
-            co[1] = ak;
+            // the seed as a system of its own (deferred mode): pi = zeta = 1,
+            // shift 0.  Its x is not carried in coefficient form: K4 adds
+            // alpha p_s + omega q to its row of X directly, with the
+            // materialised p_s, as the reference's seed step does
+            // (src/solver_dynamic.c:156-210).  In coefficient form p_s would enter
+            // through s = (r_{k-1} - q) / alpha, which cancels when a step makes
+            // little progress; its p coefficients stay (needed after a switch).
+            co[0] = 0.0;
+            co[1] = 0.0;
             co[2] = dvd(wk, ak);
             co[3] = -dvd(wk, ak);
             co[4] = bk;
@@ -407,23 +413,16 @@ __global__ void __launch_bounds__(NT) k_seed_update(Ctx c) {
     const double *__restrict__ rh = c.v.r_hat;
     double *__restrict__ rn = vec_r_new(c, sc);
     double2 acc = make_double2(0.0, 0.0);
-    if (!c.v.deferred) {
-        double *__restrict__ xs = c.v.X + (size_t)seed * ldn(n);
-        for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
-            const double qi = q[i];
-            xs[i] = fma(w, qi, fma(a, ps[i], xs[i]));
-            const double r = fma(-w, y[i], qi);
-            rn[i] = r;
-            acc.x = fma(r, r, acc.x);
-            acc.y = fma(rh[i], r, acc.y);
-        }
-    } else {
-        for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
-            const double r = fma(-w, y[i], q[i]);
-            rn[i] = r;
-            acc.x = fma(r, r, acc.x);
-            acc.y = fma(rh[i], r, acc.y);
-        }
+    // the seed's x in both shift modes (in deferred mode its x coefficients
+    // are kept at zero, so the basis flushes leave this row as it is)
+    double *__restrict__ xs = c.v.X + (size_t)seed * ldn(n);
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
+        const double qi = q[i];
+        xs[i] = fma(w, qi, fma(a, ps[i], xs[i]));
+        const double r = fma(-w, y[i], qi);
+        rn[i] = r;
+        acc.x = fma(r, r, acc.x);
+        acc.y = fma(rh[i], r, acc.y);
     }
     acc = block_sum2(acc, sh);
     if (threadIdx.x == 0) {
