@@ -126,6 +126,12 @@ def lib() -> C.CDLL:
         "hbicg_matrix_load_mm": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
         "hbicg_matrix_get_csr": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
         "hbicg_matrix_format": (C.c_int, [C.c_void_p]),
+        "hbicg_matrix_transpose": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+        "hbicg_adjoint_gradients": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_ulonglong, C.c_void_p,
+                                              C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "hbicg_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                    C.c_void_p, C.POINTER(Params), C.POINTER(C.c_double), C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
         "hbicg_matrix_set_format": (C.c_int, [C.c_void_p, C.c_int]),
         "hbicg_matrix_autotune": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                             C.POINTER(C.c_double)]),
@@ -287,6 +293,39 @@ def solve(a, b, sigma, seed=0, *, tol=1e-12, max_iter=2000, switching=True, form
     return _result(st, bufs, m, x, r, true_residuals)
 
 
+def adjoint(a, b, sigma, w, c, seed: int = 0, **kw) -> dict:
+    """J = sum_j w_j c^T x_j for (A + sigma_j I) x_j = b and its gradients
+    with respect to A's values (on its pattern), b and the shifts
+    (hbicg_adjoint: one forward family, one transposed family).  numpy in/out."""
+    ptr, col, val = _csr_arrays(a)
+    n, m = int(ptr.shape[0] - 1), len(sigma)
+    ctx = Context()
+    A = Matrix(ctx, ptr, col, val)
+    p = params(**kw)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    sig = np.ascontiguousarray(sigma, dtype=np.float64)
+    ww = np.ascontiguousarray(w, dtype=np.float64)
+    cc = np.ascontiguousarray(c, dtype=np.float64)
+    J = C.c_double()
+    dval, db, ds, x = np.zeros(int(ptr[-1])), np.zeros(n), np.zeros(m), np.zeros((m, n))
+    rc = lib().hbicg_adjoint(A.h, None, _ptr(bb), _ptr(sig), m, int(seed), _ptr(ww), _ptr(cc), C.byref(p), C.byref(J),
+                             _ptr(dval), _ptr(db), _ptr(ds), _ptr(x), None, None)
+    A.close()
+    ctx.close()
+    if rc not in (0, 4):
+        _check(rc, "hbicg_adjoint")
+    return {"J": J.value, "dval": dval, "db": db, "dsigma": ds, "x": x, "status": rc}
+
+
+def shifted_solve(ptr, col, val, b, sigma, seed: int = 0, **kw):
+    """X = [x_j] with (A + sigma_j I) x_j = b as a differentiable torch op
+    (val, b, sigma: float64 CUDA tensors; ptr, col: int32 CUDA tensors of A's
+    pattern).  Backward: the transposed family (see torch_ops.py)."""
+    from . import torch_ops
+
+    return torch_ops.shifted_solve(ptr, col, val, b, sigma, seed, **kw)
+
+
 @dataclass
 class FamilyResult:
     status: int
@@ -393,6 +432,30 @@ class Matrix:
         _check(lib().hbicg_matrix_load_mm(ctx.h, str(path).encode(), int(bool(expand_symmetric)), C.byref(h)),
                "hbicg_matrix_load_mm")
         return cls._wrap(ctx, h)
+
+    def transpose(self) -> "Matrix":
+        """A^T on the same context, built on the GPU (stable by column)."""
+        h = C.c_void_p()
+        _check(lib().hbicg_matrix_transpose(self.h, C.byref(h)), "hbicg_matrix_transpose")
+        return Matrix._wrap(self.ctx, h)
+
+    def adjoint_gradients(self, X, Lam, w=None, want=("val", "b", "sigma")):
+        """Gradients from solutions (torch CUDA tensors, [m, n] each): X with
+        (A + sigma_j I) x_j = b, Lam with (A^T + sigma_j I) lam_j = g_j.
+        Returns (dval [nnz], db [n], dsigma [m]) as CUDA tensors."""
+        import torch
+
+        m = int(X.shape[0])
+        dev = X.device
+        dval = torch.empty(self.nnz, dtype=torch.float64, device=dev) if "val" in want else None
+        db = torch.empty(self.n, dtype=torch.float64, device=dev) if "b" in want else None
+        ds = torch.empty(m, dtype=torch.float64, device=dev) if "sigma" in want else None
+        _check(lib().hbicg_adjoint_gradients(self.h, m, _ptr(X), int(X.stride(0)), _ptr(Lam), int(Lam.stride(0)),
+                                             _ptr(w) if w is not None else None,
+                                             _ptr(dval) if dval is not None else None,
+                                             _ptr(db) if db is not None else None,
+                                             _ptr(ds) if ds is not None else None), "hbicg_adjoint_gradients")
+        return dval, db, ds
 
     @property
     def format(self) -> str:

@@ -159,6 +159,14 @@ int hbk_true_residuals(const hbk_matrix *A, const double *X, const double *b, co
 size_t hbk_coo_to_csr_tmp_bytes(unsigned nnz);
 int hbk_coo_to_csr(unsigned n, unsigned nnz, const unsigned *row, const unsigned *col, const double *val,
                    unsigned *ptr, unsigned *col_out, double *val_out, void *tmp, int *err, cudaStream_t st);
+/* adjoint gradients (csrc/adjoint.cu) */
+int hbk_entry_rows(unsigned n, const unsigned *ptr, unsigned *rows, cudaStream_t st);
+size_t hbk_adjoint_tmp_bytes(int m);
+int hbk_shift_dots(unsigned n, int m, const double *X, size_t ldx, const double *a, size_t lda, int a_shared,
+                   const double *w, double scale, double *out, void *tmp, cudaStream_t st);
+int hbk_grad_b(unsigned n, int m, const double *Y, size_t ldy, const double *w, double *db, cudaStream_t st);
+int hbk_grad_val(unsigned nnz, const unsigned *rows, const unsigned *col, int m, const double *X, size_t ldx,
+                 const double *Y, size_t ldy, const double *w, double *dval, cudaStream_t st);
 size_t hbk_flush_tc_workspace_bytes(int m);
 int hbk_flush_tc_max_slots(void);
 int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,

@@ -413,6 +413,7 @@ void hbicg_matrix_destroy(hbicg_matrix *A) {
 }
 
 const hbk_matrix *hbicg__matrix_kernel_view(const hbicg_matrix *A) { return &A->k; }
+hbicg_context *hbicg__matrix_context(const hbicg_matrix *A) { return A->ctx; }
 
 unsigned hbicg_matrix_rows(const hbicg_matrix *A) { return A->k.n; }
 unsigned long long hbicg_matrix_nnz(const hbicg_matrix *A) { return A->k.nnz; }

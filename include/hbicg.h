@@ -218,6 +218,25 @@ typedef struct {
 int hbicg_batch_solve(hbicg_family *fams, int count, const hbicg_params *p, int workers, const char *autotune_cache,
                       double *wall_ms);
 
+/* Adjoint (no counterpart in the reference, which only solves forward).
+ * A^T as a new matrix on A's context, built on the GPU (stable by column). */
+int hbicg_matrix_transpose(hbicg_matrix *A, hbicg_matrix **At);
+/* Gradients from given solutions, all device pointers: X [m][ldx] with
+ * (A + sigma_j I) x_j = b, Lam [m][ldl] with (A^T + sigma_j I) lam_j = g_j,
+ * weights w [m] (NULL = ones):
+ *   dJ_dval[e] = -sum_j w_j lam_j[row e] x_j[col e],  dJ_db = sum_j w_j lam_j,
+ *   dJ_dsigma[j] = -w_j lam_j . x_j   (each output may be NULL). */
+int hbicg_adjoint_gradients(hbicg_matrix *A, int m, const double *X, unsigned long long ldx, const double *Lam,
+                            unsigned long long ldl, const double *w, double *dJ_dval, double *dJ_db,
+                            double *dJ_dsigma);
+/* J = sum_j w_j c^T x_j and its gradients for a family on A (host pointers
+ * in and out; At may be NULL to build A^T here).  One forward family on A
+ * and one transposed family on A^T with right-hand side c, same shifts and
+ * seed; fwd/adj stats optional; x_out [m*n] optional. */
+int hbicg_adjoint(hbicg_matrix *A, hbicg_matrix *At, const double *b, const double *sigma, int m, int seed,
+                  const double *w, const double *c, const hbicg_params *p, double *J, double *dJ_dval, double *dJ_db,
+                  double *dJ_dsigma, double *x_out, hbicg_stats *fwd, hbicg_stats *adj);
+
 /* One-call form with host pointers (creates and frees everything). */
 int hbicg_solve(unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *col, const double *val,
                 const double *b, const double *sigma, int m, int seed, const hbicg_params *p, double *x,
