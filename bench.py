@@ -453,6 +453,48 @@ def run_batch_c4(args, dist: Dist):
     return line
 
 
+def run_adjoint_c5(args, dist: Dist):
+    """Config 5: J = sum_k w_k c^T x(sigma_k) on the 128^3 convection-diffusion
+    matrix with 32 shifts, and its gradients with respect to A's values, b and
+    the shifts (hbicg_adjoint: forward family, GPU transpose, transposed family
+    on A^T with right-hand side c, gradient kernels).  A step is one call from
+    host arrays (matrix, b, sigma, w, c in; J, the three gradients and all x_j
+    out).  CPU baseline: the reference's algorithm for the forward family on a
+    bounded sample (its cost model), counted twice (the transposed family has
+    the same size and iteration count to within a few)."""
+    pkg, f = workload("c5", args.scale)
+    w, c = f.extra["w"], f.extra["c"]
+    kw = dict(seed=f.seed, tol=f.tol, max_iter=f.max_iter)
+    for _ in range(args.warmup):
+        out = pkg.adjoint(f.a, f.b, f.sigma, w, c, **kw)
+    times = []
+    with Clocks(dist.local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            out = pkg.adjoint(f.a, f.b, f.sigma, w, c, **kw)
+            times.append(time.perf_counter() - t0)
+    value = float(np.median(times))
+    n, m, nnz = f.a.n, len(f.sigma), f.a.nnz
+    line = {"metric": "C5: J = sum_k w_k c^T x(sigma_k) and dJ/dval, dJ/db, dJ/dsigma (host arrays in/out)",
+            "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": {"workload": f"c5: {n} rows, {nnz} nonzeros, 3-D 7-point convection-diffusion, {m} shifts "
+                                   f"uniform in [1e-3, 1], w ~ U(0,1), b, c ~ N(0,1), tol {f.tol:g}"},
+            "status": out["status"], "J": out["J"],
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": int(12 * nnz + 4 * (n + 1) + 16 * n + 16 * m),
+                    "d2h_bytes_per_step": int(8 * (nnz + n + m + m * n))},
+            "clocks": clk.summary(), "cpu_baseline": None}
+    if not args.no_cpu_baseline:
+        fwd = pkg.solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=f.max_iter)
+        prof = {"k": int(fwd.k), "shift_updates": int(np.sum(fwd.active)), "source": "the GPU forward solve's profile"}
+        cb = cpu_baseline(f, prof)
+        cb["value"] *= 2.0
+        cb["sample"] = "2 x (forward family) " + cb["sample"]
+        line["cpu_baseline"] = cb
+    return line
+
+
 def run_flush_kernel(args):
     """The basis flush alone (hbk_flush_tc_run: slot maxima, coefficient
     digits, the tensor-core kernel) on random FP64 data of a solve's shape:
@@ -637,6 +679,8 @@ def main(argv=None):
     try:
         if args.workload == "c4" and args.impl == "ours":
             line = run_batch_c4(args, dist)
+        elif args.workload == "c5" and args.impl == "ours":
+            line = run_adjoint_c5(args, dist)
         else:
             line = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
         if line is not None and dist.rank == 0:
