@@ -266,8 +266,10 @@ def run_ours(args, dist: Dist):
     n, nnz, m = f.a.n, f.a.nnz, len(f.sigma)
     form = "plain" if args.mode == "static" else "fused"
     use_graph = args.mode != "normal"
+    # the metric is the true residual: check it after every solve and correct
+    # the shifts whose recursive residual converged above it (params.refine)
     kw = dict(tol=f.tol, max_iter=f.max_iter, form=form, shift_mode=args.shift_mode, use_graph=use_graph,
-              flush=args.flush, basis_block=args.basis_block)
+              flush=args.flush, basis_block=args.basis_block, refine=not args.no_refine)
     ctx = pkg.Context()
     ptr = torch.from_numpy(f.a.ptr.astype(np.int32)).cuda()
     col = torch.from_numpy(f.a.col.astype(np.int32)).cuda()
@@ -358,9 +360,11 @@ def run_ours(args, dist: Dist):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator; the reference ships no matrices)",
         "config": {"workload": f"{args.workload}: {f.a.n} rows, {f.a.nnz} nonzeros, 3-D 7-point convection-"
                    f"diffusion, {m} shifts in [{f.sigma.min():g}, {f.sigma.max():g}], tol {f.tol:g}, seed {f.seed}",
-                   "mode": args.mode, "shift_mode": res.shift_mode, "parallelism": f"replicas x{dist.world}",
+                   "mode": args.mode, "shift_mode": res.shift_mode, "refine": not args.no_refine,
+                   "parallelism": f"replicas x{dist.world}",
                    "l2": "working set >> 129 MB L2 (no flush needed)"},
-        "iterations": res.k, "switches": res.switches, "max_true_residual": vres.max_true_residual,
+        "iterations": res.k, "switches": res.switches, "refined_shifts": res.refined,
+        "max_true_residual": vres.max_true_residual,
         "all_converged": bool(np.all(vres.conv_k > 0)),
         "solve_breakdown_ms": {"flush": flush_ms / args.steps},
         "roofline": roofline, "roofline_spmv": spmv, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu,
@@ -403,7 +407,8 @@ def run_batch_c4(args, dist: Dist):
     (nnz + 6 m n) x iterations and scaled to all 256 with the GPU's counts."""
     pkg = graft.load_package()
     fams = pkg.workloads.batched_families(256)
-    kw = dict(tol=1e-10, max_iter=10000, shift_mode=args.shift_mode, flush=args.flush, true_residuals=True)
+    kw = dict(tol=1e-10, max_iter=10000, shift_mode=args.shift_mode, flush=args.flush, true_residuals=True,
+              refine=not args.no_refine)
     for _ in range(max(1, min(args.warmup, 1))):
         pkg.batch_solve(fams, workers=args.workers, **kw)
     walls, res = [], None
@@ -422,7 +427,7 @@ def run_batch_c4(args, dist: Dist):
             "dtype": "f64", "data": "synthetic (seeded generator)",
             "config": {"workload": "c4: 256 families, n log-uniform in [1e4, 5e5] (2-D 5-point / 3-D 7-point "
                                    "convection-diffusion), 8..64 shifts uniform in [1e-3, 1], b ~ N(0,1)",
-                       "workers": args.workers, "shift_mode": args.shift_mode,
+                       "workers": args.workers, "shift_mode": args.shift_mode, "refine": not args.no_refine,
                        "l2": "every family's working set is re-read from HBM"},
             "families_per_s": 256 / value, "total_iterations": iters, "status_failures": status_bad,
             "families_over_tol": over, "max_true_residual": max(r.max_true_residual for r in res),
@@ -664,6 +669,7 @@ def main(argv=None):
     ap.add_argument("--basis-block", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-refine", action="store_true", help="keep the reference's x (no true-residual correction)")
     ap.add_argument("--kernel", default=None, choices=["flush", "coo2csr", "mmread"],
                     help="time one kernel alone on random data instead of the solve")
     ap.add_argument("--n", type=int, default=2097152, help="elements for --kernel")

@@ -69,12 +69,13 @@ class Params(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("switching", C.c_int), ("form", C.c_int),
                 ("shift_mode", C.c_int), ("use_graph", C.c_int), ("graph_chunk", C.c_int),
                 ("basis_mem_frac", C.c_double), ("true_residuals", C.c_int), ("basis_block", C.c_int),
-                ("flush_mode", C.c_int)]
+                ("flush_mode", C.c_int), ("refine", C.c_int)]
 
 
 class Stats(C.Structure):
     _fields_ = [("k", C.c_int), ("status", C.c_int), ("n_switches", C.c_int), ("final_seed", C.c_int),
                 ("shift_mode", C.c_int), ("basis_flushes", C.c_int), ("launches", C.c_int),
+                ("refined_shifts", C.c_int),
                 ("solve_ms", C.c_double), ("flush_ms", C.c_double), ("max_true_residual", C.c_double),
                 ("bytes_algorithmic", C.c_double), ("flush_bytes", C.c_double),
                 ("switch_k", _PI), ("switch_seed", _PI), ("conv_k", _PI), ("active_per_iter", _PI),
@@ -187,7 +188,8 @@ def _ptr(a) -> int:
 
 
 def params(tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="auto", use_graph=True,
-           graph_chunk=0, basis_mem_frac=0.0, true_residuals=False, basis_block=0, flush="auto") -> Params:
+           graph_chunk=0, basis_mem_frac=0.0, true_residuals=False, basis_block=0, flush="auto",
+           refine=False) -> Params:
     p = Params()
     lib().hbicg_params_default(C.byref(p))
     p.tol = float(tol)
@@ -202,6 +204,7 @@ def params(tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="a
     p.true_residuals = 1 if true_residuals else 0
     p.basis_block = int(basis_block)
     p.flush_mode = FLUSH_MODES[flush]
+    p.refine = 1 if refine else 0
     return p
 
 
@@ -222,6 +225,7 @@ class SolveResult:
     flushes: int
     bytes_algorithmic: float
     flush_bytes: float = 0.0
+    refined: int = 0
     true_residual: np.ndarray | None = None
     extra: dict = field(default_factory=dict)
 
@@ -261,7 +265,7 @@ def _result(st: Stats, bufs, m, x, r, want_res) -> SolveResult:
                        shift_mode={1: "incremental", 2: "deferred"}.get(st.shift_mode, "?"), solve_ms=st.solve_ms,
                        flush_ms=st.flush_ms,
                        launches=st.launches, flushes=st.basis_flushes, bytes_algorithmic=st.bytes_algorithmic,
-                       flush_bytes=st.flush_bytes,
+                       flush_bytes=st.flush_bytes, refined=st.refined_shifts,
                        true_residual=bufs["true_residual"][:m].copy() if want_res else None,
                        extra={"hist": {"alpha": bufs["seed_alpha"][:st.k].copy(), "beta": bufs["seed_beta"][:st.k].copy(),
                                        "omega": bufs["seed_omega"][:st.k].copy(), "rr": bufs["seed_rr"][:st.k].copy()}})
@@ -274,7 +278,7 @@ def _csr_arrays(a):
 
 def solve(a, b, sigma, seed=0, *, tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="auto",
           use_graph=True, true_residuals=False, graph_chunk=0, basis_mem_frac=0.0, basis_block=0,
-          flush="auto") -> SolveResult:
+          flush="auto", refine=False) -> SolveResult:
     """One-call solve with host (numpy) arrays through hbicg_solve."""
     L = lib()
     ptr, col, val = _csr_arrays(a)
@@ -284,7 +288,7 @@ def solve(a, b, sigma, seed=0, *, tol=1e-12, max_iter=2000, switching=True, form
     x = np.zeros((m, n))
     r = np.zeros(n)
     p = params(tol, max_iter, switching, form, shift_mode, use_graph, graph_chunk, basis_mem_frac, true_residuals,
-               basis_block, flush)
+               basis_block, flush, refine)
     st, bufs = _stats(m, max_iter)
     rc = L.hbicg_solve(n, int(ptr[-1]), _ptr(ptr), _ptr(col), _ptr(val), _ptr(bb), _ptr(sig), m, int(seed),
                        C.byref(p), _ptr(x), _ptr(r), C.byref(st))

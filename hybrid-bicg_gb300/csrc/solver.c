@@ -1162,6 +1162,65 @@ static void *touch_pages(void *arg) {
 static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma, int seed, int in_where, double *x,
                            double *r_out, int out_where, hbicg_stats *stats, touch_t *touch);
 
+/* params.refine: true residuals of every shift; a shift above tol gets
+ * x_j += e with (A + sigma_j I) e = b - (A + sigma_j I) x_j solved (single
+ * shift, incremental form) to 0.5 tol ||b|| / ||r_j||; at most 3 rounds. */
+static int refine_shifts(hbicg_solver *s, const double *h_sigma, int *refined) {
+    cudaStream_t st = s->ctx->stream;
+    const unsigned n = s->A->k.n;
+    const int m = s->m;
+    const size_t ld = s->ld;
+    double *h = malloc(sizeof(double) * (size_t)m), *r = NULL, *e = NULL;
+    hbicg_solver *sub = NULL;
+    int rc = HBICG_OK;
+    if (!h) return HBICG_E_NOMEM;
+    HBK_TRY(hbk_dot(n, s->d_b, s->d_b, s->sh.partials, s->sh.counters + 7, s->d_dot, st));
+    CUDA_TRY(cudaMemcpyAsync(s->ctx->h_dbl, s->d_dot, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    const double bn = sqrt(s->ctx->h_dbl[0]);
+    for (int round = 0; round < 3 && rc == HBICG_OK && bn > 0.0; ++round) {
+        HBK_TRY(hbk_true_residuals(&s->A->k, s->v.X, s->d_b, s->d_sigma, m, s->sh.partials, s->sh.counters + 16,
+                                   s->d_res, st));
+        CUDA_TRY(cudaMemcpyAsync(h, s->d_res, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        int any = 0;
+        for (int j = 0; j < m && rc == HBICG_OK; ++j) {
+            const double res = sqrt(h[j]) / bn;
+            if (res <= s->p.tol) continue;
+            any = 1;
+            if (!r) {
+                CUDA_TRY(cudaMalloc((void **)&r, sizeof(double) * ((size_t)n + 1)));
+                CUDA_TRY(cudaMalloc((void **)&e, sizeof(double) * ((size_t)n + 1)));
+            }
+            if (!sub) {
+                hbicg_params p1 = s->p;
+                p1.refine = 0;
+                p1.true_residuals = 0;
+                p1.shift_mode = HBICG_SHIFTS_INCREMENTAL;
+                if ((rc = hbicg_solver_create(s->ctx, s->A, 1, &p1, &sub)) != HBICG_OK) break;
+            }
+            double *xj = s->v.X + (size_t)j * ld;
+            HBK_TRY(hbk_spmv(&s->A->k, xj, e, h_sigma[j], 1, st)); /* e = (A + sigma_j I) x_j */
+            HBK_TRY(hbk_copy(n, s->d_b, r, st));
+            HBK_TRY(hbk_axpy(n, -1.0, e, r, st));                   /* r = b - e */
+            sub->p.tol = isfinite(res) ? 0.5 * s->p.tol / res : s->p.tol;
+            const int sr = hbicg_solver_run(sub, r, s->d_sigma + j, 0, HBICG_DEVICE, e, NULL, HBICG_DEVICE, NULL);
+            if (sr != HBICG_OK && sr != HBICG_E_MAXITER) {
+                rc = sr;
+                break;
+            }
+            HBK_TRY(hbk_axpy(n, 1.0, e, xj, st));
+            ++*refined;
+        }
+        if (!any) break;
+    }
+    hbicg_solver_destroy(sub);
+    cudaFree(r);
+    cudaFree(e);
+    free(h);
+    return rc;
+}
+
 /* the page-touching helper is joined on every return path of the solve */
 int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int seed, int in_where, double *x,
                      double *r_out, int out_where, hbicg_stats *stats) {
@@ -1251,6 +1310,11 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
         }
     }
     CUDA_TRY(cudaEventRecord(ctx->ev1, st));
+    int refined = 0;
+    if (rc == HBICG_OK && s->p.refine && m > 0) {
+        rc = refine_shifts(s, h_sigma, &refined);
+        CUDA_TRY(cudaEventRecord(ctx->ev1, st)); /* solve_ms includes the corrections */
+    }
     touch_join(touch);
     if (rc == HBICG_OK && x && m > 0)
         CUDA_TRY(cudaMemcpy2DAsync(x, sizeof(double) * n, s->v.X, sizeof(double) * s->ld, sizeof(double) * n, m, kout, st));
@@ -1289,6 +1353,7 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
         stats->shift_mode = s->mode;
         stats->basis_flushes = flushes;
         stats->launches = launches;
+        stats->refined_shifts = refined;
         stats->solve_ms = ms;
         stats->flush_ms = flush_ms;
         stats->max_true_residual = maxres;

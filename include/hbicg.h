@@ -56,6 +56,11 @@ typedef struct {
     int basis_block;       /* deferred mode: iterations per basis block before x_j, p_j are formed
                               (0 = automatic, 24; < 0 = as long as memory allows) */
     int flush_mode;        /* deferred mode: hbicg_flush_mode (default AUTO) */
+    int refine;            /* 1: after the solve, check every shift's true residual
+                              ||b - (A + sigma_j I) x_j|| / ||b|| and correct shifts above
+                              tol by solving (A + sigma_j I) e = r_j (at most 3 rounds).
+                              The recursive residual the reference tests can leave the
+                              true one above tol.  Default 0 (the reference's result). */
 } hbicg_params;
 
 typedef enum {
@@ -72,6 +77,7 @@ typedef struct {
     int shift_mode;           /* mode actually used */
     int basis_flushes;        /* deferred mode: basis flushes during the solve */
     int launches;             /* kernel launches issued for the solve */
+    int refined_shifts;       /* corrections made by params.refine */
     double solve_ms;          /* device time of init + iterations + final flush (CUDA events) */
     double flush_ms;          /* deferred mode: device time of the basis flushes */
     double max_true_residual; /* when params.true_residuals */
