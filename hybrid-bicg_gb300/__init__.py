@@ -189,7 +189,7 @@ def _ptr(a) -> int:
 
 def params(tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="auto", use_graph=True,
            graph_chunk=0, basis_mem_frac=0.0, true_residuals=False, basis_block=0, flush="auto",
-           refine=False) -> Params:
+           refine=True) -> Params:
     p = Params()
     lib().hbicg_params_default(C.byref(p))
     p.tol = float(tol)
@@ -278,7 +278,7 @@ def _csr_arrays(a):
 
 def solve(a, b, sigma, seed=0, *, tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="auto",
           use_graph=True, true_residuals=False, graph_chunk=0, basis_mem_frac=0.0, basis_block=0,
-          flush="auto", refine=False) -> SolveResult:
+          flush="auto", refine=True) -> SolveResult:
     """One-call solve with host (numpy) arrays through hbicg_solve."""
     L = lib()
     ptr, col, val = _csr_arrays(a)

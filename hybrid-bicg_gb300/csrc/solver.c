@@ -96,6 +96,7 @@ void hbicg_params_default(hbicg_params *p) {
     p->true_residuals = 0;
     p->basis_block = 0;
     p->flush_mode = HBICG_FLUSH_AUTO;
+    p->refine = 1;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1311,7 +1312,9 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
     }
     CUDA_TRY(cudaEventRecord(ctx->ev1, st));
     int refined = 0;
-    if (rc == HBICG_OK && s->p.refine && m > 0) {
+    /* only after a converged solve: a solve stopped by max_iter or a breakdown
+     * keeps its x as the reference leaves it */
+    if (rc == HBICG_OK && status == HBICG_OK && s->p.refine && m > 0 && k < s->kcap) {
         rc = refine_shifts(s, h_sigma, &refined);
         CUDA_TRY(cudaEventRecord(ctx->ev1, st)); /* solve_ms includes the corrections */
     }
@@ -1451,6 +1454,7 @@ static int dropin(CSR_Matrix *A_loc_diag, CSR_Matrix *A_loc_offd, INFO_Matrix *A
     p.switching = g_switching;
     p.form = form;
     p.use_graph = use_graph;
+    p.refine = 0; /* the reference's entry points return the reference's x */
     const CSR_Matrix *A = A_loc_diag;
     unsigned *ptr = A->ptr, *col = A->col;
     double *val = A->val;

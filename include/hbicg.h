@@ -60,7 +60,8 @@ typedef struct {
                               ||b - (A + sigma_j I) x_j|| / ||b|| and correct shifts above
                               tol by solving (A + sigma_j I) e = r_j (at most 3 rounds).
                               The recursive residual the reference tests can leave the
-                              true one above tol.  Default 0 (the reference's result). */
+                              true one above tol.  Default 1; the reference's entry points
+                              (solver.h) use 0 and return the reference's result. */
 } hbicg_params;
 
 typedef enum {
