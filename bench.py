@@ -180,9 +180,11 @@ FLUSH_TRAFFIC_PER_ALGORITHMIC_BYTE = 5.097 / 5.151
 
 def flush_roofline(bytes_per_launch: float, ms_per_launch: float, n: int, m: int, hbm: float, peak_kind: str):
     """Roofline of the basis flush (the solve's dominant kernel in deferred
-    mode): its compulsory HBM bytes per launch over its device time per launch
-    (CUDA events around every flush of the timed solves, the small
-    slot-maximum and coefficient-digit kernels included).  The tensor-core
+    mode): its compulsory HBM bytes per launch (basis slots once, x_j and
+    Pmat_j of the shifts it forms: those not converged by the previous flush)
+    over its device time per launch (CUDA events around every flush of the
+    timed solves, the small live-list, slot-maximum and coefficient-digit
+    kernels included).  The tensor-core
     work behind it is reported beside: 45 digit-pair products over K = 64 per
     48-element tile and group of 64 shifts, M = 128."""
     achieved = bytes_per_launch / (ms_per_launch * 1e-3) / 1e9
@@ -503,8 +505,9 @@ def run_adjoint_c5(args, dist: Dist):
 def run_flush_kernel(args):
     """The basis flush alone (hbk_flush_tc_run: slot maxima, coefficient
     digits, the tensor-core kernel) on random FP64 data of a solve's shape:
-    n elements, 64 shifts, 51 basis slots, p kept.  CUDA events around
-    `--steps` calls after `--warmup`; algorithmic bytes 8 n (L + 4 m)."""
+    n elements, 64 shifts, 51 basis slots, p kept, x_j and p_j panel-major
+    as in a solve.  CUDA events around `--steps` calls after `--warmup`;
+    algorithmic bytes 8 n (L + 4 m)."""
     import ctypes as C
 
     import torch
@@ -521,8 +524,9 @@ def run_flush_kernel(args):
     ld = (n + 31) // 32 * 32
     g = torch.Generator(device="cuda").manual_seed(0)
     V = torch.randn(L, ld, dtype=torch.float64, device="cuda", generator=g)
-    X = torch.randn(m, ld, dtype=torch.float64, device="cuda", generator=g)
-    P = torch.randn(m, ld, dtype=torch.float64, device="cuda", generator=g)
+    panel_elems = -(-n // 48) * 48 * m  # panel-major x_j and p_j
+    X = torch.randn(panel_elems, dtype=torch.float64, device="cuda", generator=g)
+    P = torch.randn(panel_elems, dtype=torch.float64, device="cuda", generator=g)
     Xc = torch.randn(m, cap, dtype=torch.float64, device="cuda", generator=g)
     Pc = torch.randn(m, cap, dtype=torch.float64, device="cuda", generator=g)
     own = torch.randn(m, 2, dtype=torch.float64, device="cuda", generator=g)

@@ -14,12 +14,16 @@
 // Diagonals past 8 are dropped (their total is below 2^-54 of the
 // row/element scale, the accuracy of an FP64 dot product of the same length).
 // The epilogue joins the nine exact diagonal sums in 64-bit integer arithmetic
-// and rounds once to FP64; only the own-vector terms use the FP64 pipe.  (The
+// (keeping floor(T / 2^12) of the 75-bit sum T: the dropped bits are below
+// 2^-56 of the row x element scale) and rounds once to FP64; only the
+// own-vector terms use the FP64 pipe.  (The
 // digit splitting is the error-free splitting of Ozaki, Ogita, Oishi and Rump
 // for matrix products, arranged here so that the exact sums fit TMEM.)
 //
 // One CTA per SM (203 KB of shared memory), persistent over tiles of 48
-// vector elements; 128 output rows per group of 64 shifts, ordered so that
+// vector elements (one panel of the panel-major x_j and p_j arrays, whose
+// values for all shifts lie in one contiguous block); 128 output rows per
+// group of 64 shifts, ordered so that
 // TMEM lanes 32q..32q+15 hold the x rows of shifts 16q..16q+15 and lanes
 // 32q+16..32q+31 their p rows.  Warps 0-3 make the basis digits of a tile
 // and thread 0 issues its MMAs (M=128, N up to 256, K=16; 52 per tile) into
@@ -27,6 +31,12 @@
 // that the next tile's MMAs run while they round, add the own-vector terms
 // and write x and p.  Every wait is bounded: a timeout sets an error flag,
 // the CTA skips its remaining work and still frees its TMEM.
+//
+// Only the live shifts are formed: a shift that had converged by the previous
+// flush has zero coefficients and own terms (0, 1) since that flush's reset,
+// so its rows would come out unchanged.  The rows of a group are the live
+// shifts in index order; a group without live shifts does nothing, and the
+// epilogue warps of a TMEM quadrant without live rows sit the tiles out.
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdint.h>
@@ -40,6 +50,7 @@ namespace {
 constexpr int TC_M = 128;
 constexpr int TC_N = 48;
 constexpr int TC_K = 64;
+static_assert(TC_N == HBK_PANEL, "a tile is one panel of x_j and p_j");
 constexpr int NDIG = 9;
 constexpr int NDIAG = 9;
 constexpr int A_SLICE = TC_M * TC_K * 2;  // 16384 B
@@ -64,8 +75,9 @@ constexpr uint64_t DIGIT_BIAS = 0x4081020408102040ull;
 // magic FP32 1.5 * 2^23: for |D| < 2^22, bits(D + MAGIC) = MAGIC_BITS + D
 constexpr float MAGIC = 12582912.0f;
 constexpr uint32_t MAGIC_BITS = 0x4B400000u;
-constexpr uint64_t HI_BIAS = (uint64_t)MAGIC_BITS * 2113665ull;    // * (2^21 + 2^14 + 2^7 + 1)
-constexpr uint64_t LO_BIAS = (uint64_t)MAGIC_BITS * 270549121ull;  // * (2^28 + 2^21 + 2^14 + 2^7 + 1)
+constexpr uint64_t HI_BIAS = (uint64_t)MAGIC_BITS * 2113665ull;  // * (2^21 + 2^14 + 2^7 + 1)
+constexpr uint64_t MID_BIAS = (uint64_t)MAGIC_BITS * 66052ull;   // * (2^16 + 2^9 + 2^2)
+constexpr uint64_t T_BIAS = (HI_BIAS << 23) + MID_BIAS;          // (mod 2^64)
 
 static_assert(ITEMS % BUILD_THREADS == 0, "builder items");
 static_assert(EPI_COLS % 4 == 0 && TC_N % 8 == 0, "epilogue columns");
@@ -186,30 +198,28 @@ __device__ __forceinline__ uint64_t madw(uint32_t a, uint32_t b, uint64_t c) {
     return d;
 }
 
-// the exact sum T = hs 2^35 + ls (|T| < 2^79) times 2^k, rounded to FP64
-// (round half up on a 64-bit window of |T| whose leading bit is bit 63;
-// bits of |T| below the window only break exact ties: error <= 0.5 ulp + 2^-64)
-__device__ __forceinline__ double join_diagonals(long long hs, long long ls, int k) {
-    const long long sg = (hs + (ls >> 35)) >> 63;  // sign of T = sign of floor(T / 2^35)
-    hs = (hs ^ sg) - sg;
-    ls = (ls ^ sg) - sg;
-    const unsigned long long th = (unsigned long long)(hs + (ls >> 35));  // |T| = th 2^35 + tl, th < 2^45
-    const unsigned long long tl = (unsigned long long)ls & ((1ull << 35) - 1);
-    unsigned long long W;
-    int lead;  // position of the leading bit of |T|
-    if (th >> 28) {
-        const int bl = 64 - __clzll((long long)th);  // 29..45
-        W = (th << (64 - bl)) | (tl >> (bl - 29));
-        lead = bl + 34;
-    } else {
-        const unsigned long long t64 = (th << 35) | tl;  // |T| < 2^63
-        if (t64 == 0) return 0.0;
-        const int z = __clzll((long long)t64);
-        W = t64 << z;
-        lead = 63 - z;
-    }
+// floor(T / 2^12) of the exact diagonal sum T = sum_d D_d 2^(7 (8 - d)), from
+// the biased FP32 bits B_d = MAGIC_BITS + D_d.  |D_d| <= (d + 1) 64 2^12, so
+// |T| < 2^74.03 and the result fits a signed 64-bit integer; the dropped bits
+// are below 2^-56 of the row x element scale (the dropped diagonals: 2^-54).
+// Arithmetic is modulo 2^64 (the biases cancel exactly).
+__device__ __forceinline__ long long diag_sum(const uint32_t (&B)[NDIAG]) {
+    const uint64_t h = madw(B[0], 1u << 21, madw(B[1], 1u << 14, madw(B[2], 1u << 7, (uint64_t)B[3])));
+    const uint64_t mid = madw(B[4], 1u << 16, madw(B[5], 1u << 9, (uint64_t)B[6] << 2));
+    const int lo = (int)(B[7] * 128u + B[8] - MAGIC_BITS * 129u);  // D_7 2^7 + D_8, |.| < 2^29
+    return (long long)((h << 23) + mid - T_BIAS + (uint64_t)(long long)(lo >> 12));
+}
+
+// T 2^k rounded to FP64: round half up on the 64-bit magnitude, whose leading
+// bit is normalised to bit 63 (error <= 0.5 ulp of the result)
+__device__ __forceinline__ double join_t(long long T, int k) {
+    const long long sg = T >> 63;
+    const unsigned long long a = (unsigned long long)((T ^ sg) - sg);
+    if (a == 0) return 0.0;
+    const int z = __clzll((long long)a);
+    const unsigned long long W = a << z;
     const unsigned long long mant = (W >> 11) + ((W >> 10) & 1);  // 2^52 .. 2^53 (carries into the exponent)
-    const int ebm1 = lead + k + 1022;                               // biased exponent - 1
+    const int ebm1 = 63 - z + k + 1022;                             // biased exponent - 1
     if ((unsigned)ebm1 > 2044u) {
         if (ebm1 < 0) return sg ? -0.0 : 0.0;  // below the normal range: negligible here
         return sg ? -INFINITY : INFINITY;
@@ -237,10 +247,29 @@ struct TcArgs {
     const unsigned char *aimg;           // per group: 9 digit slices of the 128 x 64 coefficient block
     const int *rowexp;    // per group: [128]
     const double *rown;   // per group: [128] own-term scalar (xi for x rows, rho for p rows)
-    double *X, *Pmat;     // [m][ld]
+    double *X, *Pmat;     // panel-major, m systems
     int m, keep_p;
+    const int *live;      // [0]: number of live shifts; [1 ..]: their indices, ascending
     int *err;
 };
+
+// live shifts: not converged (conv_k == 0) or converged after iteration
+// k_last (the last one the previous flush covered); one warp, index order
+__global__ void k_flush_live(const int *__restrict__ conv_k, int m, int k_last, int *live) {
+    int cnt = 0;
+    for (int base = 0; base < m; base += 32) {
+        const int j = base + (int)threadIdx.x;
+        bool on = false;
+        if (j < m) {
+            const int c = conv_k ? conv_k[j] : 0;
+            on = c == 0 || c > k_last;
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, on);
+        if (on) live[1 + cnt + __popc(b & ((1u << threadIdx.x) - 1u))] = j;
+        cnt += __popc(b);
+    }
+    if (threadIdx.x == 0) live[0] = cnt;
+}
 
 // ---- per-slot max |V[l]| (bits of a non-negative double order as integers)
 __global__ void __launch_bounds__(NT) k_slot_max(const double *__restrict__ V, size_t ld, unsigned n, int L,
@@ -267,14 +296,17 @@ __device__ __forceinline__ int row_shift(int r) { return ((r >> 5) << 4) | (r & 
 
 // ---- coefficient digits: one block per output row, one thread per slot
 __global__ void __launch_bounds__(TC_K) k_flush_prep(const double *__restrict__ Xc, const double *__restrict__ Pc,
-                                                     int cap, const double *__restrict__ own, int m, int L,
+                                                     int cap, const double *__restrict__ own, int L,
                                                      const unsigned long long *__restrict__ slot_max,
-                                                     unsigned char *aimg, int *rowexp, double *rown) {
+                                                     const int *__restrict__ live, unsigned char *aimg, int *rowexp,
+                                                     double *rown) {
     __shared__ unsigned long long s_max[2];
     const int r = blockIdx.x, g = blockIdx.y, l = threadIdx.x;
-    const int which = row_which(r), j = g * 64 + row_shift(r);
+    const int which = row_which(r), pos = g * 64 + row_shift(r);
+    if (g * 64 >= live[0]) return;  // the whole group is idle
+    const int j = pos < live[0] ? live[1 + pos] : -1;
     double a = 0.0;
-    if (j < m && l < L) {
+    if (j >= 0 && l < L) {
         const double c = (which ? Pc : Xc)[(size_t)j * cap + l];
         const unsigned long long sm = slot_max[l];
         a = sm ? ldexp(c, exp_of_bits(sm)) : 0.0;  // fold the slot's scale into the coefficient
@@ -299,7 +331,7 @@ __global__ void __launch_bounds__(TC_K) k_flush_prep(const double *__restrict__ 
         *reinterpret_cast<__nv_bfloat16 *>(img + (size_t)s * A_SLICE + off) = __float2bfloat16_rn(d[s]);
     if (l == 0) {
         rowexp[g * TC_M + r] = E;
-        rown[g * TC_M + r] = (j < m) ? own[2 * (size_t)j + which] : 0.0;
+        rown[g * TC_M + r] = (j >= 0) ? own[2 * (size_t)j + which] : 0.0;
     }
 }
 
@@ -325,13 +357,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int g = blockIdx.y;
+    // live rows of this group; the whole CTA leaves (before any barrier or
+    // TMEM allocation) when there are none
+    const int n_live = a.live[0];
+    const int g_live = n_live - 64 * g;
+    if (g_live <= 0) return;
+    const int live_quads = g_live >= 64 ? 4 : (g_live + 15) / 16;  // TMEM quadrants with a live row
 
     if (tid == 0) {
         mbar_init(bar_a, 1);
         mbar_init(bar_full, BUILD_THREADS);
         mbar_init(bar_mma, 1);
         mbar_init(bar_ready, 1);
-        mbar_init(bar_tfree, EPI_WARPS);
+        mbar_init(bar_tfree, (EPI_WARPS / 4) * live_quads);
         mbar_init(bar_cexp, BUILD_THREADS);
         *s_fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -495,21 +533,45 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                 mbar_arrive(bar_ready);
             }
         }
-    } else {
+    } else if ((warp & 3) < live_quads) {
         // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, columns
         // 16 c .. 16 c + 15 with c = (w - 4) / 4; lane u < 16 holds the x row
-        // of shift 16 (w % 4) + u, lane u + 16 its p row.
+        // of live shift 16 (w % 4) + u of the group, lane u + 16 its p row.
+        // (Warps of a quadrant without live rows skip this loop; the
+        // accumulator-free barrier counts only the others.)
         const int q = warp & 3, cg = (warp - BUILD_WARPS) >> 2;
         const int r = 32 * q + lane;
         const int which = row_which(r);
-        const int j = g * 64 + row_shift(r);
-        const bool live = j < a.m;
+        const int pos = g * 64 + row_shift(r);
+        const bool live = pos < n_live;
+        const int j = live ? a.live[1 + pos] : 0;
         const bool store = live && (which == 0 || a.keep_p);
         const int E = s_rowexp[r];
         const double own = s_rown[r];
         double *const prim = which ? a.Pmat : a.X;  // the row this lane loads and writes
         const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(cg * EPI_COLS);
-        constexpr uint32_t m7 = 1u << 7, m14 = 1u << 14, m21 = 1u << 21, m28 = 1u << 28;
+        // this lane's piece of a panel (system j, columns 16 cg .. 16 cg + 15):
+        // x rows in X, p rows in Pmat; consecutive panels m * 48 values apart
+        double *const pbase =
+            live && (which == 0 || a.Pmat) ? (which ? a.Pmat : a.X) + (size_t)j * TC_N + cg * EPI_COLS : nullptr;
+        const size_t pstride = (size_t)a.m * TC_N;
+        const bool have_p = a.Pmat != nullptr;
+        // x and p values of a tile, loaded one tile ahead: the loads are in
+        // flight while the warp waits for that tile's MMAs and drains them.
+        // 32-byte sector accesses (pieces are 16 values from a 32-byte aligned base)
+        double pv[EPI_COLS];
+        auto load_pv = [&](unsigned t) {
+            const unsigned c0 = t * TC_N + cg * EPI_COLS;
+            const double *src = pbase ? pbase + (size_t)t * pstride : nullptr;
+            if (src && c0 + EPI_COLS <= n) {
+#pragma unroll
+                for (int u = 0; u < EPI_COLS; u += 4) ld_sector(src + u, pv[u], pv[u + 1], pv[u + 2], pv[u + 3]);
+            } else {
+#pragma unroll
+                for (int u = 0; u < EPI_COLS; ++u) pv[u] = (src && c0 + u < n) ? src[u] : 0.0;
+            }
+        };
+        if (blockIdx.x < ntiles) load_pv(blockIdx.x);
         int it = 0;
         for (unsigned t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
             // the warp decides as one: tcgen05.ld and the shuffles below are warp-collective
@@ -520,8 +582,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                 break;
             }
             tc_fence_after();
-            // exact diagonal sums -> T = hs 2^35 + ls
-            long long hs[EPI_COLS], ls[EPI_COLS];
+            // exact diagonal sums -> floor(T / 2^12)
+            long long T[EPI_COLS];
 #pragma unroll
             for (int c4 = 0; c4 < EPI_COLS / 4; ++c4) {
                 uint32_t dv[NDIAG][4];
@@ -536,42 +598,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                     uint32_t B[NDIAG];
 #pragma unroll
                     for (int d = 0; d < NDIAG; ++d) B[d] = __float_as_uint(__uint_as_float(dv[d][u]) + MAGIC);
-                    const uint64_t h = madw(B[0], m21, madw(B[1], m14, madw(B[2], m7, (uint64_t)B[3])));
-                    const uint64_t l =
-                        madw(B[4], m28, madw(B[5], m21, madw(B[6], m14, madw(B[7], m7, (uint64_t)B[8]))));
-                    hs[4 * c4 + u] = (long long)(h - HI_BIAS);
-                    ls[4 * c4 + u] = (long long)(l - LO_BIAS);
+                    T[4 * c4 + u] = diag_sum(B);
                 }
             }
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(bar_tfree);
 
-            // x lanes load X, p lanes load Pmat (before the join, to hide the
-            // latency; 32-byte rows pieces, aligned since ld % 4 == 0 and
-            // c0 % 4 == 0); x lanes take the old Pmat from their p lane before
-            // it is overwritten
             const unsigned c0 = t * TC_N + cg * EPI_COLS;
             const bool full = c0 + EPI_COLS <= n;
-            double pv[EPI_COLS];
-            const double *src = prim ? prim + (size_t)j * ld + c0 : nullptr;
-            if (live && src && full) {
-#pragma unroll
-                for (int u = 0; u < EPI_COLS; u += 4) ld_sector(src + u, pv[u], pv[u + 1], pv[u + 2], pv[u + 3]);
-            } else {
-#pragma unroll
-                for (int u = 0; u < EPI_COLS; ++u) pv[u] = (live && src && c0 + u < n) ? src[u] : 0.0;
-            }
             const int *Fc = s_F + (it & 3) * TC_N + cg * EPI_COLS;
-            const bool have_p = a.Pmat != nullptr;
-            double *dst = store ? prim + (size_t)j * ld + c0 : nullptr;
-            // one pass per four columns: join, own-vector terms, store
+            double *dst = store && pbase ? pbase + (size_t)t * pstride : nullptr;
+            // one pass per four columns: round, own-vector terms (x lanes take
+            // the old Pmat from their p lane), store
 #pragma unroll
             for (int u = 0; u < EPI_COLS; u += 4) {
                 double o4[4];
 #pragma unroll
                 for (int h = 0; h < 4; ++h) {
-                    const double G = E != EXP_NONE ? join_diagonals(hs[u + h], ls[u + h], E + Fc[u + h] - 68) : 0.0;
+                    const double G = E != EXP_NONE ? join_t(T[u + h], E + Fc[u + h] - 56) : 0.0;
                     const double po = __shfl_xor_sync(0xffffffffu, pv[u + h], 16);
                     const double pold = which ? pv[u + h] : (have_p ? po : 0.0);
                     const double y = fma(own, pold, G);
@@ -587,6 +632,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                     }
                 }
             }
+            if (t + gridDim.x < ntiles) load_pv(t + gridDim.x);
         }
     }
     // every path ends here: let copies and MMAs still in flight after a
@@ -610,18 +656,22 @@ extern "C" {
 
 size_t hbk_flush_tc_workspace_bytes(int m) {
     const int groups = (m + 63) / 64;
-    return 256 + 64 * sizeof(unsigned long long) + (size_t)groups * (A_BYTES + TC_M * (sizeof(int) + sizeof(double)));
+    return 256 + 64 * sizeof(unsigned long long) + (size_t)groups * (A_BYTES + TC_M * (sizeof(int) + sizeof(double))) +
+           sizeof(int) * ((size_t)(m > 0 ? m : 0) + 1);
 }
 
 int hbk_flush_tc_max_slots(void) { return TC_K; }
 
-// x_j (and p_j when keep_p) from the first L basis slots on the tensor cores;
-// ws: device workspace of hbk_flush_tc_workspace_bytes(m), err: device int.
-int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
-                     const double *own, int m, double *X, double *Pmat, int keep_p, void *ws, int *err,
-                     cudaStream_t st) {
-    // x and p rows are accessed in 32-byte sectors: 32-byte aligned rows
-    if (L > TC_K || L < 1 || m < 1 || n == 0 || (ld & 3) || ((uintptr_t)X & 31) || ((uintptr_t)Pmat & 31))
+// x_j (and p_j when keep_p) from the first L basis slots on the tensor cores,
+// for the live shifts only: conv_k[j] == 0 or conv_k[j] > k_last (conv_k
+// NULL: every shift).  V: [L][ld] slots; X, Pmat: panel-major (HBK_PANEL),
+// m systems, 32-byte aligned; ws: device workspace of
+// hbk_flush_tc_workspace_bytes(m), err: device int.
+int hbk_flush_tc_run_live(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
+                          const double *own, int m, double *X, double *Pmat, int keep_p, const int *conv_k,
+                          int k_last, void *ws, int *err, cudaStream_t st) {
+    // x and p pieces are accessed in 32-byte sectors: 32-byte aligned arrays
+    if (L > TC_K || L < 1 || m < 1 || n == 0 || ld < n || ((uintptr_t)X & 31) || ((uintptr_t)Pmat & 31))
         return (int)cudaErrorInvalidValue;
     const int groups = (m + 63) / 64;
     unsigned char *w = (unsigned char *)ws;
@@ -629,11 +679,13 @@ int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double
     unsigned char *aimg = w + 256 + 64 * sizeof(unsigned long long);
     int *rowexp = (int *)(aimg + (size_t)groups * A_BYTES);
     double *rown = (double *)(rowexp + groups * TC_M);
+    int *live = (int *)(rown + (size_t)groups * TC_M);
     cudaError_t e = cudaMemsetAsync(slot_max, 0, 64 * sizeof(unsigned long long), st);
     if (e) return (int)e;
+    k_flush_live<<<1, 32, 0, st>>>(conv_k, m, k_last, live);
     dim3 gs(grid_for(n, 16) < 64 ? grid_for(n, 16) : 64, L);
     k_slot_max<<<gs, NT, 0, st>>>(V, ld, n, L, slot_max);
-    k_flush_prep<<<dim3(TC_M, groups), TC_K, 0, st>>>(Xc, Pc, cap, own, m, L, slot_max, aimg, rowexp, rown);
+    k_flush_prep<<<dim3(TC_M, groups), TC_K, 0, st>>>(Xc, Pc, cap, own, L, slot_max, live, aimg, rowexp, rown);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     static unsigned attr_set = 0;  // one bit per device
@@ -645,9 +697,23 @@ int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const unsigned ntiles = (n + TC_N - 1) / TC_N;
     const unsigned gx = ntiles < (unsigned)sms ? ntiles : (unsigned)sms;
-    TcArgs args{V, ld, n, L, slot_max, aimg, rowexp, rown, X, Pmat, m, keep_p, err};
+    TcArgs args{V, ld, n, L, slot_max, aimg, rowexp, rown, X, Pmat, m, keep_p, live, err};
     k_flush_tc<<<dim3(gx, groups), TC_THREADS, SMEM_BYTES, st>>>(args);
     return (int)cudaGetLastError();
+}
+
+// device address of the live-shift count of the last hbk_flush_tc_run_live on ws
+const int *hbk_flush_tc_live_count(const void *ws, int m) {
+    const int groups = (m + 63) / 64;
+    const unsigned char *w = (const unsigned char *)ws + 256 + 64 * sizeof(unsigned long long) + (size_t)groups * A_BYTES;
+    return (const int *)(w + (size_t)groups * TC_M * (sizeof(int) + sizeof(double)));
+}
+
+// every shift live
+int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
+                     const double *own, int m, double *X, double *Pmat, int keep_p, void *ws, int *err,
+                     cudaStream_t st) {
+    return hbk_flush_tc_run_live(V, ld, n, L, Xc, Pc, cap, own, m, X, Pmat, keep_p, nullptr, 0, ws, err, st);
 }
 
 }  // extern "C"

@@ -101,18 +101,30 @@ typedef struct {
     int m, kcap;
 } hbk_shifts;
 
+/* Deferred mode keeps x_j and the flushed p_j panel-major: element i of
+ * system j at ((i / HBK_PANEL) m + j) HBK_PANEL + i % HBK_PANEL.  The basis
+ * flush forms every system's values for one panel of HBK_PANEL elements at a
+ * time, so it reads and writes one contiguous block per panel instead of m
+ * rows that lie n elements apart. */
+#define HBK_PANEL 48
+static inline size_t hbk_panel_elems(unsigned n, int m) {
+    return ((size_t)n + HBK_PANEL - 1) / HBK_PANEL * HBK_PANEL * (size_t)(m > 0 ? m : 1);
+}
+
 typedef struct {
     unsigned n;
     double *r_hat;              /* shadow residual = b */
     double *rbuf[2];            /* r_{k-1} / r_k, alternating with k */
     double *s, *q, *y;
-    double *X, *P;              /* [m][n] shift-major (P unused in deferred mode) */
+    double *X, *P;              /* [m][n] shift-major (P unused in deferred mode; X written at the end) */
     /* deferred (Krylov basis) mode */
     double *V;                  /* [slot_cap][n] */
     double *ps;                 /* the seed's search vector */
     double *Xc, *Pc;            /* [m][slot_cap] coefficients */
     double *own;                /* [m][2]: coefficient of the flushed p_j in x_j and in p_j */
-    double *Pmat;               /* [m][n] flushed p_j (allocated on the first flush) */
+    double *Pmat;               /* flushed p_j, panel-major (allocated on the first flush) */
+    double *Xp;                 /* x_j during the solve, panel-major */
+    int pm;                     /* systems per panel (m) */
     int slot_cap;
     int deferred;
 } hbk_vectors;
@@ -153,8 +165,9 @@ int hbk_true_residuals(const hbk_matrix *A, const double *X, const double *b, co
 
 /* basis flush on the tensor cores (flush_tc.cu): x_j += xi_j Pmat_j + Xc_j . V,
  * p_j = rho_j Pmat_j + Pc_j . V over the first L <= hbk_flush_tc_max_slots()
- * slots, FP64-accurate; ws of hbk_flush_tc_workspace_bytes(m) bytes; *err set
- * on a bounded-wait timeout.  No reset (see hbk_deferred_reset). */
+ * slots, FP64-accurate; X and Pmat panel-major (HBK_PANEL) with m systems;
+ * ws of hbk_flush_tc_workspace_bytes(m) bytes; *err set on a bounded-wait
+ * timeout.  No reset (see hbk_deferred_reset). */
 /* COO -> CSR on the device, stable within rows (csrc/coo_csr.cu) */
 size_t hbk_coo_to_csr_tmp_bytes(unsigned nnz);
 int hbk_coo_to_csr(unsigned n, unsigned nnz, const unsigned *row, const unsigned *col, const double *val,
@@ -172,6 +185,14 @@ int hbk_flush_tc_max_slots(void);
 int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
                      const double *own, int m, double *X, double *Pmat, int keep_p, void *ws, int *err,
                      cudaStream_t st);
+/* the same for the live shifts only (conv_k[j] == 0 or conv_k[j] > k_last; the
+ * others' rows are left as they are); conv_k: device [m] or NULL (all live) */
+int hbk_flush_tc_run_live(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
+                          const double *own, int m, double *X, double *Pmat, int keep_p, const int *conv_k,
+                          int k_last, void *ws, int *err, cudaStream_t st);
+const int *hbk_flush_tc_live_count(const void *ws, int m); /* device int: live shifts of the last run on ws */
+/* X[j][i] (leading dimension ld) = Xp in panel layout with m systems, i < n */
+int hbk_panel_to_rows(const double *Xp, int m, unsigned n, double *X, size_t ld, cudaStream_t st);
 /* after a flush: zero the coefficients, own = (0, keep_p), basis slot 0 = r_{k-1} */
 int hbk_deferred_reset(const hbk_vectors *v, const hbk_shifts *sh, int keep_p, cudaStream_t st);
 

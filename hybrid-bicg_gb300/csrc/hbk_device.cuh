@@ -68,6 +68,12 @@ __device__ __forceinline__ double sum_partials(const double *partials, int npart
 
 __device__ __forceinline__ bool fin(double v) { return isfinite(v) != 0; }
 
+// index of element i of system j in a panel-major array of m systems
+__device__ __forceinline__ size_t panel_idx(int j, unsigned i, int m) {
+    const unsigned p = i / HBK_PANEL;
+    return ((size_t)p * (unsigned)m + (unsigned)j) * HBK_PANEL + (i - p * HBK_PANEL);
+}
+
 // ---------------------------------------------------------------------------
 // Row-block CSR SpMV core.
 //

@@ -414,11 +414,15 @@ __global__ void __launch_bounds__(NT) k_seed_update(Ctx c) {
     double *__restrict__ rn = vec_r_new(c, sc);
     double2 acc = make_double2(0.0, 0.0);
     // the seed's x in both shift modes (in deferred mode its x coefficients
-    // are kept at zero, so the basis flushes leave this row as it is)
-    double *__restrict__ xs = c.v.X + (size_t)seed * ldn(n);
+    // are kept at zero, so the basis flushes leave it as it is; there x_j are
+    // panel-major)
+    const bool dm = c.v.deferred != 0;
+    double *__restrict__ xrow = dm ? c.v.Xp : c.v.X + (size_t)seed * ldn(n);
+    const int pm = c.v.pm;
     for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
         const double qi = q[i];
-        xs[i] = fma(w, qi, fma(a, ps[i], xs[i]));
+        double *xi = dm ? xrow + panel_idx(seed, (unsigned)i, pm) : xrow + i;
+        *xi = fma(w, qi, fma(a, ps[i], *xi));
         const double r = fma(-w, y[i], qi);
         rn[i] = r;
         acc.x = fma(r, r, acc.x);
@@ -619,10 +623,10 @@ __global__ void __launch_bounds__(NT) k_materialize_ps(Ctx c) {
     const size_t ld = ldn(n);
     const double *pc = c.v.Pc + (size_t)t * c.v.slot_cap;
     const double rho = c.v.own[2 * (size_t)t + 1];
-    const double *pm = c.v.Pmat ? c.v.Pmat + (size_t)t * ld : nullptr;
+    const double *pmat = c.v.Pmat;  // panel-major
     for (size_t i0 = (size_t)blockIdx.x * NT; i0 < n; i0 += (size_t)gridDim.x * NT) {
         const size_t i = i0 + threadIdx.x;
-        double acc = (pm && i < n) ? rho * pm[i] : 0.0;
+        double acc = (pmat && i < n) ? rho * pmat[panel_idx(t, (unsigned)i, c.v.pm)] : 0.0;
         for (int l0 = 0; l0 < L; l0 += 1024) {
             const int cnt = min(1024, L - l0);
             __syncthreads();
@@ -657,7 +661,8 @@ __global__ void __launch_bounds__(NT) k_flush(Ctx c, int keep_p, int which) {
     int L = 0;
     for (int t = 0; t < g; t++) L = max(L, c.sh.lslot[j0 + t]);
     const double *coef = which == 0 ? c.v.Xc : c.v.Pc;
-    double *out = which == 0 ? c.v.X : c.v.Pmat;
+    double *out = which == 0 ? c.v.Xp : c.v.Pmat;  // panel-major
+    const int pm = c.v.pm;
     for (size_t i0 = (size_t)blockIdx.x * NT; i0 < n; i0 += (size_t)gridDim.x * NT) {
         const size_t i = i0 + threadIdx.x;
         double acc[GROUP];
@@ -666,12 +671,13 @@ __global__ void __launch_bounds__(NT) k_flush(Ctx c, int keep_p, int which) {
             acc[t] = 0.0;
             if (t < g && i < n) {
                 const int j = j0 + t;
-                const double *pm = c.v.Pmat ? c.v.Pmat + (size_t)j * ld : nullptr;
+                const size_t pi = panel_idx(j, (unsigned)i, pm);
+                const double *pmat = c.v.Pmat;
                 if (which == 0) {
-                    acc[t] = c.v.X[(size_t)j * ld + i];
-                    if (pm) acc[t] = fma(c.v.own[2 * (size_t)j], pm[i], acc[t]);
-                } else if (pm) {
-                    acc[t] = c.v.own[2 * (size_t)j + 1] * pm[i];
+                    acc[t] = c.v.Xp[pi];
+                    if (pmat) acc[t] = fma(c.v.own[2 * (size_t)j], pmat[pi], acc[t]);
+                } else if (pmat) {
+                    acc[t] = c.v.own[2 * (size_t)j + 1] * pmat[pi];
                 }
             }
         }
@@ -694,7 +700,7 @@ __global__ void __launch_bounds__(NT) k_flush(Ctx c, int keep_p, int which) {
         if (i < n) {
 #pragma unroll
             for (int t = 0; t < GROUP; t++)
-                if (t < g) out[(size_t)(j0 + t) * ld + i] = acc[t];
+                if (t < g) out[panel_idx(j0 + t, (unsigned)i, pm)] = acc[t];
         }
     }
     (void)keep_p;
@@ -731,9 +737,32 @@ __global__ void __launch_bounds__(NT) k_flush_reset(Ctx c, int keep_p) {
     }
 }
 
+// X[j][i] = element i of system j of the panel-major Xp: one block per panel
+// (m * HBK_PANEL values read contiguously, written as runs of HBK_PANEL)
+__global__ void __launch_bounds__(NT) k_panel_to_rows(const double *__restrict__ Xp, int m, unsigned n,
+                                                      double *__restrict__ X, size_t ld) {
+    const unsigned per = (unsigned)m * HBK_PANEL;
+    const size_t np = ((size_t)n + HBK_PANEL - 1) / HBK_PANEL;
+    for (size_t p = blockIdx.x; p < np; p += gridDim.x) {
+        const double *src = Xp + p * per;
+        const size_t i0 = p * HBK_PANEL;
+        for (unsigned r = threadIdx.x; r < per; r += NT) {
+            const unsigned j = r / HBK_PANEL, c = r - j * HBK_PANEL;
+            if (i0 + c < n) X[(size_t)j * ld + i0 + c] = src[r];
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+int hbk_panel_to_rows(const double *Xp, int m, unsigned n, double *X, size_t ld, cudaStream_t st) {
+    if (m <= 0 || n == 0) return 0;
+    const size_t np = ((size_t)n + HBK_PANEL - 1) / HBK_PANEL;
+    k_panel_to_rows<<<(unsigned)(np < 4864 ? np : 4864), NT, 0, st>>>(Xp, m, n, X, ld);
+    return (int)cudaGetLastError();
+}
 
 static Ctx make_ctx(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh) {
     Ctx c;
@@ -762,7 +791,11 @@ int hbk_fused_init(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *
         k_init_coef<<<grid_for((unsigned)((size_t)sh->m * v->slot_cap), 1), NT, 0, st>>>(c);
         if ((e = (int)cudaGetLastError())) return e;
     }
-    if ((e = (int)cudaMemsetAsync(v->X, 0, sizeof(double) * ld * (size_t)sh->m, st))) return e;
+    if (v->deferred) {
+        if ((e = (int)cudaMemsetAsync(v->Xp, 0, sizeof(double) * hbk_panel_elems(n, v->pm), st))) return e;
+    } else if ((e = (int)cudaMemsetAsync(v->X, 0, sizeof(double) * ld * (size_t)sh->m, st))) {
+        return e;
+    }
     k_init<<<1, NT, 0, st>>>(c, seed, tol);
     return (int)cudaGetLastError();
 }

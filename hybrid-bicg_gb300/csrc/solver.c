@@ -707,11 +707,13 @@ int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_
     } else {
         v->deferred = 1;
         DALLOC(v->ps, vb);
+        v->pm = mm;
+        DALLOC(v->Xp, sizeof(double) * hbk_panel_elems(n, mm));
         size_t fr = 0, tot = 0;
         CUDA_TRY(cudaMemGetInfo(&fr, &tot));
         double frac = p.basis_mem_frac > 0 ? p.basis_mem_frac : 0.6;
-        /* keep room for a later flush buffer (m*n) out of the basis budget */
-        double budget = frac * (double)fr - (double)vb * mm;
+        /* keep room for the flushed p_j (allocated on the first flush) */
+        double budget = frac * (double)fr - (double)sizeof(double) * (double)hbk_panel_elems(n, mm);
         long cap = (long)(budget / (double)vb);
         long want = 2L * s->kcap + 8;
         if (cap > want) cap = want;
@@ -729,6 +731,8 @@ int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_
             v->deferred = 0;
             cudaFree(v->ps);
             v->ps = NULL;
+            cudaFree(v->Xp);
+            v->Xp = NULL;
             DALLOC(v->rbuf[0], vb);
             DALLOC(v->rbuf[1], vb);
             DALLOC(v->q, vb);
@@ -799,7 +803,7 @@ void hbicg_solver_destroy(hbicg_solver *s) {
     hbk_vectors *v = &s->v;
     hbk_shifts *sh = &s->sh;
     void *ptrs[] = {v->r_hat, v->rbuf[0], v->rbuf[1], v->s, v->q, v->y, v->X, v->P, v->V, v->ps, v->Xc, v->Pc,
-                    v->own, v->Pmat, s->d_sc, s->d_sigma, sh->a_hist, sh->b_hist, sh->w_hist, sh->ratio, sh->pi,
+                    v->own, v->Pmat, v->Xp, s->d_sc, s->d_sigma, sh->a_hist, sh->b_hist, sh->w_hist, sh->ratio, sh->pi,
                     sh->eta, sh->zeta, sh->done, sh->conv_k, sh->act_list, sh->lslot, sh->coef, sh->sw_k,
                     sh->rr_hist, sh->sw_seed, sh->act_hist, sh->partials, sh->counters, s->d_b, s->d_res, s->d_dot, s->d_rold,
                     s->d_qcopy, s->tc_ws, s->d_tc_err};
@@ -1015,8 +1019,9 @@ static int capture_graph(hbicg_solver *s) {
 static int ensure_pmat(hbicg_solver *s) {
     if (s->v.Pmat) return HBICG_OK;
     const int mm = s->m > 0 ? s->m : 1;
-    CUDA_TRY(cudaMalloc((void **)&s->v.Pmat, sizeof(double) * s->ld * (size_t)mm));
-    CUDA_TRY(cudaMemsetAsync(s->v.Pmat, 0, sizeof(double) * s->ld * (size_t)mm, s->ctx->stream));
+    const size_t bytes = sizeof(double) * hbk_panel_elems(s->A->k.n, mm); /* panel-major */
+    CUDA_TRY(cudaMalloc((void **)&s->v.Pmat, bytes));
+    CUDA_TRY(cudaMemsetAsync(s->v.Pmat, 0, bytes, s->ctx->stream));
     /* the graphs captured the old (null) Pmat pointer: capture again */
     if (s->graph) {
         cudaGraphExecDestroy(s->graph);
@@ -1027,16 +1032,26 @@ static int ensure_pmat(hbicg_solver *s) {
 
 /* Form x_j (and p_j) from the L basis slots in use: on the tensor cores when
  * the basis fits one K = 64 operand, else with the FP64 kernel; then reset. */
-static int do_flush(hbicg_solver *s, int keep_p, int L, int *launches) {
+/* k_last: the last iteration the previous flush covered (0 before the first).
+ * A shift that converged at or before it has had zero coefficients since
+ * that flush, so the tensor-core flush leaves its rows out. */
+static int do_flush(hbicg_solver *s, int keep_p, int L, int k_last, int *launches) {
     cudaStream_t st = s->ctx->stream;
-    /* basis slots read once; x_j read and written; Pmat_j read (and written) */
-    s->flush_bytes += 8.0 * s->A->k.n * ((double)L + (keep_p ? 4.0 : 3.0) * s->m);
+    /* basis slots read once; x_j read and written; Pmat_j read (and written),
+     * for the shifts the flush forms */
+    const double per_shift = keep_p ? 4.0 : 3.0;
     if (s->tc_ws && L >= 1 && L <= hbk_flush_tc_max_slots()) {
-        HBK_TRY(hbk_flush_tc_run(s->v.V, s->ld, s->A->k.n, L, s->v.Xc, s->v.Pc, s->v.slot_cap, s->v.own, s->m, s->v.X,
-                                 s->v.Pmat, keep_p, s->tc_ws, s->d_tc_err, st));
+        HBK_TRY(hbk_flush_tc_run_live(s->v.V, s->ld, s->A->k.n, L, s->v.Xc, s->v.Pc, s->v.slot_cap, s->v.own, s->m,
+                                      s->v.Xp, s->v.Pmat, keep_p, s->sh.conv_k, k_last, s->tc_ws, s->d_tc_err, st));
+        int n_live = 0; /* pageable destination: the copy waits for the flush */
+        CUDA_TRY(cudaMemcpyAsync(&n_live, hbk_flush_tc_live_count(s->tc_ws, s->m), sizeof(int),
+                                 cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        s->flush_bytes += 8.0 * s->A->k.n * ((double)L + per_shift * n_live);
         HBK_TRY(hbk_deferred_reset(&s->v, &s->sh, keep_p, st));
-        *launches += 4;
+        *launches += 5;
     } else {
+        s->flush_bytes += 8.0 * s->A->k.n * ((double)L + per_shift * s->m);
         HBK_TRY(hbk_deferred_flush(&s->v, &s->sh, keep_p, st));
         *launches += keep_p ? 3 : 2;
     }
@@ -1057,6 +1072,7 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, dou
      * the basis pauses it; bound the host loop all the same */
     long guard = 0;
     const long guard_max = 4L * s->kcap / s->chunk + 64;
+    int k_flushed = 0; /* last iteration covered by a flush */
     for (;;) {
         if (++guard > guard_max) {
             set_msg("fused loop made no progress after %ld chunks", guard_max);
@@ -1080,8 +1096,9 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, dou
             if (rc) return rc;
             float t = 0.f;
             CUDA_TRY(cudaEventRecord(s->ctx->evf0, st));
-            rc = do_flush(s, 1, h->slots, launches);
+            rc = do_flush(s, 1, h->slots, k_flushed, launches);
             if (rc) return rc;
+            k_flushed = h->k - 1;
             CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
             CUDA_TRY(cudaEventSynchronize(s->ctx->evf1));
             CUDA_TRY(cudaEventElapsedTime(&t, s->ctx->evf0, s->ctx->evf1));
@@ -1094,9 +1111,12 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, dou
     if (s->v.deferred) {
         float t = 0.f;
         CUDA_TRY(cudaEventRecord(s->ctx->evf0, st));
-        int rc = do_flush(s, 0, h->slots, launches);
+        int rc = do_flush(s, 0, h->slots, k_flushed, launches);
         if (rc) return rc;
         CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
+        /* x_j were panel-major during the solve */
+        HBK_TRY(hbk_panel_to_rows(s->v.Xp, s->v.pm, s->A->k.n, s->v.X, s->ld, st));
+        ++*launches;
         CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
         int tc_err = 0;
         if (s->d_tc_err) CUDA_TRY(cudaMemcpyAsync(&tc_err, s->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
