@@ -410,7 +410,7 @@ def run_batch_c4(args, dist: Dist):
     pkg = graft.load_package()
     fams = pkg.workloads.batched_families(256)
     kw = dict(tol=1e-10, max_iter=10000, shift_mode=args.shift_mode, flush=args.flush, true_residuals=True,
-              refine=not args.no_refine)
+              refine=not args.no_refine, basis_block=args.basis_block)
     for _ in range(max(1, min(args.warmup, 1))):
         pkg.batch_solve(fams, workers=args.workers, **kw)
     walls, res = [], None

@@ -664,12 +664,13 @@ int hbk_flush_tc_max_slots(void) { return TC_K; }
 
 // x_j (and p_j when keep_p) from the first L basis slots on the tensor cores,
 // for the live shifts only: conv_k[j] == 0 or conv_k[j] > k_last (conv_k
-// NULL: every shift).  V: [L][ld] slots; X, Pmat: panel-major (HBK_PANEL),
+// NULL: every shift).  slot_max: bits of each slot's max |value| (NULL:
+// computed here).  V: [L][ld] slots; X, Pmat: panel-major (HBK_PANEL),
 // m systems, 32-byte aligned; ws: device workspace of
 // hbk_flush_tc_workspace_bytes(m), err: device int.
 int hbk_flush_tc_run_live(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
                           const double *own, int m, double *X, double *Pmat, int keep_p, const int *conv_k,
-                          int k_last, void *ws, int *err, cudaStream_t st) {
+                          int k_last, const unsigned long long *slot_max_in, void *ws, int *err, cudaStream_t st) {
     // x and p pieces are accessed in 32-byte sectors: 32-byte aligned arrays
     if (L > TC_K || L < 1 || m < 1 || n == 0 || ld < n || ((uintptr_t)X & 31) || ((uintptr_t)Pmat & 31))
         return (int)cudaErrorInvalidValue;
@@ -680,11 +681,15 @@ int hbk_flush_tc_run_live(const double *V, size_t ld, unsigned n, int L, const d
     int *rowexp = (int *)(aimg + (size_t)groups * A_BYTES);
     double *rown = (double *)(rowexp + groups * TC_M);
     int *live = (int *)(rown + (size_t)groups * TC_M);
-    cudaError_t e = cudaMemsetAsync(slot_max, 0, 64 * sizeof(unsigned long long), st);
-    if (e) return (int)e;
+    cudaError_t e = cudaSuccess;
     k_flush_live<<<1, 32, 0, st>>>(conv_k, m, k_last, live);
-    dim3 gs(grid_for(n, 16) < 64 ? grid_for(n, 16) : 64, L);
-    k_slot_max<<<gs, NT, 0, st>>>(V, ld, n, L, slot_max);
+    if (slot_max_in) {
+        slot_max = (unsigned long long *)slot_max_in;  // kept by the kernels that wrote the slots
+    } else {
+        if ((e = cudaMemsetAsync(slot_max, 0, 64 * sizeof(unsigned long long), st))) return (int)e;
+        dim3 gs(grid_for(n, 16) < 64 ? grid_for(n, 16) : 64, L);
+        k_slot_max<<<gs, NT, 0, st>>>(V, ld, n, L, slot_max);
+    }
     k_flush_prep<<<dim3(TC_M, groups), TC_K, 0, st>>>(Xc, Pc, cap, own, L, slot_max, live, aimg, rowexp, rown);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -713,7 +718,7 @@ const int *hbk_flush_tc_live_count(const void *ws, int m) {
 int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
                      const double *own, int m, double *X, double *Pmat, int keep_p, void *ws, int *err,
                      cudaStream_t st) {
-    return hbk_flush_tc_run_live(V, ld, n, L, Xc, Pc, cap, own, m, X, Pmat, keep_p, nullptr, 0, ws, err, st);
+    return hbk_flush_tc_run_live(V, ld, n, L, Xc, Pc, cap, own, m, X, Pmat, keep_p, nullptr, 0, nullptr, ws, err, st);
 }
 
 }  // extern "C"

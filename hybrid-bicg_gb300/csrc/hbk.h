@@ -124,6 +124,7 @@ typedef struct {
     double *own;                /* [m][2]: coefficient of the flushed p_j in x_j and in p_j */
     double *Pmat;               /* flushed p_j, panel-major (allocated on the first flush) */
     double *Xp;                 /* x_j during the solve, panel-major */
+    unsigned long long *slot_max; /* [slot_cap] bits of max |V[l]|, kept by the kernels that write the slots */
     int pm;                     /* systems per panel (m) */
     int slot_cap;
     int deferred;
@@ -186,10 +187,11 @@ int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double
                      const double *own, int m, double *X, double *Pmat, int keep_p, void *ws, int *err,
                      cudaStream_t st);
 /* the same for the live shifts only (conv_k[j] == 0 or conv_k[j] > k_last; the
- * others' rows are left as they are); conv_k: device [m] or NULL (all live) */
+ * others' rows are left as they are); conv_k: device [m] or NULL (all live);
+ * slot_max: device [L] bits of each slot's max |value|, or NULL (computed) */
 int hbk_flush_tc_run_live(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
                           const double *own, int m, double *X, double *Pmat, int keep_p, const int *conv_k,
-                          int k_last, void *ws, int *err, cudaStream_t st);
+                          int k_last, const unsigned long long *slot_max, void *ws, int *err, cudaStream_t st);
 const int *hbk_flush_tc_live_count(const void *ws, int m); /* device int: live shifts of the last run on ws */
 /* X[j][i] (leading dimension ld) = Xp in panel layout with m systems, i < n */
 int hbk_panel_to_rows(const double *Xp, int m, unsigned n, double *X, size_t ld, cudaStream_t st);

@@ -68,6 +68,30 @@ __device__ __forceinline__ double sum_partials(const double *partials, int npart
 
 __device__ __forceinline__ bool fin(double v) { return isfinite(v) != 0; }
 
+// max of v over the block (every thread calls), then one atomicMax into *out
+// when it is nonzero (bits of non-negative doubles order as unsigned
+// integers); `sh` needs NW values
+__device__ __forceinline__ void block_max_to(unsigned long long v, unsigned long long *sh, unsigned long long *out) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+        v = t > v ? t : v;
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = 0;
+        for (int i = 0; i < NW; ++i) m = sh[i] > m ? sh[i] : m;
+        if (m) atomicMax(out, m);
+    }
+}
+
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+}
+
 // index of element i of system j in a panel-major array of m systems
 __device__ __forceinline__ size_t panel_idx(int j, unsigned i, int m) {
     const unsigned p = i / HBK_PANEL;

@@ -153,8 +153,10 @@ __global__ void __launch_bounds__(NT) k_seed_s(Ctx c) {
     }
 }
 
-// K2: q = r_{k-1} - alpha s
+// K2: q = r_{k-1} - alpha s (deferred mode: q is a basis slot; its max |q| is
+// kept for the flush)
 __global__ void __launch_bounds__(NT) k_seed_q(Ctx c) {
+    __shared__ unsigned long long smx[NW];
     const hbk_scalars *sc = c.sh.sc;
     if (stopped(sc)) return;
     const double a = sc->alpha;
@@ -162,7 +164,14 @@ __global__ void __launch_bounds__(NT) k_seed_q(Ctx c) {
     const double *__restrict__ s = c.v.s;
     double *__restrict__ q = vec_q(c, sc);
     const unsigned n = c.v.n;
-    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) q[i] = fma(-a, s[i], ro[i]);
+    unsigned long long mx = 0;
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
+        const double qi = fma(-a, s[i], ro[i]);
+        q[i] = qi;
+        const unsigned long long b = abs_bits(qi);
+        mx = b > mx ? b : mx;
+    }
+    if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + sc->slots);
 }
 
 // K3: y = (A + sigma_s I) q, (q,q) and (q,y)
@@ -402,6 +411,7 @@ __device__ void seed_step_scalars(const Ctx &c, double rr, double rrh) {
 // K4: x_s += alpha p_s + omega q ; r_k = q - omega y ; (r,r), (r^,r)
 __global__ void __launch_bounds__(NT) k_seed_update(Ctx c) {
     __shared__ double sh[2 * NW];
+    __shared__ unsigned long long smx[NW];
     hbk_scalars *sc = c.sh.sc;
     if (stopped(sc)) return;
     const double a = sc->alpha, w = sc->omega;
@@ -413,6 +423,7 @@ __global__ void __launch_bounds__(NT) k_seed_update(Ctx c) {
     const double *__restrict__ rh = c.v.r_hat;
     double *__restrict__ rn = vec_r_new(c, sc);
     double2 acc = make_double2(0.0, 0.0);
+    unsigned long long mx = 0;
     // the seed's x in both shift modes (in deferred mode its x coefficients
     // are kept at zero, so the basis flushes leave it as it is; there x_j are
     // panel-major)
@@ -427,7 +438,10 @@ __global__ void __launch_bounds__(NT) k_seed_update(Ctx c) {
         rn[i] = r;
         acc.x = fma(r, r, acc.x);
         acc.y = fma(rh[i], r, acc.y);
+        const unsigned long long b = abs_bits(r);
+        mx = b > mx ? b : mx;
     }
+    if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + sc->slots + 1);  // r_k: a basis slot
     acc = block_sum2(acc, sh);
     if (threadIdx.x == 0) {
         c.sh.partials[blockIdx.x] = acc.x;
@@ -536,6 +550,7 @@ __global__ void __launch_bounds__(NT) k_shift_update(Ctx c) {
 // K5 (deferred): p_s update; on a switch the rescaled r_k goes to a new slot
 __global__ void __launch_bounds__(NT) k_seed_p_deferred(Ctx c) {
     __shared__ double sh[NW];
+    __shared__ unsigned long long smx[NW];
     hbk_scalars *sc = c.sh.sc;
     if (stopped(sc)) return;
     const double bk = sc->beta, bw = -mul(bk, sc->omega);
@@ -549,6 +564,7 @@ __global__ void __launch_bounds__(NT) k_seed_p_deferred(Ctx c) {
     double *__restrict__ rsl = c.v.V + (size_t)(sc->slots + 2) * ld;
     const double *__restrict__ rh = c.v.r_hat;
     double acc = 0.0;
+    unsigned long long mx = 0;
     for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
         const double ri = rn[i];
         ps[i] = fma(bw, s[i], fma(bk, ps[i], ri));
@@ -556,9 +572,12 @@ __global__ void __launch_bounds__(NT) k_seed_p_deferred(Ctx c) {
             const double rs = ri * rsc;
             rsl[i] = rs;
             acc = fma(rh[i], rs, acc);
+            const unsigned long long b = abs_bits(rs);
+            mx = b > mx ? b : mx;
         }
     }
     if (!sw) return;  // uniform: the reduction is needed only after a switch
+    if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + sc->slots + 2);  // the rescaled r_k slot
     acc = block_sum(acc, sh);
     if (threadIdx.x == 0) c.sh.partials[blockIdx.x] = acc;
     if (take_ticket(c.sh.counters + 3)) {
@@ -726,6 +745,16 @@ __global__ void __launch_bounds__(NT) k_flush_reset(Ctx c, int keep_p) {
     if (so != 0)
         for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT)
             c.v.V[i] = c.v.V[(size_t)so * ld + i];
+    if (c.v.slot_max) {
+        // slot 0 takes the copied slot's maximum (one thread: no other thread
+        // touches slots 0 and so); the others start empty
+        for (size_t l = blockIdx.x * (size_t)NT + threadIdx.x; l < (size_t)cap; l += (size_t)gridDim.x * NT)
+            if (l != 0 && l != (size_t)so) c.v.slot_max[l] = 0;
+        if (blockIdx.x == 0 && threadIdx.x == 0 && so != 0) {
+            c.v.slot_max[0] = c.v.slot_max[so];
+            c.v.slot_max[so] = 0;
+        }
+    }
     if (take_ticket(c.sh.counters + 6)) {
         if (threadIdx.x == 0) {
             sc->slots = 1;
@@ -735,6 +764,17 @@ __global__ void __launch_bounds__(NT) k_flush_reset(Ctx c, int keep_p) {
             c.sh.counters[6] = 0;
         }
     }
+}
+
+// *out = max(*out, bits of max |x|) (out zeroed by the caller)
+__global__ void __launch_bounds__(NT) k_absmax(const double *__restrict__ x, unsigned n, unsigned long long *out) {
+    __shared__ unsigned long long smx[NW];
+    unsigned long long mx = 0;
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
+        const unsigned long long b = abs_bits(x[i]);
+        mx = b > mx ? b : mx;
+    }
+    block_max_to(mx, smx, out);
 }
 
 // X[j][i] = element i of system j of the panel-major Xp: one block per panel
@@ -788,6 +828,12 @@ int hbk_fused_init(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *
     } else {
         if ((e = hbk_copy(n, b, v->V, st))) return e;
         if ((e = hbk_copy(n, b, v->ps, st))) return e;
+        if (v->slot_max) {
+            if ((e = (int)cudaMemsetAsync(v->slot_max, 0, sizeof(unsigned long long) * (size_t)v->slot_cap, st)))
+                return e;
+            k_absmax<<<grid_for(n ? n : 1, 4), NT, 0, st>>>(b, n, v->slot_max);  // slot 0 = b
+            if ((e = (int)cudaGetLastError())) return e;
+        }
         k_init_coef<<<grid_for((unsigned)((size_t)sh->m * v->slot_cap), 1), NT, 0, st>>>(c);
         if ((e = (int)cudaGetLastError())) return e;
     }

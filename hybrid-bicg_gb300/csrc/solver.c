@@ -743,6 +743,7 @@ int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_
             DALLOC(v->Xc, sizeof(double) * (size_t)mm * (size_t)cap);
             DALLOC(v->Pc, sizeof(double) * (size_t)mm * (size_t)cap);
             DALLOC(v->own, sizeof(double) * 2 * (size_t)mm);
+            DALLOC(v->slot_max, sizeof(unsigned long long) * (size_t)cap);
             if (p.flush_mode != HBICG_FLUSH_FP64) {
                 DALLOC(s->tc_ws, hbk_flush_tc_workspace_bytes(mm));
                 DALLOC(s->d_tc_err, sizeof(int));
@@ -803,7 +804,7 @@ void hbicg_solver_destroy(hbicg_solver *s) {
     hbk_vectors *v = &s->v;
     hbk_shifts *sh = &s->sh;
     void *ptrs[] = {v->r_hat, v->rbuf[0], v->rbuf[1], v->s, v->q, v->y, v->X, v->P, v->V, v->ps, v->Xc, v->Pc,
-                    v->own, v->Pmat, v->Xp, s->d_sc, s->d_sigma, sh->a_hist, sh->b_hist, sh->w_hist, sh->ratio, sh->pi,
+                    v->own, v->Pmat, v->Xp, v->slot_max, s->d_sc, s->d_sigma, sh->a_hist, sh->b_hist, sh->w_hist, sh->ratio, sh->pi,
                     sh->eta, sh->zeta, sh->done, sh->conv_k, sh->act_list, sh->lslot, sh->coef, sh->sw_k,
                     sh->rr_hist, sh->sw_seed, sh->act_hist, sh->partials, sh->counters, s->d_b, s->d_res, s->d_dot, s->d_rold,
                     s->d_qcopy, s->tc_ws, s->d_tc_err};
@@ -1042,14 +1043,15 @@ static int do_flush(hbicg_solver *s, int keep_p, int L, int k_last, int *launche
     const double per_shift = keep_p ? 4.0 : 3.0;
     if (s->tc_ws && L >= 1 && L <= hbk_flush_tc_max_slots()) {
         HBK_TRY(hbk_flush_tc_run_live(s->v.V, s->ld, s->A->k.n, L, s->v.Xc, s->v.Pc, s->v.slot_cap, s->v.own, s->m,
-                                      s->v.Xp, s->v.Pmat, keep_p, s->sh.conv_k, k_last, s->tc_ws, s->d_tc_err, st));
+                                      s->v.Xp, s->v.Pmat, keep_p, s->sh.conv_k, k_last, s->v.slot_max, s->tc_ws,
+                                      s->d_tc_err, st));
         int n_live = 0; /* pageable destination: the copy waits for the flush */
         CUDA_TRY(cudaMemcpyAsync(&n_live, hbk_flush_tc_live_count(s->tc_ws, s->m), sizeof(int),
                                  cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         s->flush_bytes += 8.0 * s->A->k.n * ((double)L + per_shift * n_live);
         HBK_TRY(hbk_deferred_reset(&s->v, &s->sh, keep_p, st));
-        *launches += 5;
+        *launches += 4;
     } else {
         s->flush_bytes += 8.0 * s->A->k.n * ((double)L + per_shift * s->m);
         HBK_TRY(hbk_deferred_flush(&s->v, &s->sh, keep_p, st));

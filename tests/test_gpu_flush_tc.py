@@ -35,7 +35,8 @@ def _run_tc(pkg, torch, V, Xc, Pc, own, X, Pm, n, L, m, keep_p, conv_k=None, k_l
     fn = lib.hbk_flush_tc_run_live
     fn.restype = C.c_int
     fn.argtypes = [C.c_void_p, C.c_size_t, C.c_uint, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
-                   C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+                   C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                   C.c_void_p]
     lib.hbk_flush_tc_workspace_bytes.restype = C.c_size_t
     lib.hbk_flush_tc_workspace_bytes.argtypes = [C.c_int]
     ws = torch.zeros(int(lib.hbk_flush_tc_workspace_bytes(m)) // 8 + 1, dtype=torch.float64, device="cuda")
@@ -47,7 +48,7 @@ def _run_tc(pkg, torch, V, Xc, Pc, own, X, Pm, n, L, m, keep_p, conv_k=None, k_l
     cap = Xc.stride(0)
     rc = fn(V.data_ptr(), ld, n, L, Xc.data_ptr(), Pc.data_ptr(), cap, own.data_ptr(), m, tX.data_ptr(),
             tP.data_ptr() if tP is not None else None, keep_p, ck.data_ptr() if ck is not None else None, k_last,
-            ws.data_ptr(), err.data_ptr(), None)
+            None, ws.data_ptr(), err.data_ptr(), None)
     torch.cuda.synchronize()
     assert rc == 0
     assert int(err.item()) == 0
