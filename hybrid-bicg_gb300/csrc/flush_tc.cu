@@ -290,6 +290,20 @@ __global__ void __launch_bounds__(NT) k_slot_max(const double *__restrict__ V, s
     if ((threadIdx.x & 31) == 0 && mx) atomicMax(slot_max + l, mx);
 }
 
+// slot maxima from the partial maxima kept by the kernels that wrote the slots
+// (one warp per slot)
+__global__ void k_fold_slot_max(const unsigned long long *__restrict__ part, int L, unsigned long long *slot_max) {
+    const int l = blockIdx.x;
+    if (l >= L) return;
+    unsigned long long m = part[(size_t)l * HBK_SLOT_SPREAD + threadIdx.x];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    if (threadIdx.x == 0) slot_max[l] = m;
+}
+
 // TMEM lane / A row r of a group -> (x or p, shift within the group)
 __device__ __forceinline__ int row_which(int r) { return (r >> 4) & 1; }
 __device__ __forceinline__ int row_shift(int r) { return ((r >> 5) << 4) | (r & 15); }
@@ -665,7 +679,7 @@ int hbk_flush_tc_max_slots(void) { return TC_K; }
 // x_j (and p_j when keep_p) from the first L basis slots on the tensor cores,
 // for the live shifts only: conv_k[j] == 0 or conv_k[j] > k_last (conv_k
 // NULL: every shift).  slot_max: bits of each slot's max |value| (NULL:
-// computed here).  V: [L][ld] slots; X, Pmat: panel-major (HBK_PANEL),
+// computed here; else [L][HBK_SLOT_SPREAD] partial maxima).  V: [L][ld] slots; X, Pmat: panel-major (HBK_PANEL),
 // m systems, 32-byte aligned; ws: device workspace of
 // hbk_flush_tc_workspace_bytes(m), err: device int.
 int hbk_flush_tc_run_live(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
@@ -684,7 +698,8 @@ int hbk_flush_tc_run_live(const double *V, size_t ld, unsigned n, int L, const d
     cudaError_t e = cudaSuccess;
     k_flush_live<<<1, 32, 0, st>>>(conv_k, m, k_last, live);
     if (slot_max_in) {
-        slot_max = (unsigned long long *)slot_max_in;  // kept by the kernels that wrote the slots
+        static_assert(HBK_SLOT_SPREAD == 32, "one warp folds a slot's partial maxima");
+        k_fold_slot_max<<<L, 32, 0, st>>>(slot_max_in, L, slot_max);
     } else {
         if ((e = cudaMemsetAsync(slot_max, 0, 64 * sizeof(unsigned long long), st))) return (int)e;
         dim3 gs(grid_for(n, 16) < 64 ? grid_for(n, 16) : 64, L);

@@ -107,6 +107,8 @@ typedef struct {
  * time, so it reads and writes one contiguous block per panel instead of m
  * rows that lie n elements apart. */
 #define HBK_PANEL 48
+/* entries per basis slot of the slot-maximum array (spreads the atomics) */
+#define HBK_SLOT_SPREAD 32
 static inline size_t hbk_panel_elems(unsigned n, int m) {
     return ((size_t)n + HBK_PANEL - 1) / HBK_PANEL * HBK_PANEL * (size_t)(m > 0 ? m : 1);
 }
@@ -124,7 +126,8 @@ typedef struct {
     double *own;                /* [m][2]: coefficient of the flushed p_j in x_j and in p_j */
     double *Pmat;               /* flushed p_j, panel-major (allocated on the first flush) */
     double *Xp;                 /* x_j during the solve, panel-major */
-    unsigned long long *slot_max; /* [slot_cap] bits of max |V[l]|, kept by the kernels that write the slots */
+    unsigned long long *slot_max; /* [slot_cap][HBK_SLOT_SPREAD] bits of max |V[l]|: the kernels that write a
+                                     slot fold block b's maximum into entry b % HBK_SLOT_SPREAD */
     int pm;                     /* systems per panel (m) */
     int slot_cap;
     int deferred;
@@ -188,7 +191,8 @@ int hbk_flush_tc_run(const double *V, size_t ld, unsigned n, int L, const double
                      cudaStream_t st);
 /* the same for the live shifts only (conv_k[j] == 0 or conv_k[j] > k_last; the
  * others' rows are left as they are); conv_k: device [m] or NULL (all live);
- * slot_max: device [L] bits of each slot's max |value|, or NULL (computed) */
+ * slot_max: device [L][HBK_SLOT_SPREAD] partial maxima of each slot's |value|
+ * (bits), or NULL (computed) */
 int hbk_flush_tc_run_live(const double *V, size_t ld, unsigned n, int L, const double *Xc, const double *Pc, int cap,
                           const double *own, int m, double *X, double *Pmat, int keep_p, const int *conv_k,
                           int k_last, const unsigned long long *slot_max, void *ws, int *err, cudaStream_t st);

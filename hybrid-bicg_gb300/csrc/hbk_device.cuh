@@ -68,9 +68,10 @@ __device__ __forceinline__ double sum_partials(const double *partials, int npart
 
 __device__ __forceinline__ bool fin(double v) { return isfinite(v) != 0; }
 
-// max of v over the block (every thread calls), then one atomicMax into *out
-// when it is nonzero (bits of non-negative doubles order as unsigned
-// integers); `sh` needs NW values
+// max of v over the block (every thread calls), then one atomicMax into
+// out[blockIdx.x % HBK_SLOT_SPREAD] when it is nonzero (bits of non-negative
+// doubles order as unsigned integers; spreading the blocks over entries keeps
+// the atomics from queueing on one address); `sh` needs NW values
 __device__ __forceinline__ void block_max_to(unsigned long long v, unsigned long long *sh, unsigned long long *out) {
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
@@ -84,7 +85,7 @@ __device__ __forceinline__ void block_max_to(unsigned long long v, unsigned long
     if (threadIdx.x == 0) {
         unsigned long long m = 0;
         for (int i = 0; i < NW; ++i) m = sh[i] > m ? sh[i] : m;
-        if (m) atomicMax(out, m);
+        if (m) atomicMax(out + blockIdx.x % HBK_SLOT_SPREAD, m);
     }
 }
 

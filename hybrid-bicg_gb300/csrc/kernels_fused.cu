@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(NT) k_seed_q(Ctx c) {
         const unsigned long long b = abs_bits(qi);
         mx = b > mx ? b : mx;
     }
-    if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + sc->slots);
+    if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + (size_t)sc->slots * HBK_SLOT_SPREAD);
 }
 
 // K3: y = (A + sigma_s I) q, (q,q) and (q,y)
@@ -441,7 +441,7 @@ __global__ void __launch_bounds__(NT) k_seed_update(Ctx c) {
         const unsigned long long b = abs_bits(r);
         mx = b > mx ? b : mx;
     }
-    if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + sc->slots + 1);  // r_k: a basis slot
+    if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + (size_t)(sc->slots + 1) * HBK_SLOT_SPREAD);  // r_k
     acc = block_sum2(acc, sh);
     if (threadIdx.x == 0) {
         c.sh.partials[blockIdx.x] = acc.x;
@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(NT) k_seed_p_deferred(Ctx c) {
         }
     }
     if (!sw) return;  // uniform: the reduction is needed only after a switch
-    if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + sc->slots + 2);  // the rescaled r_k slot
+    if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + (size_t)(sc->slots + 2) * HBK_SLOT_SPREAD);  // rescaled r_k
     acc = block_sum(acc, sh);
     if (threadIdx.x == 0) c.sh.partials[blockIdx.x] = acc;
     if (take_ticket(c.sh.counters + 3)) {
@@ -748,11 +748,15 @@ __global__ void __launch_bounds__(NT) k_flush_reset(Ctx c, int keep_p) {
     if (c.v.slot_max) {
         // slot 0 takes the copied slot's maximum (one thread: no other thread
         // touches slots 0 and so); the others start empty
-        for (size_t l = blockIdx.x * (size_t)NT + threadIdx.x; l < (size_t)cap; l += (size_t)gridDim.x * NT)
-            if (l != 0 && l != (size_t)so) c.v.slot_max[l] = 0;
-        if (blockIdx.x == 0 && threadIdx.x == 0 && so != 0) {
-            c.v.slot_max[0] = c.v.slot_max[so];
-            c.v.slot_max[so] = 0;
+        const size_t tot_e = (size_t)cap * HBK_SLOT_SPREAD;
+        for (size_t e = blockIdx.x * (size_t)NT + threadIdx.x; e < tot_e; e += (size_t)gridDim.x * NT) {
+            const size_t l = e / HBK_SLOT_SPREAD;
+            if (l != 0 && l != (size_t)so) c.v.slot_max[e] = 0;
+        }
+        if (blockIdx.x == 0 && threadIdx.x < HBK_SLOT_SPREAD && so != 0) {
+            const size_t e0 = threadIdx.x, es = (size_t)so * HBK_SLOT_SPREAD + threadIdx.x;
+            c.v.slot_max[e0] = c.v.slot_max[es];
+            c.v.slot_max[es] = 0;
         }
     }
     if (take_ticket(c.sh.counters + 6)) {
@@ -766,7 +770,7 @@ __global__ void __launch_bounds__(NT) k_flush_reset(Ctx c, int keep_p) {
     }
 }
 
-// *out = max(*out, bits of max |x|) (out zeroed by the caller)
+// out[0 .. HBK_SLOT_SPREAD) take the bits of max |x| (zeroed by the caller)
 __global__ void __launch_bounds__(NT) k_absmax(const double *__restrict__ x, unsigned n, unsigned long long *out) {
     __shared__ unsigned long long smx[NW];
     unsigned long long mx = 0;
@@ -829,7 +833,8 @@ int hbk_fused_init(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *
         if ((e = hbk_copy(n, b, v->V, st))) return e;
         if ((e = hbk_copy(n, b, v->ps, st))) return e;
         if (v->slot_max) {
-            if ((e = (int)cudaMemsetAsync(v->slot_max, 0, sizeof(unsigned long long) * (size_t)v->slot_cap, st)))
+            if ((e = (int)cudaMemsetAsync(v->slot_max, 0,
+                                          sizeof(unsigned long long) * (size_t)v->slot_cap * HBK_SLOT_SPREAD, st)))
                 return e;
             k_absmax<<<grid_for(n ? n : 1, 4), NT, 0, st>>>(b, n, v->slot_max);  // slot 0 = b
             if ((e = (int)cudaGetLastError())) return e;

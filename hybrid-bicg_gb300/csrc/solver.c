@@ -743,7 +743,7 @@ int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_
             DALLOC(v->Xc, sizeof(double) * (size_t)mm * (size_t)cap);
             DALLOC(v->Pc, sizeof(double) * (size_t)mm * (size_t)cap);
             DALLOC(v->own, sizeof(double) * 2 * (size_t)mm);
-            DALLOC(v->slot_max, sizeof(unsigned long long) * (size_t)cap);
+            DALLOC(v->slot_max, sizeof(unsigned long long) * (size_t)cap * HBK_SLOT_SPREAD);
             if (p.flush_mode != HBICG_FLUSH_FP64) {
                 DALLOC(s->tc_ws, hbk_flush_tc_workspace_bytes(mm));
                 DALLOC(s->d_tc_err, sizeof(int));
@@ -1051,7 +1051,7 @@ static int do_flush(hbicg_solver *s, int keep_p, int L, int k_last, int *launche
         CUDA_TRY(cudaStreamSynchronize(st));
         s->flush_bytes += 8.0 * s->A->k.n * ((double)L + per_shift * n_live);
         HBK_TRY(hbk_deferred_reset(&s->v, &s->sh, keep_p, st));
-        *launches += 4;
+        *launches += 5; /* live list, slot maxima, coefficient digits, flush, reset */
     } else {
         s->flush_bytes += 8.0 * s->A->k.n * ((double)L + per_shift * s->m);
         HBK_TRY(hbk_deferred_flush(&s->v, &s->sh, keep_p, st));
