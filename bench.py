@@ -160,6 +160,14 @@ class Clocks:
 
 
 # ------------------------------------------------------------- workload
+MATRIX_KIND = {
+    "c1": "3-D 7-point convection-diffusion, ",
+    "c2": "3-D 7-point convection-diffusion, ",
+    "c3": "power-law rows (Zipf 2.0, mean 16, up to 4000; 70 % random and 30 % near-diagonal columns, "
+          "diagonally dominant), ",
+}
+
+
 def workload(name: str, scale):
     pkg = graft.load_package()
     return pkg, pkg.workloads.family(name, scale)
@@ -360,9 +368,10 @@ def run_ours(args, dist: Dist):
         "metric": METRIC, "value": step_max, "unit": "s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_max * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator; the reference ships no matrices)",
-        "config": {"workload": f"{args.workload}: {f.a.n} rows, {f.a.nnz} nonzeros, 3-D 7-point convection-"
-                   f"diffusion, {m} shifts in [{f.sigma.min():g}, {f.sigma.max():g}], tol {f.tol:g}, seed {f.seed}",
+        "config": {"workload": f"{args.workload}: {f.a.n} rows, {f.a.nnz} nonzeros, {MATRIX_KIND.get(args.workload, '')}"
+                   f"{m} shifts in [{f.sigma.min():g}, {f.sigma.max():g}], tol {f.tol:g}, seed {f.seed}",
                    "mode": args.mode, "shift_mode": res.shift_mode, "refine": not args.no_refine,
+                   "spmv_format": A.format,
                    "parallelism": f"replicas x{dist.world}",
                    "l2": "working set >> 129 MB L2 (no flush needed)"},
         "iterations": res.k, "switches": res.switches, "refined_shifts": res.refined,

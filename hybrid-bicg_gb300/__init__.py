@@ -208,6 +208,10 @@ def params(tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="a
     return p
 
 
+# SpMV storage forms (hbicg_spmv_format)
+_FORMATS = {0: "tile", 1: "sell", 2: "hyb"}
+
+
 @dataclass
 class SolveResult:
     k: int
@@ -375,7 +379,7 @@ def batch_solve(families, workers: int = 8, autotune: bool = False, autotune_cac
     for i in range(len(families)):
         fa = arr[i]
         out.append(FamilyResult(status=fa.status, k=fa.k, x=keep[i][5], switches=fa.n_switches,
-                                final_seed=fa.final_seed, spmv_format="sell" if fa.spmv_format == 1 else "tile",
+                                final_seed=fa.final_seed, spmv_format=_FORMATS.get(fa.spmv_format, "tile"),
                                 solve_ms=fa.solve_ms, wall_ms=fa.wall_ms, max_true_residual=fa.max_true_residual,
                                 true_residual=keep[i][6][:len(keep[i][4])].copy() if want_res else None))
     return out, wall.value / 1e3
@@ -463,17 +467,17 @@ class Matrix:
 
     @property
     def format(self) -> str:
-        return "sell" if lib().hbicg_matrix_format(self.h) == 1 else "tile"
+        return _FORMATS.get(lib().hbicg_matrix_format(self.h), "tile")
 
     def set_format(self, fmt: str) -> None:
-        _check(lib().hbicg_matrix_set_format(self.h, {"tile": 0, "sell": 1}[fmt]), "hbicg_matrix_set_format")
+        _check(lib().hbicg_matrix_set_format(self.h, {v: k for k, v in _FORMATS.items()}[fmt]), "hbicg_matrix_set_format")
 
     def autotune(self, cache: str | None = None) -> dict:
         """Time both SpMV forms (or read the cached choice) and keep the faster."""
         ch, t1, t2 = C.c_int(), C.c_double(), C.c_double()
         _check(lib().hbicg_matrix_autotune(self.h, str(cache).encode() if cache else None, C.byref(ch), C.byref(t1),
                                            C.byref(t2)), "hbicg_matrix_autotune")
-        return {"format": "sell" if ch.value == 1 else "tile", "tile_ms": t1.value, "sell_ms": t2.value}
+        return {"format": _FORMATS.get(ch.value, "tile"), "tile_ms": t1.value, "sell_ms": t2.value}
 
     def csr(self):
         """(ptr, col, val) copied to numpy."""

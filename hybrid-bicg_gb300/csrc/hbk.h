@@ -38,6 +38,9 @@ extern "C" {
 #define HBK_FMT_TILE 0       /* CSR, row blocks staged in shared memory */
 #define HBK_FMT_SELL 1       /* SELL-32: slices of 32 rows, column-major within a slice */
 #define HBK_SELL_MAX_LEN 64  /* longest row the SELL format takes */
+#define HBK_FMT_HYB 2        /* short rows in SELL-32 slices (length-sorted inside windows), long rows one warp each */
+#define HBK_HYB_SHORT 32     /* longest row of a HYB slice */
+#define HBK_HYB_WINDOW 256   /* rows are sorted by length only inside windows of this many consecutive rows */
 
 typedef struct {
     unsigned n, nnz;
@@ -50,7 +53,11 @@ typedef struct {
     int fmt;                   /* HBK_FMT_* */
     const double *sval;        /* SELL: values, slice s at sptr[s], entry e of lane l at +e*32+l */
     const unsigned *scol;      /* SELL: column indices (padding: the row itself, value 0) */
-    const unsigned long long *sptr; /* SELL: n/32 rounded up + 1 slice offsets */
+    const unsigned long long *sptr; /* SELL: n/32 rounded up + 1 slice offsets; HYB: nslice + 1 */
+    const unsigned *srow;      /* HYB: row of slice s, lane l at 32 s + l (>= n: an empty lane) */
+    unsigned nslice;           /* HYB: slices of short rows */
+    const unsigned *wrow;      /* HYB: rows longer than HBK_HYB_SHORT, longest first, one warp each */
+    unsigned nwrow;
 } hbk_matrix;
 
 /* Device-resident scalars of one solve. */
@@ -154,6 +161,9 @@ int hbk_spmv_grid(unsigned nblk);
 /* SELL-32 build on the device: widths of the ceil(n/32) slices into w ... */
 int hbk_sell_widths(unsigned n, const unsigned *ptr, unsigned *w, cudaStream_t st);
 /* ... then, with sptr = exclusive prefix sum of 32*w (host), fill the arrays */
+/* HYB slices: slice s, lane l holds row srow[32 s + l] (entry e at sptr[s] + 32 e + l) */
+int hbk_hyb_fill(unsigned nslice, const unsigned *srow, unsigned n, const unsigned *ptr, const unsigned *col,
+                 const double *val, const unsigned long long *sptr, double *sval, unsigned *scol, cudaStream_t st);
 int hbk_sell_fill(unsigned n, const unsigned *ptr, const unsigned *col, const double *val,
                   const unsigned long long *sptr, double *sval, unsigned *scol, cudaStream_t st);
 

@@ -186,12 +186,53 @@ __device__ __forceinline__ void spmv_rows_tile(const hbk_matrix &A, const double
     }
 }
 
+// HYB path: persistent warps over work items; the first nwrow items are the
+// long rows (longest first), one warp each: lanes take every 32nd entry in
+// stored order and the 32 partial sums meet in a fixed shuffle tree.  The
+// rest are SELL-32 slices of short rows, one warp each, whose 32 rows were
+// sorted by length inside a window of HBK_HYB_WINDOW rows, so the lanes of a
+// warp have similar row lengths (an FP64 instruction costs the same whatever
+// its active lanes); each short row is summed in stored order with FMAs from
+// 0, as in the other paths.
+template <class Epi>
+__device__ __forceinline__ void spmv_rows_hyb(const hbk_matrix &A, const double *__restrict__ x, Epi &epi) {
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned nw = (gridDim.x * NT) >> 5;
+    const unsigned items = A.nwrow + A.nslice;
+    for (unsigned it = (blockIdx.x * NT + threadIdx.x) >> 5; it < items; it += nw) {
+        if (it < A.nwrow) {
+            const unsigned r = __ldg(A.wrow + it);
+            const unsigned e1 = __ldg(A.ptr + r + 1);
+            double acc = 0.0;
+            for (unsigned e = __ldg(A.ptr + r) + lane; e < e1; e += 32)
+                acc = fma(__ldg(A.val + e), __ldg(x + __ldg(A.col + e)), acc);
+            acc = warp_sum(acc);
+            if (lane == 0) epi(r, acc);
+        } else {
+            const unsigned s = it - A.nwrow;
+            const unsigned long long base = __ldg(A.sptr + s);
+            const unsigned w = (unsigned)((__ldg(A.sptr + s + 1) - base) >> 5);
+            const unsigned r = __ldg(A.srow + 32 * (size_t)s + lane);
+            const unsigned len = r < A.n ? __ldg(A.ptr + r + 1) - __ldg(A.ptr + r) : 0;
+            const double *__restrict__ vv = A.sval + base + lane;
+            const unsigned *__restrict__ cc = A.scol + base + lane;
+            double acc = 0.0;
+#pragma unroll 4
+            for (unsigned e = 0; e < w; ++e)
+                if (e < len) acc = fma(__ldg(vv + 32 * (size_t)e), __ldg(x + __ldg(cc + 32 * (size_t)e)), acc);
+            if (r < A.n) epi(r, acc);
+        }
+    }
+}
+
 // Format chosen at compile time so the SELL kernels carry no shared-memory
 // tile (full occupancy); launchers pick the instantiation from A.fmt.
 template <int FMT, class Epi>
 __device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__restrict__ x, Epi &epi) {
     if constexpr (FMT == HBK_FMT_SELL) {
         spmv_rows_sell(A, x, epi);
+    } else if constexpr (FMT == HBK_FMT_HYB) {
+        spmv_rows_hyb(A, x, epi);
     } else {
         __shared__ SpmvSmem sm;
         spmv_rows_tile(A, x, epi, sm);
@@ -202,6 +243,7 @@ __device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__r
 #define HBK_LAUNCH_FMT(A, kern, grid, block, stream, ...)                                   \
     do {                                                                                    \
         if ((A).fmt == HBK_FMT_SELL) kern<HBK_FMT_SELL><<<grid, block, 0, stream>>>(__VA_ARGS__); \
+        else if ((A).fmt == HBK_FMT_HYB) kern<HBK_FMT_HYB><<<grid, block, 0, stream>>>(__VA_ARGS__); \
         else kern<HBK_FMT_TILE><<<grid, block, 0, stream>>>(__VA_ARGS__);                  \
     } while (0)
 

@@ -104,6 +104,29 @@ __global__ void __launch_bounds__(NT) k_true_res(hbk_matrix A, const double *__r
 
 // SELL-32 build: slice widths, then one thread per row writes its entries
 // (column-major within the slice) and its padding (value 0, column = row).
+// HYB slices from CSR: lane l of slice s copies row srow[32 s + l]; padding
+// entries get value 0 and a column index of 0 (an empty lane's entries too)
+__global__ void __launch_bounds__(NT) k_hyb_fill(unsigned nslice, const unsigned *__restrict__ srow, unsigned n,
+                                                 const unsigned *__restrict__ ptr, const unsigned *__restrict__ col,
+                                                 const double *__restrict__ val,
+                                                 const unsigned long long *__restrict__ sptr,
+                                                 double *__restrict__ sval, unsigned *__restrict__ scol) {
+    const size_t tot = (size_t)nslice * 32;
+    for (size_t t = blockIdx.x * (size_t)NT + threadIdx.x; t < tot; t += (size_t)gridDim.x * NT) {
+        const size_t s = t >> 5;
+        const unsigned lane = (unsigned)(t & 31);
+        const unsigned long long base = sptr[s];
+        const unsigned w = (unsigned)((sptr[s + 1] - base) >> 5);
+        const unsigned r = srow[t];
+        const unsigned a = r < n ? ptr[r] : 0, len = r < n ? ptr[r + 1] - ptr[r] : 0;
+        for (unsigned e = 0; e < w; ++e) {
+            const size_t o = base + 32 * (size_t)e + lane;
+            sval[o] = e < len ? val[a + e] : 0.0;
+            scol[o] = e < len ? col[a + e] : 0u;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(NT) k_sell_widths(unsigned n, const unsigned *__restrict__ ptr,
                                                     unsigned *__restrict__ w) {
     const unsigned ns = (n + 31) / 32;
@@ -137,6 +160,13 @@ __global__ void __launch_bounds__(NT) k_sell_fill(unsigned n, const unsigned *__
 }  // namespace
 
 extern "C" {
+
+int hbk_hyb_fill(unsigned nslice, const unsigned *srow, unsigned n, const unsigned *ptr, const unsigned *col,
+                 const double *val, const unsigned long long *sptr, double *sval, unsigned *scol, cudaStream_t st) {
+    if (!nslice) return 0;
+    k_hyb_fill<<<grid_for(nslice * 32u, 1), NT, 0, st>>>(nslice, srow, n, ptr, col, val, sptr, sval, scol);
+    return (int)cudaGetLastError();
+}
 
 int hbk_sell_widths(unsigned n, const unsigned *ptr, unsigned *w, cudaStream_t st) {
     if (!n) return 0;

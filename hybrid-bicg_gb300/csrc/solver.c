@@ -161,7 +161,132 @@ struct hbicg_matrix {
     double *d_sval;
     unsigned *d_scol;
     unsigned long long *d_sptr;
+    /* HYB form (hbk.h HBK_FMT_HYB) */
+    double *d_hval;
+    unsigned *d_hcol, *d_srow, *d_wrow;
+    unsigned long long *d_hsptr;
+    unsigned nslice, nwrow;
 };
+
+static int cmp_u64(const void *a, const void *b) {
+    const unsigned long long x = *(const unsigned long long *)a, y = *(const unsigned long long *)b;
+    return x < y ? -1 : x > y;
+}
+
+/* HYB: rows of at most HBK_HYB_SHORT entries in SELL-32 slices, sorted by
+ * length (longest first, stable) inside windows of HBK_HYB_WINDOW consecutive
+ * rows, so that the 32 rows of a slice have similar lengths and the rows a
+ * warp writes stay inside one window; each window's list is padded to whole
+ * slices with empty lanes.  Longer rows go to a list, longest first, one warp
+ * each.  For power-law row lengths (most rows short, a few thousands long),
+ * where a thread per row leaves most lanes of a warp idle. */
+static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
+    cudaStream_t st = A->ctx->stream;
+    if (!n || A->d_hval) return HBICG_OK;
+    size_t cap = 0, nw = 0;
+    for (unsigned w0 = 0; w0 < n; w0 += HBK_HYB_WINDOW) {
+        const unsigned w1 = n - w0 < HBK_HYB_WINDOW ? n : w0 + HBK_HYB_WINDOW;
+        unsigned cnt = 0;
+        for (unsigned r = w0; r < w1; ++r) {
+            if (h_ptr[r + 1] - h_ptr[r] <= HBK_HYB_SHORT)
+                cnt++;
+            else
+                nw++;
+        }
+        cap += (cnt + 31) / 32 * 32;
+    }
+    const size_t ns = cap / 32;
+    unsigned *srow = malloc(sizeof(unsigned) * (cap + 1));
+    unsigned long long *wkey = malloc(sizeof(unsigned long long) * (nw + 1));
+    unsigned *wrow = malloc(sizeof(unsigned) * (nw + 1));
+    unsigned long long *sp = malloc(sizeof(unsigned long long) * (ns + 1));
+    int rc = HBICG_OK;
+    if (!srow || !wkey || !wrow || !sp) {
+        rc = HBICG_E_NOMEM;
+        goto done;
+    }
+    {
+        size_t o = 0, wi = 0;
+        for (unsigned w0 = 0; w0 < n; w0 += HBK_HYB_WINDOW) {
+            const unsigned w1 = n - w0 < HBK_HYB_WINDOW ? n : w0 + HBK_HYB_WINDOW;
+            unsigned cnt[HBK_HYB_SHORT + 1] = {0}, pos[HBK_HYB_SHORT + 1];
+            for (unsigned r = w0; r < w1; ++r) {
+                const unsigned len = h_ptr[r + 1] - h_ptr[r];
+                if (len <= HBK_HYB_SHORT)
+                    cnt[len]++;
+                else /* longest first, then by row: sort the complement of the length */
+                    wkey[wi++] = ((unsigned long long)(0xFFFFFFFFu - len) << 32) | r;
+            }
+            unsigned acc = 0;
+            for (int L = HBK_HYB_SHORT; L >= 0; --L) {
+                pos[L] = acc;
+                acc += cnt[L];
+            }
+            for (unsigned r = w0; r < w1; ++r) {
+                const unsigned len = h_ptr[r + 1] - h_ptr[r];
+                if (len <= HBK_HYB_SHORT) srow[o + pos[len]++] = r;
+            }
+            o += acc;
+            while (o % 32) srow[o++] = 0xFFFFFFFFu; /* empty lane */
+        }
+        qsort(wkey, nw, sizeof *wkey, cmp_u64);
+        for (size_t i = 0; i < nw; ++i) wrow[i] = (unsigned)(wkey[i] & 0xFFFFFFFFu);
+        sp[0] = 0;
+        for (size_t s = 0; s < ns; ++s) {
+            unsigned w = 0;
+            for (int l = 0; l < 32; ++l) {
+                const unsigned r = srow[32 * s + l];
+                if (r < n && h_ptr[r + 1] - h_ptr[r] > w) w = h_ptr[r + 1] - h_ptr[r];
+            }
+            sp[s + 1] = sp[s] + 32ull * w;
+        }
+    }
+#define HTRY(call)                                                                               \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess) {                                                                 \
+            set_msg("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));          \
+            rc = HBICG_E_CUDA;                                                                   \
+            goto done;                                                                           \
+        }                                                                                        \
+    } while (0)
+    HTRY(cudaMalloc((void **)&A->d_hsptr, sizeof(unsigned long long) * (ns + 1)));
+    HTRY(cudaMalloc((void **)&A->d_hval, sizeof(double) * (sp[ns] + 1)));
+    HTRY(cudaMalloc((void **)&A->d_hcol, sizeof(unsigned) * (sp[ns] + 1)));
+    HTRY(cudaMalloc((void **)&A->d_srow, sizeof(unsigned) * (cap + 1)));
+    HTRY(cudaMalloc((void **)&A->d_wrow, sizeof(unsigned) * (nw + 1)));
+    HTRY(cudaMemcpyAsync(A->d_hsptr, sp, sizeof(unsigned long long) * (ns + 1), cudaMemcpyHostToDevice, st));
+    if (cap) HTRY(cudaMemcpyAsync(A->d_srow, srow, sizeof(unsigned) * cap, cudaMemcpyHostToDevice, st));
+    if (nw) HTRY(cudaMemcpyAsync(A->d_wrow, wrow, sizeof(unsigned) * nw, cudaMemcpyHostToDevice, st));
+    {
+        const int e = hbk_hyb_fill((unsigned)ns, A->d_srow, n, A->d_ptr, A->d_col, A->d_val, A->d_hsptr, A->d_hval,
+                                   A->d_hcol, st);
+        if (e) HTRY((cudaError_t)e);
+    }
+    HTRY(cudaStreamSynchronize(st));
+#undef HTRY
+    A->nslice = (unsigned)ns;
+    A->nwrow = (unsigned)nw;
+done:
+    free(srow);
+    free(wkey);
+    free(wrow);
+    free(sp);
+    return rc;
+}
+
+/* point the kernel view at the HYB arrays */
+static void use_hyb(hbicg_matrix *A) {
+    A->k.fmt = HBK_FMT_HYB;
+    A->k.sval = A->d_hval;
+    A->k.scol = A->d_hcol;
+    A->k.sptr = A->d_hsptr;
+    A->k.srow = A->d_srow;
+    A->k.wrow = A->d_wrow;
+    A->k.nslice = A->nslice;
+    A->k.nwrow = A->nwrow;
+    A->k.grid = hbk_spmv_grid((A->k.n + HBK_THREADS - 1) / HBK_THREADS);
+}
 
 /* SELL-32 when every row fits in HBK_SELL_MAX_LEN and padding stays under a
  * third of the nonzeros (rows are short and regular, as in stencils); the CSR
@@ -272,6 +397,12 @@ int hbicg_matrix_create(hbicg_context *ctx, unsigned n, unsigned nnz, const unsi
             CUDA_TRY(cudaMemcpy(hp, ptr, sizeof(unsigned) * ((size_t)n + 1), cudaMemcpyDeviceToHost));
         }
         int rc = build_sell(A, hp, n, nnz, 0);
+        /* irregular rows: the HYB form unless the tile form was asked for */
+        const char *env = getenv("HBICG_SPMV_FORMAT");
+        if (!rc && A->k.fmt != HBK_FMT_SELL && n && !(env && !strcmp(env, "tile"))) {
+            rc = build_hyb(A, hp, n);
+            if (!rc) use_hyb(A);
+        }
         if (where == HBICG_DEVICE) free(hp);
         if (rc) return rc;
         if (A->k.fmt == HBK_FMT_SELL) A->k.grid = hbk_spmv_grid((n + HBK_THREADS - 1) / HBK_THREADS);
@@ -408,6 +539,11 @@ void hbicg_matrix_destroy(hbicg_matrix *A) {
     if (A->d_sval) cudaFree(A->d_sval);
     if (A->d_scol) cudaFree(A->d_scol);
     if (A->d_sptr) cudaFree(A->d_sptr);
+    cudaFree(A->d_hval);
+    cudaFree(A->d_hcol);
+    cudaFree(A->d_hsptr);
+    cudaFree(A->d_srow);
+    cudaFree(A->d_wrow);
     hbicg_context *ctx = A->ctx;
     free(A);
     ctx_release(ctx);
@@ -453,7 +589,9 @@ int hbicg_matrix_time_spmv(hbicg_matrix *A, const double *x, double *y, double s
     return HBICG_OK;
 }
 
-int hbicg_matrix_format(const hbicg_matrix *A) { return A->k.fmt == HBK_FMT_SELL ? HBICG_SPMV_SELL : HBICG_SPMV_TILE; }
+int hbicg_matrix_format(const hbicg_matrix *A) {
+    return A->k.fmt == HBK_FMT_SELL ? HBICG_SPMV_SELL : A->k.fmt == HBK_FMT_HYB ? HBICG_SPMV_HYB : HBICG_SPMV_TILE;
+}
 
 static unsigned *host_ptr_copy(hbicg_matrix *A) {
     const size_t n = A->k.n;
@@ -467,10 +605,21 @@ static unsigned *host_ptr_copy(hbicg_matrix *A) {
 }
 
 int hbicg_matrix_set_format(hbicg_matrix *A, int fmt) {
-    if (!A || (fmt != HBICG_SPMV_TILE && fmt != HBICG_SPMV_SELL)) return HBICG_E_ARG;
+    if (!A || (fmt != HBICG_SPMV_TILE && fmt != HBICG_SPMV_SELL && fmt != HBICG_SPMV_HYB)) return HBICG_E_ARG;
     if (fmt == HBICG_SPMV_TILE) {
         A->k.fmt = HBK_FMT_TILE;
         A->k.grid = hbk_spmv_grid(A->k.nblk);
+        return HBICG_OK;
+    }
+    if (fmt == HBICG_SPMV_HYB) {
+        if (!A->d_hval && A->k.n) {
+            unsigned *hp = host_ptr_copy(A);
+            if (!hp) return HBICG_E_NOMEM;
+            int rc = build_hyb(A, hp, A->k.n);
+            free(hp);
+            if (rc) return rc;
+        }
+        use_hyb(A);
         return HBICG_OK;
     }
     if (!A->d_sval) {
@@ -516,7 +665,7 @@ static void pattern_signature(const unsigned *hp, unsigned n, char *key, size_t 
 
 static pthread_mutex_t g_tune_lock = PTHREAD_MUTEX_INITIALIZER;
 
-/* cached choice for key: 0 tile, 1 sell, -1 none */
+/* cached choice for key: 0 tile, 1 sell, 2 hyb, -1 none */
 static int tune_lookup(const char *path, const char *key, double *tile_ms, double *sell_ms) {
     FILE *f = fopen(path, "r");
     if (!f) return -1;
@@ -526,7 +675,7 @@ static int tune_lookup(const char *path, const char *key, double *tile_ms, doubl
         double t, sl;
         if (line[0] == '#') continue;
         if (sscanf(line, "%255s %15s %lf %lf", k, fmt, &t, &sl) == 4 && !strcmp(k, key)) {
-            found = !strcmp(fmt, "sell") ? 1 : 0;
+            found = !strcmp(fmt, "sell") ? 1 : !strcmp(fmt, "hyb") ? 2 : 0;
             *tile_ms = t;
             *sell_ms = sl;
         }
@@ -558,15 +707,27 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
         CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, A->ctx->stream));
         int rc = hbicg_matrix_set_format(A, HBICG_SPMV_TILE);
         if (!rc) rc = hbicg_matrix_time_spmv(A, x, y, 0.0, 10, &t_tile);
+        double t_s = -1.0, t_h = -1.0;
         if (!rc && hbicg_matrix_set_format(A, HBICG_SPMV_SELL) == HBICG_OK)
-            rc = hbicg_matrix_time_spmv(A, x, y, 0.0, 10, &t_sell);
+            rc = hbicg_matrix_time_spmv(A, x, y, 0.0, 10, &t_s);
+        if (!rc && hbicg_matrix_set_format(A, HBICG_SPMV_HYB) == HBICG_OK)
+            rc = hbicg_matrix_time_spmv(A, x, y, 0.0, 10, &t_h);
         cudaFree(x);
         cudaFree(y);
         if (rc) return rc;
-        pick = (t_sell >= 0.0 && t_sell < t_tile) ? 1 : 0;
+        pick = 0;
+        double best = t_tile;
+        if (t_s >= 0.0 && t_s < best) {
+            pick = 1;
+            best = t_s;
+        }
+        if (t_h >= 0.0 && t_h < best) pick = 2;
+        /* the packed form's time: SELL-32 where it exists and was not beaten by HYB */
+        t_sell = pick == 2 || t_s < 0.0 ? t_h : t_s;
         if (cache_path && *cache_path) {
             char line[512];
-            const int len = snprintf(line, sizeof line, "%s %s %.6f %.6f\n", key, pick ? "sell" : "tile", t_tile, t_sell);
+            static const char *names[3] = {"tile", "sell", "hyb"};
+            const int len = snprintf(line, sizeof line, "%s %s %.6f %.6f\n", key, names[pick], t_tile, t_sell);
             pthread_mutex_lock(&g_tune_lock);
             const int fd = open(cache_path, O_WRONLY | O_CREAT | O_APPEND, 0644);
             if (fd >= 0) {
@@ -583,9 +744,24 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
             pthread_mutex_unlock(&g_tune_lock);
         }
     }
-    int rc = hbicg_matrix_set_format(A, pick ? HBICG_SPMV_SELL : HBICG_SPMV_TILE);
+    int rc = hbicg_matrix_set_format(A, pick == 1 ? HBICG_SPMV_SELL : pick == 2 ? HBICG_SPMV_HYB : HBICG_SPMV_TILE);
     if (rc) return rc;
-    if (!pick && A->d_sval) { /* the SELL copy is not used: give its memory back */
+    if (pick != 2 && A->d_hval) { /* the HYB copy is not used: give its memory back */
+        cudaStreamSynchronize(A->ctx->stream);
+        cudaFree(A->d_hval);
+        cudaFree(A->d_hcol);
+        cudaFree(A->d_hsptr);
+        cudaFree(A->d_srow);
+        cudaFree(A->d_wrow);
+        A->d_hval = NULL;
+        A->d_hcol = NULL;
+        A->d_hsptr = NULL;
+        A->d_srow = NULL;
+        A->d_wrow = NULL;
+        A->k.srow = NULL;
+        A->k.wrow = NULL;
+    }
+    if (pick != 1 && A->d_sval) { /* the SELL copy is not used: give its memory back */
         cudaStreamSynchronize(A->ctx->stream);
         cudaFree(A->d_sval);
         cudaFree(A->d_scol);
@@ -597,7 +773,7 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
         A->k.scol = NULL;
         A->k.sptr = NULL;
     }
-    if (chosen) *chosen = pick ? HBICG_SPMV_SELL : HBICG_SPMV_TILE;
+    if (chosen) *chosen = pick == 1 ? HBICG_SPMV_SELL : pick == 2 ? HBICG_SPMV_HYB : HBICG_SPMV_TILE;
     if (tile_ms) *tile_ms = t_tile;
     if (sell_ms) *sell_ms = t_sell;
     return HBICG_OK;

@@ -125,7 +125,7 @@ int hbicg_matrix_time_spmv(hbicg_matrix *A, const double *x, double *y, double s
 
 /* SpMV form of a matrix: CSR row blocks, or SELL-32 (slices of 32 rows padded
  * to their longest row; rows of at most 64 entries). */
-typedef enum { HBICG_SPMV_TILE = 0, HBICG_SPMV_SELL = 1 } hbicg_spmv_format;
+typedef enum { HBICG_SPMV_TILE = 0, HBICG_SPMV_SELL = 1, HBICG_SPMV_HYB = 2 } hbicg_spmv_format;
 int hbicg_matrix_format(const hbicg_matrix *A);
 /* Switch the SpMV form (builds the SELL-32 copy if needed; HBICG_E_ARG when a
  * row is too long for it).  Call before creating solvers on A. */
