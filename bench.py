@@ -567,6 +567,39 @@ def run_flush_kernel(args):
             "achieved_gbs": byt / (ms * 1e-3) / 1e9, "frac": byt / (ms * 1e-3) / 1e9 / hbm, "peak_kind": kind}
 
 
+def run_spmv_kernel(args):
+    """y = (A + sigma I) x alone for a workload's matrix in each SpMV form the
+    matrix has (tile always; SELL-32 where every row fits; HYB), device
+    buffers, CUDA events over `--steps` launches after `--warmup`; algorithmic
+    bytes 12 nnz + 4 (n + 1) + 16 n.  The default form comes first."""
+    import torch
+
+    pkg, f = workload(args.workload, args.scale)
+    n, nnz = f.a.n, f.a.nnz
+    ctx = pkg.Context()
+    A = pkg.Matrix(ctx, torch.from_numpy(f.a.ptr.astype(np.int32)).cuda(),
+                   torch.from_numpy(f.a.col.astype(np.int32)).cuda(), torch.from_numpy(f.a.val).cuda())
+    x = torch.randn(n, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(0))
+    y = torch.empty_like(x)
+    hbm, kind = peaks()
+    byt = spmv_bytes(n, nnz)
+    default = A.format
+    out = {"kernel": "k_spmv", "workload": args.workload, "n": n, "nnz": nnz, "default_format": default,
+           "bytes_per_launch": byt, "peak_kind": kind, "forms": {}}
+    for fmt in [default] + [g for g in ("tile", "sell", "hyb") if g != default]:
+        try:
+            A.set_format(fmt)
+        except RuntimeError:
+            continue  # no such form for this matrix (SELL-32 with rows over 64 entries)
+        ms = A.time_spmv(x, y, 0.1, iters=max(args.steps, 1))
+        out["forms"][fmt] = {"ms_per_launch": ms, "achieved_gbs": byt / (ms * 1e-3) / 1e9,
+                             "frac": byt / (ms * 1e-3) / 1e9 / hbm}
+    A.set_format(default)
+    A.close()
+    ctx.close()
+    return out
+
+
 def run_coo2csr_kernel(args):
     """COO -> CSR of a workload's matrix (its triplets in a random order) on
     the GPU (hbk_coo_to_csr: stable radix sort by row, row pointers, gather;
@@ -683,13 +716,14 @@ def main(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-refine", action="store_true", help="keep the reference's x (no true-residual correction)")
-    ap.add_argument("--kernel", default=None, choices=["flush", "coo2csr", "mmread"],
+    ap.add_argument("--kernel", default=None, choices=["flush", "spmv", "coo2csr", "mmread"],
                     help="time one kernel alone on random data instead of the solve")
     ap.add_argument("--n", type=int, default=2097152, help="elements for --kernel")
     ap.add_argument("--workers", type=int, default=8, help="host workers for --workload c4")
     args = ap.parse_args(argv)
     if args.kernel:
-        run = {"flush": run_flush_kernel, "coo2csr": run_coo2csr_kernel, "mmread": run_mmread}[args.kernel]
+        run = {"flush": run_flush_kernel, "spmv": run_spmv_kernel, "coo2csr": run_coo2csr_kernel,
+               "mmread": run_mmread}[args.kernel]
         print(json.dumps(run(args)), flush=True)
         return
     if args.impl == "ours" and args.warmup < 3:
