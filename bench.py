@@ -222,6 +222,20 @@ def load_profile(name: str, f):
     return d
 
 
+def _cpu_baseline_child(name, scale, profile):
+    return cpu_baseline(graft.load_package().workloads.family(name, scale), profile)
+
+
+def cpu_baseline_fresh(name: str, scale, profile):
+    """cpu_baseline in a spawned process: the GPU arm's process holds torch
+    and its OpenMP thread pool, which the oracle's OpenMP team would compete
+    with; a fresh interpreter times it as the reference arm does."""
+    import multiprocessing as mp
+
+    with mp.get_context("spawn").Pool(1) as pool:
+        return pool.apply(_cpu_baseline_child, (name, scale, profile))
+
+
 def cpu_baseline(f, profile=None, threads: int | None = None):
     """The reference's algorithm (its C restatement, oracle/, with the
     reference's OpenMP layout) on the host cores, on a bounded sample:
@@ -365,7 +379,7 @@ def run_ours(args, dist: Dist):
         if prof is None:
             # the GPU solve's own profile (same algorithm; within rounding of the reference's)
             prof = {"k": int(vres.k), "shift_updates": int(np.sum(vres.active)), "source": "the GPU solve's profile"}
-        cpu = cpu_baseline(f, prof)
+        cpu = cpu_baseline_fresh(args.workload, args.scale, prof)
 
     line = {
         "metric": METRIC, "value": step_max, "unit": "s", "n_gpus": dist.world, "steps": args.steps,
@@ -507,7 +521,7 @@ def run_adjoint_c5(args, dist: Dist):
     if not args.no_cpu_baseline:
         fwd = pkg.solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=f.max_iter)
         prof = {"k": int(fwd.k), "shift_updates": int(np.sum(fwd.active)), "source": "the GPU forward solve's profile"}
-        cb = cpu_baseline(f, prof)
+        cb = cpu_baseline_fresh("c5", args.scale, prof)
         cb["value"] *= 2.0
         cb["sample"] = "2 x (forward family) " + cb["sample"]
         line["cpu_baseline"] = cb
