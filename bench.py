@@ -350,8 +350,14 @@ def run_ours(args, dist: Dist):
     if flush_launches and flush_ms > 0 and flush_ms >= spmv_share_ms:
         roofline = flush_roofline(flush_bytes / flush_launches, flush_ms / flush_launches, n, m, hbm, peak_kind)
 
-    # e2e through the reference-facing C ABI with pinned host buffers
+    # e2e through the reference-facing C ABI with pinned host buffers; the
+    # device-side objects above are closed first (their memory goes back to
+    # the library's pool, which the calls below reuse), one untimed warm-up call
     e2e = None
+    res_k, res_format = res.k, A.format
+    solver.close()
+    A.close()
+    ctx.close()
     if not args.no_e2e:
         h_ptr = torch.from_numpy(f.a.ptr).pin_memory()
         h_col = torch.from_numpy(f.a.col).pin_memory()
@@ -362,12 +368,18 @@ def run_ours(args, dist: Dist):
         h_r = torch.empty(n, dtype=torch.float64).pin_memory()
         e2e_steps = max(1, min(args.steps, 2))
         dist.barrier()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
+        e2e_times = []
+        for i in range(e2e_steps + 1):
+            # the caller's inputs per the reference's contract (x zero, r = b on
+            # entry); the timed region is the call: every host<->device copy,
+            # the device set-up, the solve and the teardown
             h_x.zero_()
             h_r.copy_(h_b)
+            t0 = time.perf_counter()
             k = pkg.dropin_raw("dynamic", h_ptr, h_col, h_val, h_x, h_r, h_sig, f.seed, f.tol, f.max_iter)
-        e2e_s = (time.perf_counter() - t0) / e2e_steps
+            if i:  # the first call is the warm-up
+                e2e_times.append(time.perf_counter() - t0)
+        e2e_s = float(np.mean(e2e_times))
         e2e_max, _ = aggregate(dist, e2e_s, 1.0)
         e2e = {"value": e2e_max, "unit": "s", "h2d_bytes_per_step": int(h_ptr.nbytes + h_col.nbytes + h_val.nbytes
                                                                           + h_b.nbytes + h_sig.nbytes),
@@ -388,7 +400,7 @@ def run_ours(args, dist: Dist):
         "config": {"workload": f"{args.workload}: {f.a.n} rows, {f.a.nnz} nonzeros, {MATRIX_KIND.get(args.workload, '')}"
                    f"{m} shifts in [{f.sigma.min():g}, {f.sigma.max():g}], tol {f.tol:g}, seed {f.seed}",
                    "mode": args.mode, "shift_mode": res.shift_mode, "refine": not args.no_refine,
-                   "spmv_format": A.format,
+                   "spmv_format": res_format,
                    "parallelism": f"replicas x{dist.world}",
                    "l2": "working set >> 129 MB L2 (no flush needed)"},
         "iterations": res.k, "switches": res.switches, "refined_shifts": res.refined,

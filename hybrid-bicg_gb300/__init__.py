@@ -127,6 +127,7 @@ def lib() -> C.CDLL:
         "hbicg_matrix_load_mm": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
         "hbicg_matrix_get_csr": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
         "hbicg_matrix_format": (C.c_int, [C.c_void_p]),
+        "hbicg_release": (None, []),
         "hbicg_matrix_transpose": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
         "hbicg_adjoint_gradients": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_ulonglong, C.c_void_p,
                                               C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -600,6 +601,11 @@ def true_residuals_noalloc(matrix: "Matrix", x, b, sigma, res, stream: int = 0) 
     ldx = int(x.stride(0)) if m else matrix.n
     _check(lib().hbicg_true_residuals_noalloc(matrix.h, _ptr(x), ldx, _ptr(b), _ptr(sigma), m, _ptr(res),
                                               C.c_void_p(stream)), "hbicg_true_residuals_noalloc")
+
+
+def release() -> None:
+    """Return the device memory the library keeps between solves (its pool)."""
+    lib().hbicg_release()
 
 
 def dropin_raw(variant: str, ptr, col, val, x, r, sigma, seed=0, tol=1e-12, max_iter=2000, switching=True) -> int:

@@ -333,6 +333,40 @@ static int build_sell(hbicg_matrix *A, const unsigned *h_ptr, unsigned n, unsign
     return HBICG_OK;
 }
 
+/* row blocks of the tile form (hbk_plan_rows) */
+static int build_tile_plan(hbicg_matrix *A, const unsigned *h_ptr) {
+    cudaStream_t st = A->ctx->stream;
+    const unsigned n = A->k.n;
+    const unsigned nb = hbk_plan_rows(n, h_ptr, NULL, NULL);
+    unsigned *blk = malloc(sizeof(unsigned) * ((size_t)nb + 1));
+    unsigned char *kind = malloc((size_t)nb + 1);
+    int rc = HBICG_OK;
+    if (!blk || !kind) {
+        rc = HBICG_E_NOMEM;
+    } else {
+        hbk_plan_rows(n, h_ptr, blk, kind);
+        cudaError_t e = cudaMalloc((void **)&A->d_blk_row, sizeof(unsigned) * ((size_t)nb + 1));
+        if (!e) e = cudaMalloc((void **)&A->d_blk_kind, (size_t)nb + 1);
+        if (!e) e = cudaMemcpyAsync(A->d_blk_row, blk, sizeof(unsigned) * ((size_t)nb + 1), cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaMemcpyAsync(A->d_blk_kind, kind, (size_t)nb + 1, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaStreamSynchronize(st);
+        if (e) {
+            set_msg("tile plan: %s", cudaGetErrorString(e));
+            rc = HBICG_E_CUDA;
+        }
+    }
+    free(blk);
+    free(kind);
+    if (rc) return rc;
+    A->k.blk_row = A->d_blk_row;
+    A->k.blk_kind = A->d_blk_kind;
+    A->k.nblk = nb;
+    A->k.grid = hbk_spmv_grid(nb);
+    return HBICG_OK;
+}
+
+static void hbicg_matrix_destroy_unretained(hbicg_matrix *A);
+
 int hbicg_matrix_create(hbicg_context *ctx, unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *col,
                         const double *val, int where, hbicg_matrix **out) {
     hbicg_matrix *A = calloc(1, sizeof *A);
@@ -367,46 +401,27 @@ int hbicg_matrix_create(hbicg_context *ctx, unsigned n, unsigned nnz, const unsi
         free(A);
         return HBICG_E_ARG;
     }
-    unsigned nb = hbk_plan_rows(n, h_ptr, NULL, NULL);
-    unsigned *blk = malloc(sizeof(unsigned) * ((size_t)nb + 1));
-    unsigned char *kind = malloc((size_t)nb + 1);
-    hbk_plan_rows(n, h_ptr, blk, kind);
-    CUDA_TRY(cudaMalloc((void **)&A->d_blk_row, sizeof(unsigned) * ((size_t)nb + 1)));
-    CUDA_TRY(cudaMalloc((void **)&A->d_blk_kind, (size_t)nb + 1));
-    CUDA_TRY(cudaMemcpyAsync(A->d_blk_row, blk, sizeof(unsigned) * ((size_t)nb + 1), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(A->d_blk_kind, kind, (size_t)nb + 1, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    free(blk);
-    free(kind);
-    if (where == HBICG_DEVICE) free(h_ptr);
     A->k.n = n;
     A->k.nnz = nnz;
     A->k.ptr = A->d_ptr;
     A->k.col = A->d_col;
     A->k.val = A->d_val;
-    A->k.blk_row = A->d_blk_row;
-    A->k.blk_kind = A->d_blk_kind;
-    A->k.nblk = nb;
-    A->k.grid = hbk_spmv_grid(nb);
     A->k.fmt = HBK_FMT_TILE;
-    {
-        unsigned *hp = h_ptr;
-        if (where == HBICG_DEVICE) {
-            hp = malloc(sizeof(unsigned) * ((size_t)n + 1));
-            if (!hp) return HBICG_E_NOMEM;
-            CUDA_TRY(cudaMemcpy(hp, ptr, sizeof(unsigned) * ((size_t)n + 1), cudaMemcpyDeviceToHost));
-        }
-        int rc = build_sell(A, hp, n, nnz, 0);
-        /* irregular rows: the HYB form unless the tile form was asked for */
-        const char *env = getenv("HBICG_SPMV_FORMAT");
-        if (!rc && A->k.fmt != HBK_FMT_SELL && n && !(env && !strcmp(env, "tile"))) {
-            rc = build_hyb(A, hp, n);
-            if (!rc) use_hyb(A);
-        }
-        if (where == HBICG_DEVICE) free(hp);
-        if (rc) return rc;
-        if (A->k.fmt == HBK_FMT_SELL) A->k.grid = hbk_spmv_grid((n + HBK_THREADS - 1) / HBK_THREADS);
+    /* SELL-32 for regular rows, HYB for irregular ones, the tile form on
+     * request; the tile form's row plan is built only when it is used */
+    int rc = build_sell(A, h_ptr, n, nnz, 0);
+    const char *env = getenv("HBICG_SPMV_FORMAT");
+    if (!rc && A->k.fmt != HBK_FMT_SELL && n && !(env && !strcmp(env, "tile"))) {
+        rc = build_hyb(A, h_ptr, n);
+        if (!rc) use_hyb(A);
     }
+    if (!rc && A->k.fmt == HBK_FMT_TILE) rc = build_tile_plan(A, h_ptr);
+    if (where == HBICG_DEVICE) free(h_ptr);
+    if (rc) {
+        hbicg_matrix_destroy_unretained(A);
+        return rc;
+    }
+    if (A->k.fmt == HBK_FMT_SELL) A->k.grid = hbk_spmv_grid((n + HBK_THREADS - 1) / HBK_THREADS);
     ctx_retain(ctx);
     *out = A;
     return HBICG_OK;
@@ -526,6 +541,27 @@ int hbicg_matrix_load_mm(hbicg_context *ctx, const char *path, int expand_symmet
     return rc;
 }
 
+/* frees a matrix whose creation failed before it took its context reference */
+static void hbicg_matrix_destroy_unretained(hbicg_matrix *A) {
+    cudaStreamSynchronize(A->ctx->stream);
+    if (A->owns) {
+        cudaFree(A->d_ptr);
+        cudaFree(A->d_col);
+        cudaFree(A->d_val);
+    }
+    cudaFree(A->d_blk_row);
+    cudaFree(A->d_blk_kind);
+    cudaFree(A->d_sval);
+    cudaFree(A->d_scol);
+    cudaFree(A->d_sptr);
+    cudaFree(A->d_hval);
+    cudaFree(A->d_hcol);
+    cudaFree(A->d_hsptr);
+    cudaFree(A->d_srow);
+    cudaFree(A->d_wrow);
+    free(A);
+}
+
 void hbicg_matrix_destroy(hbicg_matrix *A) {
     if (!A) return;
     cudaStreamSynchronize(A->ctx->stream);
@@ -607,6 +643,13 @@ static unsigned *host_ptr_copy(hbicg_matrix *A) {
 int hbicg_matrix_set_format(hbicg_matrix *A, int fmt) {
     if (!A || (fmt != HBICG_SPMV_TILE && fmt != HBICG_SPMV_SELL && fmt != HBICG_SPMV_HYB)) return HBICG_E_ARG;
     if (fmt == HBICG_SPMV_TILE) {
+        if (!A->d_blk_row) {
+            unsigned *hp = host_ptr_copy(A);
+            if (!hp) return HBICG_E_NOMEM;
+            int rc = build_tile_plan(A, hp);
+            free(hp);
+            if (rc) return rc;
+        }
         A->k.fmt = HBK_FMT_TILE;
         A->k.grid = hbk_spmv_grid(A->k.nblk);
         return HBICG_OK;
@@ -844,7 +887,59 @@ static int pick_mode(const hbicg_params *p, unsigned n, int m) {
     return HBICG_SHIFTS_INCREMENTAL;
 }
 
-#define DALLOC(ptr, bytes) CUDA_TRY(cudaMalloc((void **)&(ptr), (size_t)(bytes) > 0 ? (size_t)(bytes) : 8))
+/* Solver buffers come from a library-owned stream-ordered pool per device that
+ * keeps freed memory for the next solver (release threshold: unlimited): a
+ * one-shot call such as the reference's entry points, which sets up and tears
+ * down ~25 GB at 256^3, then neither maps nor unmaps it every time.
+ * hbicg_release() returns the cached memory to the device. */
+#define HBICG_MAX_DEVICES 64
+static cudaMemPool_t g_pools[HBICG_MAX_DEVICES];
+static pthread_mutex_t g_pool_lock = PTHREAD_MUTEX_INITIALIZER;
+
+static cudaError_t solver_pool(cudaMemPool_t *out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    if (dev < 0 || dev >= HBICG_MAX_DEVICES) return cudaErrorInvalidDevice;
+    pthread_mutex_lock(&g_pool_lock);
+    if (!g_pools[dev]) {
+        struct cudaMemPoolProps props;
+        memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool;
+        e = cudaMemPoolCreate(&pool, &props);
+        if (!e) {
+            unsigned long long keep = ~0ull;
+            e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            if (!e) g_pools[dev] = pool;
+            else cudaMemPoolDestroy(pool);
+        }
+    }
+    *out = g_pools[dev];
+    pthread_mutex_unlock(&g_pool_lock);
+    return e;
+}
+
+/* usable from any stream on return (the allocation's stream is synchronised) */
+static cudaError_t pool_alloc(void **p, size_t bytes, cudaStream_t st) {
+    cudaMemPool_t pool;
+    cudaError_t e = solver_pool(&pool);
+    if (!e) e = cudaMallocFromPoolAsync(p, bytes > 0 ? bytes : 8, pool, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    return e;
+}
+
+void hbicg_release(void) {
+    pthread_mutex_lock(&g_pool_lock);
+    for (int d = 0; d < HBICG_MAX_DEVICES; ++d)
+        if (g_pools[d]) cudaMemPoolTrimTo(g_pools[d], 0);
+    pthread_mutex_unlock(&g_pool_lock);
+}
+
+#define DALLOC(ptr, bytes) CUDA_TRY(pool_alloc((void **)&(ptr), (size_t)(bytes), ctx->stream))
 
 int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_params *pp, hbicg_solver **out) {
     hbicg_params p;
@@ -905,9 +1000,9 @@ int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_
             /* not enough memory for a useful basis: fall back */
             s->mode = HBICG_SHIFTS_INCREMENTAL;
             v->deferred = 0;
-            cudaFree(v->ps);
+            cudaFreeAsync(v->ps, ctx->stream);
             v->ps = NULL;
-            cudaFree(v->Xp);
+            cudaFreeAsync(v->Xp, ctx->stream);
             v->Xp = NULL;
             DALLOC(v->rbuf[0], vb);
             DALLOC(v->rbuf[1], vb);
@@ -985,7 +1080,7 @@ void hbicg_solver_destroy(hbicg_solver *s) {
                     sh->rr_hist, sh->sw_seed, sh->act_hist, sh->partials, sh->counters, s->d_b, s->d_res, s->d_dot, s->d_rold,
                     s->d_qcopy, s->tc_ws, s->d_tc_err};
     for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++)
-        if (ptrs[i]) cudaFree(ptrs[i]);
+        if (ptrs[i]) cudaFreeAsync(ptrs[i], s->ctx->stream); /* back to the pool, in stream order */
     hbicg_context *ctx = s->ctx;
     free(s);
     ctx_release(ctx);
@@ -1197,7 +1292,7 @@ static int ensure_pmat(hbicg_solver *s) {
     if (s->v.Pmat) return HBICG_OK;
     const int mm = s->m > 0 ? s->m : 1;
     const size_t bytes = sizeof(double) * hbk_panel_elems(s->A->k.n, mm); /* panel-major */
-    CUDA_TRY(cudaMalloc((void **)&s->v.Pmat, bytes));
+    CUDA_TRY(pool_alloc((void **)&s->v.Pmat, bytes, s->ctx->stream));
     CUDA_TRY(cudaMemsetAsync(s->v.Pmat, 0, bytes, s->ctx->stream));
     /* the graphs captured the old (null) Pmat pointer: capture again */
     if (s->graph) {

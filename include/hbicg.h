@@ -249,6 +249,11 @@ int hbicg_solve(unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *c
                 const double *b, const double *sigma, int m, int seed, const hbicg_params *p, double *x,
                 double *r_out, hbicg_stats *stats);
 
+/* Solvers take their device buffers from a library-owned pool that keeps freed
+ * memory for the next solver; this returns the memory no live solver uses to
+ * the device (call it when the library's solves are done). */
+void hbicg_release(void);
+
 #ifdef __cplusplus
 }
 #endif
