@@ -410,9 +410,6 @@ def run_ours(args, dist: Dist):
         "roofline": roofline, "roofline_spmv": spmv, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }
-    solver.close()
-    A.close()
-    ctx.close()
     return line
 
 
