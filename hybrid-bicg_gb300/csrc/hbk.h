@@ -207,6 +207,8 @@ int hbk_flush_tc_run_live(const double *V, size_t ld, unsigned n, int L, const d
                           const double *own, int m, double *X, double *Pmat, int keep_p, const int *conv_k,
                           int k_last, const unsigned long long *slot_max, void *ws, int *err, cudaStream_t st);
 const int *hbk_flush_tc_live_count(const void *ws, int m); /* device int: live shifts of the last run on ws */
+/* x[i] = element i of system j of the panel-major Xp (m systems), i < n */
+int hbk_panel_row(const double *Xp, int m, unsigned n, int j, double *x, cudaStream_t st);
 /* X[j][i] (leading dimension ld) = Xp in panel layout with m systems, i < n */
 int hbk_panel_to_rows(const double *Xp, int m, unsigned n, double *X, size_t ld, cudaStream_t st);
 /* after a flush: zero the coefficients, own = (0, keep_p), basis slot 0 = r_{k-1} */

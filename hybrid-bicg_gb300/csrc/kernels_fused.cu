@@ -781,6 +781,13 @@ __global__ void __launch_bounds__(NT) k_absmax(const double *__restrict__ x, uns
     block_max_to(mx, smx, out);
 }
 
+// x[i] = element i of system j of the panel-major Xp (runs of HBK_PANEL)
+__global__ void __launch_bounds__(NT) k_panel_row(const double *__restrict__ Xp, int m, unsigned n, int j,
+                                                  double *__restrict__ x) {
+    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT)
+        x[i] = Xp[panel_idx(j, (unsigned)i, m)];
+}
+
 // X[j][i] = element i of system j of the panel-major Xp: one block per panel
 // (m * HBK_PANEL values read contiguously, written as runs of HBK_PANEL)
 __global__ void __launch_bounds__(NT) k_panel_to_rows(const double *__restrict__ Xp, int m, unsigned n,
@@ -800,6 +807,12 @@ __global__ void __launch_bounds__(NT) k_panel_to_rows(const double *__restrict__
 }  // namespace
 
 extern "C" {
+
+int hbk_panel_row(const double *Xp, int m, unsigned n, int j, double *x, cudaStream_t st) {
+    if (n == 0 || j < 0 || j >= m) return 0;
+    k_panel_row<<<grid_for(n, 4), NT, 0, st>>>(Xp, m, n, j, x);
+    return (int)cudaGetLastError();
+}
 
 int hbk_panel_to_rows(const double *Xp, int m, unsigned n, double *X, size_t ld, cudaStream_t st) {
     if (m <= 0 || n == 0) return 0;

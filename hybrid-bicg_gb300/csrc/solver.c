@@ -102,7 +102,8 @@ void hbicg_params_default(hbicg_params *p) {
 /* ------------------------------------------------------------------------ */
 struct hbicg_context {
     cudaStream_t stream;
-    cudaEvent_t ev0, ev1, evf0, evf1;
+    cudaStream_t cstream;  /* copies of finished solutions to the host during a solve */
+    cudaEvent_t ev0, ev1, evf0, evf1, cev;
     hbk_scalars *h_sc; /* pinned */
     double *h_dbl;     /* pinned scratch */
     int refs;          /* the caller's handle + one per live matrix or solver */
@@ -121,6 +122,8 @@ int hbicg_context_create(hbicg_context **out) {
     if (!c) return HBICG_E_NOMEM;
     c->refs = 1;
     CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&c->cev, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreate(&c->ev0));
     CUDA_TRY(cudaEventCreate(&c->ev1));
     CUDA_TRY(cudaEventCreate(&c->evf0));
@@ -137,6 +140,9 @@ void hbicg_context_destroy(hbicg_context *c) {
 
 static void ctx_free(hbicg_context *c) {
     cudaStreamSynchronize(c->stream);
+    cudaStreamSynchronize(c->cstream);
+    cudaStreamDestroy(c->cstream);
+    cudaEventDestroy(c->cev);
     cudaFreeHost(c->h_sc);
     cudaFreeHost(c->h_dbl);
     cudaEventDestroy(c->ev0);
@@ -789,8 +795,16 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
     }
     int rc = hbicg_matrix_set_format(A, pick == 1 ? HBICG_SPMV_SELL : pick == 2 ? HBICG_SPMV_HYB : HBICG_SPMV_TILE);
     if (rc) return rc;
-    if (pick != 2 && A->d_hval) { /* the HYB copy is not used: give its memory back */
+    /* give the memory of the forms not chosen back; the kernel view keeps
+     * only pointers into the chosen form (SELL-32 and HYB share its
+     * sval/scol/sptr fields, so only pointers to the freed arrays are cleared) */
+    if (pick != 2 && A->d_hval) { /* the HYB copy is not used */
         cudaStreamSynchronize(A->ctx->stream);
+        if (A->k.sval == A->d_hval) {
+            A->k.sval = NULL;
+            A->k.scol = NULL;
+            A->k.sptr = NULL;
+        }
         cudaFree(A->d_hval);
         cudaFree(A->d_hcol);
         cudaFree(A->d_hsptr);
@@ -803,18 +817,22 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
         A->d_wrow = NULL;
         A->k.srow = NULL;
         A->k.wrow = NULL;
+        A->k.nslice = 0;
+        A->k.nwrow = 0;
     }
-    if (pick != 1 && A->d_sval) { /* the SELL copy is not used: give its memory back */
+    if (pick != 1 && A->d_sval) { /* the SELL copy is not used */
         cudaStreamSynchronize(A->ctx->stream);
+        if (A->k.sval == A->d_sval) {
+            A->k.sval = NULL;
+            A->k.scol = NULL;
+            A->k.sptr = NULL;
+        }
         cudaFree(A->d_sval);
         cudaFree(A->d_scol);
         cudaFree(A->d_sptr);
         A->d_sval = NULL;
         A->d_scol = NULL;
         A->d_sptr = NULL;
-        A->k.sval = NULL;
-        A->k.scol = NULL;
-        A->k.sptr = NULL;
     }
     if (chosen) *chosen = pick == 1 ? HBICG_SPMV_SELL : pick == 2 ? HBICG_SPMV_HYB : HBICG_SPMV_TILE;
     if (tile_ms) *tile_ms = t_tile;
@@ -875,7 +893,49 @@ struct hbicg_solver {
     int *d_tc_err;    /* set by the tensor-core flush on a bounded-wait timeout */
     int launches_per_iter;
     double flush_bytes; /* compulsory HBM bytes of this solve's basis flushes */
+    /* deferred mode, pinned host x: solutions that became final at a flush
+     * are copied out while the solve goes on */
+    double *early_x;        /* the caller's x (host, pinned), or NULL */
+    unsigned char *early;   /* [m] row copied */
+    int early_pending;      /* copies issued on the context's copy stream */
 };
+
+/* After a flush that covered iterations up to k_flushed: shifts that
+ * converged by then have their final x_j in the panel-major array (later
+ * flushes leave them alone), so each new one is written row-major into X and
+ * copied to the caller's buffer on the copy stream, overlapping the rest of
+ * the solve. */
+static int early_copies(hbicg_solver *s, int k_flushed, int *launches) {
+    cudaStream_t st = s->ctx->stream;
+    const int m = s->m;
+    const unsigned n = s->A->k.n;
+    int *conv = malloc(sizeof(int) * (size_t)(m > 0 ? m : 1));
+    if (!conv) return HBICG_E_NOMEM;
+    CUDA_TRY(cudaMemcpyAsync(conv, s->sh.conv_k, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    int any = 0;
+    for (int j = 0; j < m; ++j) {
+        s->early[j] = s->early[j] ? 1 : 0;
+        if (!s->early[j] && conv[j] > 0 && conv[j] <= k_flushed) {
+            HBK_TRY(hbk_panel_row(s->v.Xp, s->v.pm, n, j, s->v.X + (size_t)j * s->ld, st));
+            ++*launches;
+            s->early[j] = 2; /* written this time: copy below */
+            any = 1;
+        }
+    }
+    free(conv);
+    if (!any) return HBICG_OK;
+    CUDA_TRY(cudaEventRecord(s->ctx->cev, st));
+    CUDA_TRY(cudaStreamWaitEvent(s->ctx->cstream, s->ctx->cev, 0));
+    for (int j = 0; j < m; ++j)
+        if (s->early[j] == 2) {
+            CUDA_TRY(cudaMemcpyAsync(s->early_x + (size_t)j * n, s->v.X + (size_t)j * s->ld, sizeof(double) * n,
+                                     cudaMemcpyDeviceToHost, s->ctx->cstream));
+            s->early[j] = 1;
+        }
+    s->early_pending = 1;
+    return HBICG_OK;
+}
 
 static int pick_mode(const hbicg_params *p, unsigned n, int m) {
     if (p->form == HBICG_FORM_PLAIN) return HBICG_SHIFTS_INCREMENTAL;
@@ -1082,6 +1142,7 @@ void hbicg_solver_destroy(hbicg_solver *s) {
     for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++)
         if (ptrs[i]) cudaFreeAsync(ptrs[i], s->ctx->stream); /* back to the pool, in stream order */
     hbicg_context *ctx = s->ctx;
+    free(s->early);
     free(s);
     ctx_release(ctx);
 }
@@ -1372,6 +1433,7 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, dou
             rc = do_flush(s, 1, h->slots, k_flushed, launches);
             if (rc) return rc;
             k_flushed = h->k - 1;
+            if (s->early_x && (rc = early_copies(s, k_flushed, launches))) return rc;
             CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
             CUDA_TRY(cudaEventSynchronize(s->ctx->evf1));
             CUDA_TRY(cudaEventElapsedTime(&t, s->ctx->evf0, s->ctx->evf1));
@@ -1387,7 +1449,12 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, dou
         int rc = do_flush(s, 0, h->slots, k_flushed, launches);
         if (rc) return rc;
         CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
-        /* x_j were panel-major during the solve */
+        /* x_j were panel-major during the solve; rows already on their way to
+         * the host are rewritten with the same values only after those copies */
+        if (s->early_pending) {
+            CUDA_TRY(cudaEventRecord(s->ctx->cev, s->ctx->cstream));
+            CUDA_TRY(cudaStreamWaitEvent(st, s->ctx->cev, 0));
+        }
         HBK_TRY(hbk_panel_to_rows(s->v.Xp, s->v.pm, s->A->k.n, s->v.X, s->ld, st));
         ++*launches;
         CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
@@ -1459,7 +1526,7 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
 /* params.refine: true residuals of every shift; a shift above tol gets
  * x_j += e with (A + sigma_j I) e = b - (A + sigma_j I) x_j solved (single
  * shift, incremental form) to 0.5 tol ||b|| / ||r_j||; at most 3 rounds. */
-static int refine_shifts(hbicg_solver *s, const double *h_sigma, int *refined) {
+static int refine_shifts(hbicg_solver *s, const double *h_sigma, int *refined, unsigned char *fixed) {
     cudaStream_t st = s->ctx->stream;
     const unsigned n = s->A->k.n;
     const int m = s->m;
@@ -1505,6 +1572,7 @@ static int refine_shifts(hbicg_solver *s, const double *h_sigma, int *refined) {
             }
             HBK_TRY(hbk_axpy(n, 1.0, e, xj, st));
             ++*refined;
+            if (fixed) fixed[j] = 1;
         }
         if (!any) break;
     }
@@ -1522,6 +1590,12 @@ int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int 
     memset(&touch, 0, sizeof touch);
     const int rc = solver_run_impl(s, b, sigma, seed, in_where, x, r_out, out_where, stats, &touch);
     touch_join(&touch);
+    /* no copy into the caller's buffer outlives the call, whatever path returned */
+    if (s->early_pending) cudaStreamSynchronize(s->ctx->cstream);
+    s->early_x = NULL;
+    s->early_pending = 0;
+    free(s->early);
+    s->early = NULL;
     return rc;
 }
 
@@ -1545,12 +1619,20 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
         CUDA_TRY(cudaMemcpyAsync(s->d_sigma, sigma, sizeof(double) * m, kin, st));
     }
     CUDA_TRY(cudaMemcpyAsync(s->d_b, b, sizeof(double) * n, kin, st));
+    /* pinned host x needs no page touching; in deferred mode its finished rows
+     * are copied out during the solve */
+    int x_pinned = 0;
+    if (out_where != HBICG_DEVICE && x && m > 0) {
+        struct cudaPointerAttributes pa;
+        x_pinned = cudaPointerGetAttributes(&pa, x) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+        cudaGetLastError(); /* an unregistered pointer is not an error here */
+    }
     /* host outputs: fault their pages in while the GPU solves (the inputs are
      * consumed first, in case an output buffer also held an input) */
-    if (out_where != HBICG_DEVICE && ((x && m > 0) || r_out)) {
+    if (out_where != HBICG_DEVICE && ((x && m > 0 && !x_pinned) || r_out)) {
         CUDA_TRY(cudaStreamSynchronize(st));
-        touch->p[0] = (char *)x;
-        touch->bytes[0] = x ? sizeof(double) * (size_t)n * (size_t)(m > 0 ? m : 0) : 0;
+        touch->p[0] = x_pinned ? NULL : (char *)x;
+        touch->bytes[0] = x && !x_pinned ? sizeof(double) * (size_t)n * (size_t)(m > 0 ? m : 0) : 0;
         touch->p[1] = (char *)r_out;
         touch->bytes[1] = r_out ? sizeof(double) * (size_t)n : 0;
         if (touch->bytes[0] + touch->bytes[1] >= (1u << 20) && pthread_create(&touch->th, NULL, touch_pages, touch) == 0)
@@ -1558,6 +1640,14 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
         else
             touch_pages(touch);
     }
+    /* deferred mode into pinned host memory: copy finished solutions out
+     * during the solve (pageable copies would block the thread driving it) */
+    s->early_x = NULL;
+    s->early_pending = 0;
+    free(s->early);
+    s->early = NULL;
+    if (s->p.form != HBICG_FORM_PLAIN && s->v.deferred && x_pinned && (s->early = calloc((size_t)m, 1)) != NULL)
+        s->early_x = x;
     CUDA_TRY(cudaEventRecord(ctx->ev0, st));
     int rc = HBICG_OK, launches = 0, flushes = 0;
     double flush_ms = 0.0;
@@ -1604,16 +1694,30 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
         }
     }
     CUDA_TRY(cudaEventRecord(ctx->ev1, st));
+    /* copies issued during the solve finish before anything rewrites X */
+    if (s->early_pending) CUDA_TRY(cudaStreamSynchronize(ctx->cstream));
     int refined = 0;
+    unsigned char *fixed = s->early_x ? calloc((size_t)m, 1) : NULL;
     /* only after a converged solve: a solve stopped by max_iter or a breakdown
      * keeps its x as the reference leaves it */
     if (rc == HBICG_OK && status == HBICG_OK && s->p.refine && m > 0 && k < s->kcap) {
-        rc = refine_shifts(s, h_sigma, &refined);
+        rc = refine_shifts(s, h_sigma, &refined, fixed);
         CUDA_TRY(cudaEventRecord(ctx->ev1, st)); /* solve_ms includes the corrections */
     }
     touch_join(touch);
-    if (rc == HBICG_OK && x && m > 0)
-        CUDA_TRY(cudaMemcpy2DAsync(x, sizeof(double) * n, s->v.X, sizeof(double) * s->ld, sizeof(double) * n, m, kout, st));
+    if (rc == HBICG_OK && x && m > 0) {
+        if (s->early_x && s->early && fixed) {
+            /* the rows not copied during the solve, and the corrected ones */
+            for (int j = 0; j < m; ++j)
+                if (!s->early[j] || fixed[j])
+                    CUDA_TRY(cudaMemcpyAsync(x + (size_t)j * n, s->v.X + (size_t)j * s->ld, sizeof(double) * n,
+                                             kout, st));
+        } else {
+            CUDA_TRY(cudaMemcpy2DAsync(x, sizeof(double) * n, s->v.X, sizeof(double) * s->ld, sizeof(double) * n, m,
+                                       kout, st));
+        }
+    }
+    free(fixed);
     if (rc == HBICG_OK && r_out && r_final) CUDA_TRY(cudaMemcpyAsync(r_out, r_final, sizeof(double) * n, kout, st));
     double maxres = 0.0;
     double *h_res = NULL;
