@@ -589,8 +589,11 @@ def run_flush_kernel(args):
     ms = e0.elapsed_time(e1) / args.steps
     byt = 8.0 * n * (L + 4 * m)
     hbm, kind = peaks()
+    # the FP64 product it stands in for: 2 m rows (x and p) x L slots x n, 2 flops each
+    fp64_tflops = 2.0 * (2 * m) * L * n / (ms * 1e-3) / 1e12
     return {"kernel": "k_flush_tc", "n": n, "shifts": m, "slots": L, "ms_per_launch": ms, "bytes_per_launch": byt,
-            "achieved_gbs": byt / (ms * 1e-3) / 1e9, "frac": byt / (ms * 1e-3) / 1e9 / hbm, "peak_kind": kind}
+            "achieved_gbs": byt / (ms * 1e-3) / 1e9, "frac": byt / (ms * 1e-3) / 1e9 / hbm, "peak_kind": kind,
+            "fp64_equivalent_tflops": fp64_tflops, "fp64_peak_tflops_measured_probe": 1.012}
 
 
 def run_spmv_kernel(args):
