@@ -366,7 +366,7 @@ def run_ours(args, dist: Dist):
         h_sig = torch.from_numpy(f.sigma).pin_memory()
         h_x = torch.empty((m, n), dtype=torch.float64).pin_memory()
         h_r = torch.empty(n, dtype=torch.float64).pin_memory()
-        e2e_steps = max(1, min(args.steps, 2))
+        e2e_steps = 3  # the median of three calls: one slow call on a shared host does not set the figure
         dist.barrier()
         e2e_times = []
         for i in range(e2e_steps + 1):
@@ -379,7 +379,7 @@ def run_ours(args, dist: Dist):
             k = pkg.dropin_raw("dynamic", h_ptr, h_col, h_val, h_x, h_r, h_sig, f.seed, f.tol, f.max_iter)
             if i:  # the first call is the warm-up
                 e2e_times.append(time.perf_counter() - t0)
-        e2e_s = float(np.mean(e2e_times))
+        e2e_s = float(np.median(e2e_times))
         e2e_max, _ = aggregate(dist, e2e_s, 1.0)
         e2e = {"value": e2e_max, "unit": "s", "h2d_bytes_per_step": int(h_ptr.nbytes + h_col.nbytes + h_val.nbytes
                                                                           + h_b.nbytes + h_sig.nbytes),

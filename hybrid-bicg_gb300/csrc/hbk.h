@@ -54,6 +54,7 @@ typedef struct {
     const double *sval;        /* SELL: values, slice s at sptr[s], entry e of lane l at +e*32+l */
     const unsigned *scol;      /* SELL: column indices (padding: the row itself, value 0) */
     const unsigned long long *sptr; /* SELL: n/32 rounded up + 1 slice offsets; HYB: nslice + 1 */
+    unsigned long long sell_len;    /* SELL: entries of sval/scol (with padding) */
     const unsigned *srow;      /* HYB: row of slice s, lane l at 32 s + l (>= n: an empty lane) */
     unsigned nslice;           /* HYB: slices of short rows */
     const unsigned *wrow;      /* HYB: rows longer than HBK_HYB_SHORT, longest first, one warp each */
@@ -135,6 +136,12 @@ typedef struct {
     double *Xp;                 /* x_j during the solve, panel-major */
     unsigned long long *slot_max; /* [slot_cap][HBK_SLOT_SPREAD] bits of max |V[l]|: the kernels that write a
                                      slot fold block b's maximum into entry b % HBK_SLOT_SPREAD */
+    /* seed shift folded into the SELL-32 diagonal (deferred mode): the seed
+     * kernels' products read sval_shift = sval with sigma_seed added at each
+     * row's diagonal entry (position sdiag[row]) instead of adding sigma x */
+    double *sval_shift;
+    const double *sval_orig;
+    const unsigned long long *sdiag;
     int pm;                     /* systems per panel (m) */
     int slot_cap;
     int deferred;
@@ -164,6 +171,13 @@ int hbk_sell_widths(unsigned n, const unsigned *ptr, unsigned *w, cudaStream_t s
 /* HYB slices: slice s, lane l holds row srow[32 s + l] (entry e at sptr[s] + 32 e + l) */
 int hbk_hyb_fill(unsigned nslice, const unsigned *srow, unsigned n, const unsigned *ptr, const unsigned *col,
                  const double *val, const unsigned long long *sptr, double *sval, unsigned *scol, cudaStream_t st);
+/* sdiag[r] = position in the SELL-32 arrays of row r's first stored diagonal
+ * entry; *missing = 1 when some row has none */
+int hbk_sell_diag(unsigned n, const unsigned *ptr, const unsigned long long *sptr, const unsigned *scol,
+                  unsigned long long *sdiag, int *missing, cudaStream_t st);
+/* sval_shift = sval (len entries) with *sigma (device) added at every row's diagonal */
+int hbk_fold_diag(unsigned n, const double *sval, unsigned long long len, const unsigned long long *sdiag,
+                  const double *sigma, double *sval_shift, cudaStream_t st);
 int hbk_sell_fill(unsigned n, const unsigned *ptr, const unsigned *col, const double *val,
                   const unsigned long long *sptr, double *sval, unsigned *scol, cudaStream_t st);
 

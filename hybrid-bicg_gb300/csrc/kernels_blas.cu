@@ -127,6 +127,36 @@ __global__ void __launch_bounds__(NT) k_hyb_fill(unsigned nslice, const unsigned
     }
 }
 
+// position of each row's first stored diagonal entry in the SELL-32 arrays
+__global__ void __launch_bounds__(NT) k_sell_diag(unsigned n, const unsigned *__restrict__ ptr,
+                                                  const unsigned long long *__restrict__ sptr,
+                                                  const unsigned *__restrict__ scol,
+                                                  unsigned long long *__restrict__ sdiag, int *missing) {
+    for (unsigned r = blockIdx.x * NT + threadIdx.x; r < n; r += gridDim.x * NT) {
+        const unsigned long long base = sptr[r >> 5] + (r & 31);
+        const unsigned len = ptr[r + 1] - ptr[r];
+        unsigned long long at = ~0ull;
+        for (unsigned e = 0; e < len; ++e)
+            if (scol[base + 32ull * e] == r) {
+                at = base + 32ull * e;
+                break;
+            }
+        sdiag[r] = at;
+        if (at == ~0ull) *missing = 1;
+    }
+}
+
+// sval_shift[sdiag[r]] = sval[sdiag[r]] + sigma (the rest copied before)
+__global__ void __launch_bounds__(NT) k_fold_diag(unsigned n, const double *__restrict__ sval,
+                                                  const unsigned long long *__restrict__ sdiag,
+                                                  const double *__restrict__ sigma, double *__restrict__ sval_shift) {
+    const double sg = *sigma;
+    for (unsigned r = blockIdx.x * NT + threadIdx.x; r < n; r += gridDim.x * NT) {
+        const unsigned long long d = sdiag[r];
+        sval_shift[d] = sval[d] + sg;
+    }
+}
+
 __global__ void __launch_bounds__(NT) k_sell_widths(unsigned n, const unsigned *__restrict__ ptr,
                                                     unsigned *__restrict__ w) {
     const unsigned ns = (n + 31) / 32;
@@ -165,6 +195,21 @@ int hbk_hyb_fill(unsigned nslice, const unsigned *srow, unsigned n, const unsign
                  const double *val, const unsigned long long *sptr, double *sval, unsigned *scol, cudaStream_t st) {
     if (!nslice) return 0;
     k_hyb_fill<<<grid_for(nslice * 32u, 1), NT, 0, st>>>(nslice, srow, n, ptr, col, val, sptr, sval, scol);
+    return (int)cudaGetLastError();
+}
+
+int hbk_sell_diag(unsigned n, const unsigned *ptr, const unsigned long long *sptr, const unsigned *scol,
+                  unsigned long long *sdiag, int *missing, cudaStream_t st) {
+    if (!n) return 0;
+    k_sell_diag<<<grid_for(n, 2), NT, 0, st>>>(n, ptr, sptr, scol, sdiag, missing);
+    return (int)cudaGetLastError();
+}
+
+int hbk_fold_diag(unsigned n, const double *sval, unsigned long long len, const unsigned long long *sdiag,
+                  const double *sigma, double *sval_shift, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyAsync(sval_shift, sval, sizeof(double) * len, cudaMemcpyDeviceToDevice, st);
+    if (e || !n) return (int)e;
+    k_fold_diag<<<grid_for(n, 2), NT, 0, st>>>(n, sval, sdiag, sigma, sval_shift);
     return (int)cudaGetLastError();
 }
 

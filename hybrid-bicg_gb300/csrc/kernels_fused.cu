@@ -127,9 +127,10 @@ __global__ void __launch_bounds__(NT) k_seed_s(Ctx c) {
     const double *__restrict__ ps = seed_p(c, seed);
     const double *__restrict__ rh = c.v.r_hat;
     double *__restrict__ s = c.v.s;
+    const bool folded = c.v.sval_shift != nullptr;  // the product already holds sigma p
     double acc = 0.0;
     auto epi = [&](unsigned r, double ax) {
-        const double sv = fma(sig, ps[r], ax);
+        const double sv = folded ? ax : fma(sig, ps[r], ax);
         s[r] = sv;
         acc = fma(rh[r], sv, acc);
     };
@@ -183,10 +184,11 @@ __global__ void __launch_bounds__(NT) k_seed_y(Ctx c) {
     const double sig = c.sh.sigma[sc->seed];
     const double *__restrict__ q = vec_q(c, sc);
     double *__restrict__ y = c.v.y;
+    const bool folded = c.v.sval_shift != nullptr;  // the product already holds sigma q
     double2 acc = make_double2(0.0, 0.0);
     auto epi = [&](unsigned r, double ax) {
         const double qr = q[r];
-        const double yv = fma(sig, qr, ax);
+        const double yv = folded ? ax : fma(sig, qr, ax);
         y[r] = yv;
         acc.x = fma(qr, qr, acc.x);
         acc.y = fma(qr, yv, acc.y);
@@ -656,6 +658,13 @@ __global__ void __launch_bounds__(NT) k_materialize_ps(Ctx c) {
         }
         if (i < n) c.v.ps[i] = acc;
     }
+    if (c.v.sval_shift) {  // the new seed's shift on the diagonal of the seed kernels' products
+        const double sg = c.sh.sigma[t];
+        for (size_t r = blockIdx.x * (size_t)NT + threadIdx.x; r < n; r += (size_t)gridDim.x * NT) {
+            const unsigned long long d = c.v.sdiag[r];
+            c.v.sval_shift[d] = c.v.sval_orig[d] + sg;
+        }
+    }
     if (take_ticket(c.sh.counters + 5)) {
         if (threadIdx.x == 0) {
             sc->need_ps = 0;
@@ -826,6 +835,12 @@ static Ctx make_ctx(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts 
     c.A = *A;
     c.v = *v;
     c.sh = *sh;
+    // the seed shift sits on the diagonal of a private copy of the SELL-32
+    // values: only while the matrix is in that form and the copy was made from it
+    if (c.v.sval_shift && c.A.fmt == HBK_FMT_SELL && c.v.deferred && c.A.sval == c.v.sval_orig)
+        c.A.sval = c.v.sval_shift;
+    else
+        c.v.sval_shift = nullptr;
     return c;
 }
 
@@ -845,6 +860,9 @@ int hbk_fused_init(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *
     } else {
         if ((e = hbk_copy(n, b, v->V, st))) return e;
         if ((e = hbk_copy(n, b, v->ps, st))) return e;
+        if (v->sval_shift && A->fmt == HBK_FMT_SELL && A->sval == v->sval_orig &&
+            (e = hbk_fold_diag(n, A->sval, A->sell_len, v->sdiag, sh->sigma + seed, v->sval_shift, st)))
+            return e;
         if (v->slot_max) {
             if ((e = (int)cudaMemsetAsync(v->slot_max, 0,
                                           sizeof(unsigned long long) * (size_t)v->slot_cap * HBK_SLOT_SPREAD, st)))

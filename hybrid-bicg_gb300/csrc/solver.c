@@ -167,6 +167,11 @@ struct hbicg_matrix {
     double *d_sval;
     unsigned *d_scol;
     unsigned long long *d_sptr;
+    /* positions of the diagonal entries in the SELL-32 arrays (for folding a
+     * shift into the diagonal); diag_state: 0 not computed, 1 ok, 2 a row has
+     * no stored diagonal */
+    unsigned long long *d_sdiag;
+    int diag_state;
     /* HYB form (hbk.h HBK_FMT_HYB) */
     double *d_hval;
     unsigned *d_hcol, *d_srow, *d_wrow;
@@ -336,6 +341,29 @@ static int build_sell(hbicg_matrix *A, const unsigned *h_ptr, unsigned n, unsign
     A->k.sval = A->d_sval;
     A->k.scol = A->d_scol;
     A->k.sptr = A->d_sptr;
+    A->k.sell_len = padded;
+    A->diag_state = 0; /* a new SELL-32 layout */
+    return HBICG_OK;
+}
+
+/* diagonal positions of the SELL-32 form (computed once per layout) */
+static int sell_diag(hbicg_matrix *A) {
+    if (A->diag_state) return HBICG_OK;
+    cudaStream_t st = A->ctx->stream;
+    const unsigned n = A->k.n;
+    int *d_missing = NULL, missing = 0;
+    if (!A->d_sdiag) CUDA_TRY(cudaMalloc((void **)&A->d_sdiag, sizeof(unsigned long long) * ((size_t)n + 1)));
+    CUDA_TRY(cudaMalloc((void **)&d_missing, sizeof(int)));
+    CUDA_TRY(cudaMemsetAsync(d_missing, 0, sizeof(int), st));
+    int e = hbk_sell_diag(n, A->d_ptr, A->d_sptr, A->d_scol, A->d_sdiag, d_missing, st);
+    if (!e) e = (int)cudaMemcpyAsync(&missing, d_missing, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (!e) e = (int)cudaStreamSynchronize(st);
+    cudaFree(d_missing);
+    if (e) {
+        set_msg("diagonal positions: %s", cudaGetErrorString((cudaError_t)e));
+        return HBICG_E_CUDA;
+    }
+    A->diag_state = missing ? 2 : 1;
     return HBICG_OK;
 }
 
@@ -565,6 +593,7 @@ static void hbicg_matrix_destroy_unretained(hbicg_matrix *A) {
     cudaFree(A->d_hsptr);
     cudaFree(A->d_srow);
     cudaFree(A->d_wrow);
+    cudaFree(A->d_sdiag);
     free(A);
 }
 
@@ -586,6 +615,7 @@ void hbicg_matrix_destroy(hbicg_matrix *A) {
     cudaFree(A->d_hsptr);
     cudaFree(A->d_srow);
     cudaFree(A->d_wrow);
+    cudaFree(A->d_sdiag);
     hbicg_context *ctx = A->ctx;
     free(A);
     ctx_release(ctx);
@@ -1075,6 +1105,18 @@ int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_
             DALLOC(v->Pc, sizeof(double) * (size_t)mm * (size_t)cap);
             DALLOC(v->own, sizeof(double) * 2 * (size_t)mm);
             DALLOC(v->slot_max, sizeof(unsigned long long) * (size_t)cap * HBK_SLOT_SPREAD);
+            /* SELL-32 matrices with a stored diagonal in every row: the seed's
+             * shift goes onto the diagonal of a private copy of the values,
+             * which saves the sigma p and sigma q terms of the two products */
+            if (p.form == HBICG_FORM_FUSED && A->k.fmt == HBK_FMT_SELL && A->d_sval && A->k.sell_len) {
+                const int drc = sell_diag(A);
+                if (drc) return drc;
+                if (A->diag_state == 1) {
+                    DALLOC(v->sval_shift, sizeof(double) * (size_t)A->k.sell_len);
+                    v->sval_orig = A->d_sval;
+                    v->sdiag = A->d_sdiag;
+                }
+            }
             if (p.flush_mode != HBICG_FLUSH_FP64) {
                 DALLOC(s->tc_ws, hbk_flush_tc_workspace_bytes(mm));
                 DALLOC(s->d_tc_err, sizeof(int));
@@ -1135,7 +1177,7 @@ void hbicg_solver_destroy(hbicg_solver *s) {
     hbk_vectors *v = &s->v;
     hbk_shifts *sh = &s->sh;
     void *ptrs[] = {v->r_hat, v->rbuf[0], v->rbuf[1], v->s, v->q, v->y, v->X, v->P, v->V, v->ps, v->Xc, v->Pc,
-                    v->own, v->Pmat, v->Xp, v->slot_max, s->d_sc, s->d_sigma, sh->a_hist, sh->b_hist, sh->w_hist, sh->ratio, sh->pi,
+                    v->own, v->Pmat, v->Xp, v->slot_max, v->sval_shift, s->d_sc, s->d_sigma, sh->a_hist, sh->b_hist, sh->w_hist, sh->ratio, sh->pi,
                     sh->eta, sh->zeta, sh->done, sh->conv_k, sh->act_list, sh->lslot, sh->coef, sh->sw_k,
                     sh->rr_hist, sh->sw_seed, sh->act_hist, sh->partials, sh->counters, s->d_b, s->d_res, s->d_dot, s->d_rold,
                     s->d_qcopy, s->tc_ws, s->d_tc_err};
