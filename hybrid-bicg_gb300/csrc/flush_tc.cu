@@ -16,9 +16,9 @@
 // The epilogue joins the nine exact diagonal sums in 64-bit integer arithmetic
 // (keeping floor(T / 2^12) of the 75-bit sum T: the dropped bits are below
 // 2^-56 of the row x element scale) and rounds once to FP64; only the
-// own-vector terms use the FP64 pipe.  (The
-// digit splitting is the error-free splitting of Ozaki, Ogita, Oishi and Rump
-// for matrix products, arranged here so that the exact sums fit TMEM.)
+// own-vector terms use the FP64 pipe.  (The digit splitting is the error-free
+// splitting of Ozaki, Ogita, Oishi and Rump for matrix products, arranged here
+// so that the exact sums fit TMEM.)
 //
 // One CTA per SM (203 KB of shared memory), persistent over tiles of 48
 // vector elements (one panel of the panel-major x_j and p_j arrays, whose
