@@ -421,9 +421,10 @@ def run_reference(args, dist: Dist):
     vals = []
     info = None
     prof = load_profile(args.workload, f) if args.scale is None else None
-    for i in range(max(1, min(args.warmup, 1)) + args.steps):
+    warm = max(1, args.warmup)
+    for i in range(warm + args.steps):
         info = cpu_baseline(f, prof)
-        if i >= max(1, min(args.warmup, 1)):
+        if i >= warm:
             vals.append(info["value"])
     v = float(np.median(vals))
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": dist.world,
@@ -446,7 +447,7 @@ def run_batch_c4(args, dist: Dist):
     fams = pkg.workloads.batched_families(256)
     kw = dict(tol=1e-10, max_iter=10000, shift_mode=args.shift_mode, flush=args.flush, true_residuals=True,
               refine=not args.no_refine, basis_block=args.basis_block)
-    for _ in range(max(1, min(args.warmup, 1))):
+    for _ in range(max(1, args.warmup)):
         pkg.batch_solve(fams, workers=args.workers, **kw)
     walls, res = [], None
     with Clocks(dist.local) as clk:
