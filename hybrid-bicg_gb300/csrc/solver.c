@@ -1562,8 +1562,26 @@ static void *touch_pages(void *arg) {
     return NULL;
 }
 
+/* host scratch of one solve, freed by the caller on every return path */
+typedef struct {
+    double *h_sigma, *h_res;
+    int *act, *sw_k, *sw_seed, *conv;
+    unsigned char *fixed;
+} run_host_t;
+
+static void run_host_free(run_host_t *hb) {
+    free(hb->h_sigma);
+    free(hb->h_res);
+    free(hb->act);
+    free(hb->sw_k);
+    free(hb->sw_seed);
+    free(hb->conv);
+    free(hb->fixed);
+    memset(hb, 0, sizeof *hb);
+}
+
 static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma, int seed, int in_where, double *x,
-                           double *r_out, int out_where, hbicg_stats *stats, touch_t *touch);
+                           double *r_out, int out_where, hbicg_stats *stats, touch_t *touch, run_host_t *hb);
 
 /* params.refine: true residuals of every shift; a shift above tol gets
  * x_j += e with (A + sigma_j I) e = b - (A + sigma_j I) x_j solved (single
@@ -1625,13 +1643,17 @@ static int refine_shifts(hbicg_solver *s, const double *h_sigma, int *refined, u
     return rc;
 }
 
-/* the page-touching helper is joined on every return path of the solve */
+/* the page-touching helper is joined, and the host scratch freed, on every
+ * return path of the solve */
 int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int seed, int in_where, double *x,
                      double *r_out, int out_where, hbicg_stats *stats) {
     touch_t touch;
     memset(&touch, 0, sizeof touch);
-    const int rc = solver_run_impl(s, b, sigma, seed, in_where, x, r_out, out_where, stats, &touch);
+    run_host_t hb;
+    memset(&hb, 0, sizeof hb);
+    const int rc = solver_run_impl(s, b, sigma, seed, in_where, x, r_out, out_where, stats, &touch, &hb);
     touch_join(&touch);
+    run_host_free(&hb);
     /* no copy into the caller's buffer outlives the call, whatever path returned */
     if (s->early_pending) cudaStreamSynchronize(s->ctx->cstream);
     s->early_x = NULL;
@@ -1642,7 +1664,7 @@ int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int 
 }
 
 static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma, int seed, int in_where, double *x,
-                           double *r_out, int out_where, hbicg_stats *stats, touch_t *touch) {
+                           double *r_out, int out_where, hbicg_stats *stats, touch_t *touch, run_host_t *hb) {
     hbicg_context *ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     const unsigned n = s->A->k.n;
@@ -1653,8 +1675,14 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
     }
     const enum cudaMemcpyKind kin = in_where == HBICG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     const enum cudaMemcpyKind kout = out_where == HBICG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    double *h_sigma = malloc(sizeof(double) * (m > 0 ? m : 1));
-    int *act = calloc((size_t)s->kcap + 1, sizeof(int));
+    double *h_sigma = hb->h_sigma = malloc(sizeof(double) * (m > 0 ? m : 1));
+    int *act = hb->act = calloc((size_t)s->kcap + 1, sizeof(int));
+    int *sw_k = hb->sw_k = calloc(m > 0 ? m : 1, sizeof(int)), *sw_seed = hb->sw_seed = calloc(m > 0 ? m : 1, sizeof(int));
+    int *conv = hb->conv = calloc(m > 0 ? m : 1, sizeof(int));
+    if (!h_sigma || !act || !sw_k || !sw_seed || !conv) {
+        set_msg("host scratch of %d shifts and %d iterations", m, s->kcap);
+        return HBICG_E_NOMEM;
+    }
     if (m > 0) {
         if (in_where == HBICG_DEVICE) CUDA_TRY(cudaMemcpyAsync(h_sigma, sigma, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
         else memcpy(h_sigma, sigma, sizeof(double) * m);
@@ -1695,8 +1723,6 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
     double flush_ms = 0.0;
     s->flush_bytes = 0.0;
     int k = 1, n_sw = 0, final_seed = seed, status = HBICG_OK;
-    int *sw_k = calloc(m > 0 ? m : 1, sizeof(int)), *sw_seed = calloc(m > 0 ? m : 1, sizeof(int));
-    int *conv = calloc(m > 0 ? m : 1, sizeof(int));
     const double *r_final = NULL;
     if (s->p.form == HBICG_FORM_PLAIN) {
         plain_out o;
@@ -1739,7 +1765,7 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
     /* copies issued during the solve finish before anything rewrites X */
     if (s->early_pending) CUDA_TRY(cudaStreamSynchronize(ctx->cstream));
     int refined = 0;
-    unsigned char *fixed = s->early_x ? calloc((size_t)m, 1) : NULL;
+    unsigned char *fixed = hb->fixed = s->early_x ? calloc((size_t)m, 1) : NULL;
     /* only after a converged solve: a solve stopped by max_iter or a breakdown
      * keeps its x as the reference leaves it */
     if (rc == HBICG_OK && status == HBICG_OK && s->p.refine && m > 0 && k < s->kcap) {
@@ -1759,7 +1785,6 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
                                        kout, st));
         }
     }
-    free(fixed);
     if (rc == HBICG_OK && r_out && r_final) CUDA_TRY(cudaMemcpyAsync(r_out, r_final, sizeof(double) * n, kout, st));
     double maxres = 0.0;
     double *h_res = NULL;
@@ -1767,7 +1792,10 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
         HBK_TRY(hbk_true_residuals(&s->A->k, s->v.X, s->d_b, s->d_sigma, m, s->sh.partials, s->sh.counters + 16,
                                    s->d_res, st));
         HBK_TRY(hbk_dot(n, s->d_b, s->d_b, s->sh.partials, s->sh.counters + 7, s->d_dot, st));
-        h_res = malloc(sizeof(double) * m);
+        if (!(h_res = hb->h_res = malloc(sizeof(double) * m))) {
+            set_msg("host scratch of %d residuals", m);
+            return HBICG_E_NOMEM;
+        }
         CUDA_TRY(cudaMemcpyAsync(h_res, s->d_res, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaMemcpyAsync(ctx->h_dbl, s->d_dot, sizeof(double), cudaMemcpyDeviceToHost, st));
     }
@@ -1815,12 +1843,6 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
             if (stats->seed_rr) cudaMemcpy(stats->seed_rr, s->sh.rr_hist, sizeof(double) * nk, cudaMemcpyDeviceToHost);
         }
     }
-    free(h_res);
-    free(h_sigma);
-    free(act);
-    free(sw_k);
-    free(sw_seed);
-    free(conv);
     if (rc) return rc;
     return status;
 }
