@@ -81,6 +81,27 @@ const char *hbicg_status_string(int s) {
         }                                                                                                \
     } while (0)
 
+/* the same two checks for functions that own host or device scratch: set rc
+ * and leave through their `out:` cleanup */
+#define CUDA_GOTO(call)                                                                                  \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess) {                                                                         \
+            set_msg("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));                  \
+            rc = e_ == cudaErrorMemoryAllocation ? HBICG_E_NOMEM : HBICG_E_CUDA;                         \
+            goto out;                                                                                    \
+        }                                                                                                \
+    } while (0)
+#define HBK_GOTO(call)                                                                                   \
+    do {                                                                                                 \
+        int e_ = (call);                                                                                 \
+        if (e_) {                                                                                        \
+            set_msg("%s:%d %s: %s", __FILE__, __LINE__, #call, hbk_error_string(e_));                    \
+            rc = HBICG_E_CUDA;                                                                           \
+            goto out;                                                                                    \
+        }                                                                                                \
+    } while (0)
+
 static size_t ld_of(unsigned n) { return ((size_t)n + 31) / 32 * 32; }
 
 void hbicg_params_default(hbicg_params *p) {
@@ -313,37 +334,39 @@ static int build_sell(hbicg_matrix *A, const unsigned *h_ptr, unsigned n, unsign
     if (env && !strcmp(env, "sell")) want = maxlen <= HBK_SELL_MAX_LEN;
     if (!want || !n) return HBICG_OK;
     const unsigned ns = (n + 31) / 32;
+    int rc = HBICG_OK;
     unsigned *d_w = NULL, *h_w = malloc(sizeof(unsigned) * ns);
     unsigned long long *h_sp = malloc(sizeof(unsigned long long) * ((size_t)ns + 1));
-    if (!h_w || !h_sp) return HBICG_E_NOMEM;
-    CUDA_TRY(cudaMalloc((void **)&d_w, sizeof(unsigned) * ns));
-    HBK_TRY(hbk_sell_widths(n, A->d_ptr, d_w, st));
-    CUDA_TRY(cudaMemcpyAsync(h_w, d_w, sizeof(unsigned) * ns, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    cudaFree(d_w);
+    if (!h_w || !h_sp) {
+        rc = HBICG_E_NOMEM;
+        goto out;
+    }
+    CUDA_GOTO(cudaMalloc((void **)&d_w, sizeof(unsigned) * ns));
+    HBK_GOTO(hbk_sell_widths(n, A->d_ptr, d_w, st));
+    CUDA_GOTO(cudaMemcpyAsync(h_w, d_w, sizeof(unsigned) * ns, cudaMemcpyDeviceToHost, st));
+    CUDA_GOTO(cudaStreamSynchronize(st));
     h_sp[0] = 0;
     for (unsigned i = 0; i < ns; i++) h_sp[i + 1] = h_sp[i] + 32ull * h_w[i];
     const unsigned long long padded = h_sp[ns];
-    free(h_w);
-    if (!env && (double)padded > 1.34 * (double)nnz + 4096.0) {
-        free(h_sp);
-        return HBICG_OK;
-    }
-    CUDA_TRY(cudaMalloc((void **)&A->d_sptr, sizeof(unsigned long long) * ((size_t)ns + 1)));
-    CUDA_TRY(cudaMalloc((void **)&A->d_sval, sizeof(double) * (padded + 1)));
-    CUDA_TRY(cudaMalloc((void **)&A->d_scol, sizeof(unsigned) * (padded + 1)));
-    CUDA_TRY(cudaMemcpyAsync(A->d_sptr, h_sp, sizeof(unsigned long long) * ((size_t)ns + 1), cudaMemcpyHostToDevice,
-                             st));
-    HBK_TRY(hbk_sell_fill(n, A->d_ptr, A->d_col, A->d_val, A->d_sptr, A->d_sval, A->d_scol, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    free(h_sp);
+    if (!env && (double)padded > 1.34 * (double)nnz + 4096.0) goto out; /* too much padding: not SELL-32 */
+    CUDA_GOTO(cudaMalloc((void **)&A->d_sptr, sizeof(unsigned long long) * ((size_t)ns + 1)));
+    CUDA_GOTO(cudaMalloc((void **)&A->d_sval, sizeof(double) * (padded + 1)));
+    CUDA_GOTO(cudaMalloc((void **)&A->d_scol, sizeof(unsigned) * (padded + 1)));
+    CUDA_GOTO(cudaMemcpyAsync(A->d_sptr, h_sp, sizeof(unsigned long long) * ((size_t)ns + 1), cudaMemcpyHostToDevice,
+                              st));
+    HBK_GOTO(hbk_sell_fill(n, A->d_ptr, A->d_col, A->d_val, A->d_sptr, A->d_sval, A->d_scol, st));
+    CUDA_GOTO(cudaStreamSynchronize(st));
     A->k.fmt = HBK_FMT_SELL;
     A->k.sval = A->d_sval;
     A->k.scol = A->d_scol;
     A->k.sptr = A->d_sptr;
     A->k.sell_len = padded;
     A->diag_state = 0; /* a new SELL-32 layout */
-    return HBICG_OK;
+out:
+    cudaFree(d_w);
+    free(h_w);
+    free(h_sp);
+    return rc;
 }
 
 /* diagonal positions of the SELL-32 form (computed once per layout) */
@@ -939,22 +962,23 @@ static int early_copies(hbicg_solver *s, int k_flushed, int *launches) {
     cudaStream_t st = s->ctx->stream;
     const int m = s->m;
     const unsigned n = s->A->k.n;
+    int rc = HBICG_OK, any = 0;
     int *conv = malloc(sizeof(int) * (size_t)(m > 0 ? m : 1));
     if (!conv) return HBICG_E_NOMEM;
-    CUDA_TRY(cudaMemcpyAsync(conv, s->sh.conv_k, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    int any = 0;
+    CUDA_GOTO(cudaMemcpyAsync(conv, s->sh.conv_k, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost, st));
+    CUDA_GOTO(cudaStreamSynchronize(st));
     for (int j = 0; j < m; ++j) {
         s->early[j] = s->early[j] ? 1 : 0;
         if (!s->early[j] && conv[j] > 0 && conv[j] <= k_flushed) {
-            HBK_TRY(hbk_panel_row(s->v.Xp, s->v.pm, n, j, s->v.X + (size_t)j * s->ld, st));
+            HBK_GOTO(hbk_panel_row(s->v.Xp, s->v.pm, n, j, s->v.X + (size_t)j * s->ld, st));
             ++*launches;
             s->early[j] = 2; /* written this time: copy below */
             any = 1;
         }
     }
+out:
     free(conv);
-    if (!any) return HBICG_OK;
+    if (rc || !any) return rc;
     CUDA_TRY(cudaEventRecord(s->ctx->cev, st));
     CUDA_TRY(cudaStreamWaitEvent(s->ctx->cstream, s->ctx->cev, 0));
     for (int j = 0; j < m; ++j)
@@ -1595,23 +1619,23 @@ static int refine_shifts(hbicg_solver *s, const double *h_sigma, int *refined, u
     hbicg_solver *sub = NULL;
     int rc = HBICG_OK;
     if (!h) return HBICG_E_NOMEM;
-    HBK_TRY(hbk_dot(n, s->d_b, s->d_b, s->sh.partials, s->sh.counters + 7, s->d_dot, st));
-    CUDA_TRY(cudaMemcpyAsync(s->ctx->h_dbl, s->d_dot, sizeof(double), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
+    HBK_GOTO(hbk_dot(n, s->d_b, s->d_b, s->sh.partials, s->sh.counters + 7, s->d_dot, st));
+    CUDA_GOTO(cudaMemcpyAsync(s->ctx->h_dbl, s->d_dot, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_GOTO(cudaStreamSynchronize(st));
     const double bn = sqrt(s->ctx->h_dbl[0]);
     for (int round = 0; round < 3 && rc == HBICG_OK && bn > 0.0; ++round) {
-        HBK_TRY(hbk_true_residuals(&s->A->k, s->v.X, s->d_b, s->d_sigma, m, s->sh.partials, s->sh.counters + 16,
+        HBK_GOTO(hbk_true_residuals(&s->A->k, s->v.X, s->d_b, s->d_sigma, m, s->sh.partials, s->sh.counters + 16,
                                    s->d_res, st));
-        CUDA_TRY(cudaMemcpyAsync(h, s->d_res, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(cudaStreamSynchronize(st));
+        CUDA_GOTO(cudaMemcpyAsync(h, s->d_res, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, st));
+        CUDA_GOTO(cudaStreamSynchronize(st));
         int any = 0;
         for (int j = 0; j < m && rc == HBICG_OK; ++j) {
             const double res = sqrt(h[j]) / bn;
             if (res <= s->p.tol) continue;
             any = 1;
             if (!r) {
-                CUDA_TRY(cudaMalloc((void **)&r, sizeof(double) * ((size_t)n + 1)));
-                CUDA_TRY(cudaMalloc((void **)&e, sizeof(double) * ((size_t)n + 1)));
+                CUDA_GOTO(cudaMalloc((void **)&r, sizeof(double) * ((size_t)n + 1)));
+                CUDA_GOTO(cudaMalloc((void **)&e, sizeof(double) * ((size_t)n + 1)));
             }
             if (!sub) {
                 hbicg_params p1 = s->p;
@@ -1621,21 +1645,22 @@ static int refine_shifts(hbicg_solver *s, const double *h_sigma, int *refined, u
                 if ((rc = hbicg_solver_create(s->ctx, s->A, 1, &p1, &sub)) != HBICG_OK) break;
             }
             double *xj = s->v.X + (size_t)j * ld;
-            HBK_TRY(hbk_spmv(&s->A->k, xj, e, h_sigma[j], 1, st)); /* e = (A + sigma_j I) x_j */
-            HBK_TRY(hbk_copy(n, s->d_b, r, st));
-            HBK_TRY(hbk_axpy(n, -1.0, e, r, st));                   /* r = b - e */
+            HBK_GOTO(hbk_spmv(&s->A->k, xj, e, h_sigma[j], 1, st)); /* e = (A + sigma_j I) x_j */
+            HBK_GOTO(hbk_copy(n, s->d_b, r, st));
+            HBK_GOTO(hbk_axpy(n, -1.0, e, r, st));                   /* r = b - e */
             sub->p.tol = isfinite(res) ? 0.5 * s->p.tol / res : s->p.tol;
             const int sr = hbicg_solver_run(sub, r, s->d_sigma + j, 0, HBICG_DEVICE, e, NULL, HBICG_DEVICE, NULL);
             if (sr != HBICG_OK && sr != HBICG_E_MAXITER) {
                 rc = sr;
                 break;
             }
-            HBK_TRY(hbk_axpy(n, 1.0, e, xj, st));
+            HBK_GOTO(hbk_axpy(n, 1.0, e, xj, st));
             ++*refined;
             if (fixed) fixed[j] = 1;
         }
         if (!any) break;
     }
+out:
     hbicg_solver_destroy(sub);
     cudaFree(r);
     cudaFree(e);
