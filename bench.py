@@ -626,6 +626,20 @@ def run_spmv_kernel(args):
                              "frac": byt / (ms * 1e-3) / 1e9 / hbm}
     A.set_format(default)
     A.close()
+    if args.row_classes:
+        # the same matrix with the rows of one length class emptied, default form
+        ptr = f.a.ptr.astype(np.int64)
+        lens = np.diff(ptr)
+        rowlen = np.repeat(lens, lens)
+        out["row_classes"] = {}
+        for name, keep in (("rows_le_32", rowlen <= 32), ("rows_gt_32", rowlen > 32)):
+            nl = np.bincount(np.repeat(np.arange(n), lens)[keep], minlength=n)
+            p = np.zeros(n + 1, dtype=np.int64)
+            np.cumsum(nl, out=p[1:])
+            B = pkg.Matrix(ctx, p.astype(np.uint32), f.a.col[keep], f.a.val[keep])
+            ms = min(B.time_spmv(x, y, 0.1, iters=max(args.steps, 1)) for _ in range(3))
+            out["row_classes"][name] = {"nnz": int(keep.sum()), "format": B.format, "ms_per_launch": ms}
+            B.close()
     ctx.close()
     return out
 
@@ -746,6 +760,8 @@ def main(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-refine", action="store_true", help="keep the reference's x (no true-residual correction)")
+    ap.add_argument("--row-classes", action="store_true",
+                    help="--kernel spmv: also time the matrix with its rows of <= 32 / > 32 entries emptied")
     ap.add_argument("--kernel", default=None, choices=["flush", "spmv", "coo2csr", "mmread"],
                     help="time one kernel alone on random data instead of the solve")
     ap.add_argument("--n", type=int, default=2097152, help="elements for --kernel")

@@ -56,6 +56,7 @@ typedef struct {
     const unsigned long long *sptr; /* SELL: n/32 rounded up + 1 slice offsets; HYB: nslice + 1 */
     unsigned long long sell_len;    /* SELL: entries of sval/scol (with padding) */
     const unsigned *srow;      /* HYB: row of slice s, lane l at 32 s + l (>= n: an empty lane) */
+    const unsigned char *slen; /* HYB: length of that row (0: an empty lane) */
     unsigned nslice;           /* HYB: slices of short rows */
     const unsigned *wrow;      /* HYB: rows longer than HBK_HYB_SHORT, longest first, one warp each */
     unsigned nwrow;

@@ -213,7 +213,7 @@ __device__ __forceinline__ void spmv_rows_hyb(const hbk_matrix &A, const double 
             const unsigned long long base = __ldg(A.sptr + s);
             const unsigned w = (unsigned)((__ldg(A.sptr + s + 1) - base) >> 5);
             const unsigned r = __ldg(A.srow + 32 * (size_t)s + lane);
-            const unsigned len = r < A.n ? __ldg(A.ptr + r + 1) - __ldg(A.ptr + r) : 0;
+            const unsigned len = __ldg(A.slen + 32 * (size_t)s + lane);
             const double *__restrict__ vv = A.sval + base + lane;
             const unsigned *__restrict__ cc = A.scol + base + lane;
             double acc = 0.0;

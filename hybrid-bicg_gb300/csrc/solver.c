@@ -195,7 +195,8 @@ struct hbicg_matrix {
     int diag_state;
     /* HYB form (hbk.h HBK_FMT_HYB) */
     double *d_hval;
-    unsigned *d_hcol, *d_srow, *d_wrow;
+    unsigned *d_hcol, *d_srow, *d_wrow; /* d_srow: lane -> row map, then the lanes' row lengths (bytes) */
+    size_t slen_off;                    /* entries of the map before the lengths */
     unsigned long long *d_hsptr;
     unsigned nslice, nwrow;
 };
@@ -211,7 +212,9 @@ static int cmp_u64(const void *a, const void *b) {
  * warp writes stay inside one window; each window's list is padded to whole
  * slices with empty lanes.  Longer rows go to a list, longest first, one warp
  * each.  For power-law row lengths (most rows short, a few thousands long),
- * where a thread per row leaves most lanes of a warp idle. */
+ * where a thread per row leaves most lanes of a warp idle.  The lengths of the
+ * slice rows are kept as bytes after the lane -> row map, so that a warp reads
+ * its 32 lengths in one line instead of 64 scattered row pointers. */
 static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
     cudaStream_t st = A->ctx->stream;
     if (!n || A->d_hval) return HBICG_OK;
@@ -228,7 +231,9 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
         cap += (cnt + 31) / 32 * 32;
     }
     const size_t ns = cap / 32;
-    unsigned *srow = malloc(sizeof(unsigned) * (cap + 1));
+    /* lane -> row map (cap + 1 entries), then the lanes' row lengths as bytes */
+    const size_t srow_bytes = sizeof(unsigned) * (cap + 1) + cap + 1;
+    unsigned *srow = malloc(srow_bytes);
     unsigned long long *wkey = malloc(sizeof(unsigned long long) * (nw + 1));
     unsigned *wrow = malloc(sizeof(unsigned) * (nw + 1));
     unsigned long long *sp = malloc(sizeof(unsigned long long) * (ns + 1));
@@ -261,6 +266,9 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
             o += acc;
             while (o % 32) srow[o++] = 0xFFFFFFFFu; /* empty lane */
         }
+        unsigned char *slen = (unsigned char *)(srow + cap + 1);
+        for (size_t i = 0; i < cap; ++i)
+            slen[i] = srow[i] < n ? (unsigned char)(h_ptr[srow[i] + 1] - h_ptr[srow[i]]) : 0;
         qsort(wkey, nw, sizeof *wkey, cmp_u64);
         for (size_t i = 0; i < nw; ++i) wrow[i] = (unsigned)(wkey[i] & 0xFFFFFFFFu);
         sp[0] = 0;
@@ -285,10 +293,10 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
     HTRY(cudaMalloc((void **)&A->d_hsptr, sizeof(unsigned long long) * (ns + 1)));
     HTRY(cudaMalloc((void **)&A->d_hval, sizeof(double) * (sp[ns] + 1)));
     HTRY(cudaMalloc((void **)&A->d_hcol, sizeof(unsigned) * (sp[ns] + 1)));
-    HTRY(cudaMalloc((void **)&A->d_srow, sizeof(unsigned) * (cap + 1)));
+    HTRY(cudaMalloc((void **)&A->d_srow, srow_bytes));
     HTRY(cudaMalloc((void **)&A->d_wrow, sizeof(unsigned) * (nw + 1)));
     HTRY(cudaMemcpyAsync(A->d_hsptr, sp, sizeof(unsigned long long) * (ns + 1), cudaMemcpyHostToDevice, st));
-    if (cap) HTRY(cudaMemcpyAsync(A->d_srow, srow, sizeof(unsigned) * cap, cudaMemcpyHostToDevice, st));
+    if (cap) HTRY(cudaMemcpyAsync(A->d_srow, srow, srow_bytes, cudaMemcpyHostToDevice, st));
     if (nw) HTRY(cudaMemcpyAsync(A->d_wrow, wrow, sizeof(unsigned) * nw, cudaMemcpyHostToDevice, st));
     {
         const int e = hbk_hyb_fill((unsigned)ns, A->d_srow, n, A->d_ptr, A->d_col, A->d_val, A->d_hsptr, A->d_hval,
@@ -299,6 +307,7 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
 #undef HTRY
     A->nslice = (unsigned)ns;
     A->nwrow = (unsigned)nw;
+    A->slen_off = cap + 1;
 done:
     free(srow);
     free(wkey);
@@ -314,6 +323,7 @@ static void use_hyb(hbicg_matrix *A) {
     A->k.scol = A->d_hcol;
     A->k.sptr = A->d_hsptr;
     A->k.srow = A->d_srow;
+    A->k.slen = A->d_srow ? (const unsigned char *)(A->d_srow + A->slen_off) : NULL;
     A->k.wrow = A->d_wrow;
     A->k.nslice = A->nslice;
     A->k.nwrow = A->nwrow;
@@ -869,6 +879,7 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
         A->d_srow = NULL;
         A->d_wrow = NULL;
         A->k.srow = NULL;
+        A->k.slen = NULL;
         A->k.wrow = NULL;
         A->k.nslice = 0;
         A->k.nwrow = 0;
