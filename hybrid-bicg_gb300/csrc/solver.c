@@ -814,9 +814,15 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
         /* time both forms of y = A x (10 launches each after a warm-up) */
         const size_t n = A->k.n ? A->k.n : 1;
         double *x = NULL, *y = NULL;
-        CUDA_TRY(cudaMalloc((void **)&x, sizeof(double) * n));
-        CUDA_TRY(cudaMalloc((void **)&y, sizeof(double) * n));
-        CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, A->ctx->stream));
+        cudaError_t e = cudaMalloc((void **)&x, sizeof(double) * n);
+        if (!e) e = cudaMalloc((void **)&y, sizeof(double) * n);
+        if (!e) e = cudaMemsetAsync(x, 0, sizeof(double) * n, A->ctx->stream);
+        if (e) {
+            cudaFree(x);
+            cudaFree(y);
+            set_msg("autotune buffers: %s", cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? HBICG_E_NOMEM : HBICG_E_CUDA;
+        }
         int rc = hbicg_matrix_set_format(A, HBICG_SPMV_TILE);
         if (!rc) rc = hbicg_matrix_time_spmv(A, x, y, 0.0, 10, &t_tile);
         double t_s = -1.0, t_h = -1.0;

@@ -123,20 +123,26 @@ int hbicg_matrix_spmv(hbicg_matrix *A, const double *x, double *y, double sigma,
  * x, y) between CUDA events on the context's stream; *ms = mean per launch. */
 int hbicg_matrix_time_spmv(hbicg_matrix *A, const double *x, double *y, double sigma, int iters, double *ms);
 
-/* SpMV form of a matrix: CSR row blocks, or SELL-32 (slices of 32 rows padded
- * to their longest row; rows of at most 64 entries). */
+/* SpMV form of a matrix: CSR row blocks staged in shared memory (TILE);
+ * SELL-32, slices of 32 consecutive rows padded to their longest row (rows of
+ * at most 64 entries, padding under a third of the nonzeros); or HYB, rows of
+ * at most 32 entries in SELL-32 slices sorted by length inside windows of 256
+ * rows and longer rows one warp each.  A new matrix takes SELL-32 where it
+ * qualifies, else HYB. */
 typedef enum { HBICG_SPMV_TILE = 0, HBICG_SPMV_SELL = 1, HBICG_SPMV_HYB = 2 } hbicg_spmv_format;
 int hbicg_matrix_format(const hbicg_matrix *A);
-/* Switch the SpMV form (builds the SELL-32 copy if needed; HBICG_E_ARG when a
- * row is too long for it).  Call before creating solvers on A. */
+/* Switch the SpMV form (builds that form's copy if needed; HBICG_E_ARG when a
+ * row is too long for SELL-32).  Call before creating solvers on A. */
 int hbicg_matrix_set_format(hbicg_matrix *A, int fmt);
 /* Autotuner: the pattern's signature (log2 n, longest row, share of rows per
- * power-of-two length class) is looked up in the cache file; if absent, both
- * forms are timed (10 products each) and the faster is appended to the cache.
- * The matrix is left in the chosen form.  Cache format (text, one entry per
- * line after a '#' header): "<signature> <tile|sell> <tile_ms> <sell_ms>"
- * (sell_ms < 0 when there is no SELL form).  cache_path NULL: time, no cache.
- * chosen/tile_ms/sell_ms may be NULL.  Call before creating solvers on A. */
+ * power-of-two length class) is looked up in the cache file; if absent, every
+ * form the matrix has is timed (10 products each) and the fastest is appended
+ * to the cache.  The matrix is left in the chosen form and the copies of the
+ * other packed forms are freed.  Cache format (text, one entry per line after
+ * a '#' header): "<signature> <tile|sell|hyb> <tile_ms> <packed_ms>", where
+ * packed_ms is the SELL-32 time, or the HYB time when HYB was chosen or there
+ * is no SELL-32 form.  cache_path NULL: time, no cache.  chosen/tile_ms/sell_ms
+ * (the packed time) may be NULL.  Call before creating solvers on A. */
 int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, double *tile_ms, double *sell_ms);
 
 /* Coordinate (triplet) matrix in host memory, 0-based, as read from a file. */
