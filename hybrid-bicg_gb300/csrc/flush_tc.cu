@@ -101,11 +101,6 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
     return d;
 }
 
-// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major,
-// N >> 3 at bits 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
-                           ((uint32_t)(TC_M >> 4) << 24);
-
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
@@ -525,6 +520,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
 #pragma unroll
                         for (int part = 0; part * 256 < ntot; ++part) {
                             const int nn = ntot - part * 256 < 256 ? ntot - part * 256 : 256;
+                            // kind::f16 instruction descriptor: D = F32, A = B = BF16, both
+                            // K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
                             const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nn >> 3) << 17) |
                                                    ((uint32_t)(TC_M >> 4) << 24);
                             // start-address field: (offset >> 4) adds without carry (smem < 256 KB)
@@ -562,7 +559,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
         const bool store = live && (which == 0 || a.keep_p);
         const int E = s_rowexp[r];
         const double own = s_rown[r];
-        double *const prim = which ? a.Pmat : a.X;  // the row this lane loads and writes
         const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(cg * EPI_COLS);
         // this lane's piece of a panel (system j, columns 16 cg .. 16 cg + 15):
         // x rows in X, p rows in Pmat; consecutive panels m * 48 values apart
