@@ -14,12 +14,7 @@
 
 #include <cuda_runtime.h>
 
-#include "hbicg.h"
-#include "hbk.h"
-
-const hbk_matrix *hbicg__matrix_kernel_view(const hbicg_matrix *A);
-hbicg_context *hbicg__matrix_context(const hbicg_matrix *A);
-void hbicg__set_message(const char *msg);
+#include "host_internal.h"
 
 #define CK(call)                                                   \
     do {                                                           \

@@ -18,11 +18,8 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include "hbicg.h"
+#include "host_internal.h"
 #include "matrix.h"
-
-int hbicg__host_spmv(unsigned rows, unsigned cols, unsigned nnz, const unsigned *ptr, const unsigned *col,
-                     const double *val, const double *x, double *y, int accumulate);
 
 static void die(const char *msg) {
     fprintf(stderr, "%s", msg);

@@ -31,9 +31,7 @@
 #include <sys/stat.h>
 #include <unistd.h>
 
-#include "hbicg.h"
-
-void hbicg__set_message(const char *msg);
+#include "host_internal.h"
 
 static void msgf(const char *fmt, ...) {
     char buf[512];
