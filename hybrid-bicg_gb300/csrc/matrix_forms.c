@@ -740,19 +740,20 @@ int hbicg__host_spmv(unsigned rows, unsigned cols, unsigned nnz, const unsigned 
     if (rc) return rc;
     cudaStream_t st = g_host_ctx->stream;
     double *dx = NULL, *dy = NULL;
-    CUDA_TRY(cudaMalloc((void **)&dx, sizeof(double) * ((size_t)cols + 1)));
-    CUDA_TRY(cudaMalloc((void **)&dy, sizeof(double) * ((size_t)rows + 1)));
-    if (cols) CUDA_TRY(cudaMemcpyAsync(dx, x, sizeof(double) * cols, cudaMemcpyHostToDevice, st));
+    CUDA_GOTO(cudaMalloc((void **)&dx, sizeof(double) * ((size_t)cols + 1)));
+    CUDA_GOTO(cudaMalloc((void **)&dy, sizeof(double) * ((size_t)rows + 1)));
+    if (cols) CUDA_GOTO(cudaMemcpyAsync(dx, x, sizeof(double) * cols, cudaMemcpyHostToDevice, st));
     if (accumulate) {
-        CUDA_TRY(cudaMemcpyAsync(dy, y, sizeof(double) * rows, cudaMemcpyHostToDevice, st));
-        HBK_TRY(hbk_spmv_accumulate(&A->k, dx, dy, st));
+        CUDA_GOTO(cudaMemcpyAsync(dy, y, sizeof(double) * rows, cudaMemcpyHostToDevice, st));
+        HBK_GOTO(hbk_spmv_accumulate(&A->k, dx, dy, st));
     } else {
-        HBK_TRY(hbk_spmv(&A->k, dx, dy, 0.0, 0, st));
+        HBK_GOTO(hbk_spmv(&A->k, dx, dy, 0.0, 0, st));
     }
-    CUDA_TRY(cudaMemcpyAsync(y, dy, sizeof(double) * rows, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
+    CUDA_GOTO(cudaMemcpyAsync(y, dy, sizeof(double) * rows, cudaMemcpyDeviceToHost, st));
+    CUDA_GOTO(cudaStreamSynchronize(st));
+out:
     cudaFree(dx);
     cudaFree(dy);
     hbicg_matrix_destroy(A);
-    return HBICG_OK;
+    return rc;
 }
