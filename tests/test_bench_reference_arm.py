@@ -1,6 +1,7 @@
-"""The reference arm of bench.py on CPU: the reference's algorithm (the C
-restatement under oracle/) timed on the host cores, one JSON line in the
-bench contract, printed by rank 0 alone when launched with several ranks."""
+"""bench.py's host side on CPU: the reference arm (the reference's algorithm,
+the C restatement under oracle/, timed on the host cores) prints one JSON line
+in the bench contract, from rank 0 alone when launched with several ranks; the
+clocks object is read from nvidia-smi's sample lines."""
 import json
 import socket
 import subprocess
@@ -46,3 +47,23 @@ def test_reference_arm_two_ranks_rank0_prints():
     assert len(lines) == 1
     _check_line(lines[0])
     assert lines[0]["n_gpus"] == 2
+
+
+def test_clock_summary_reads_nvidia_smi_lines():
+    """The clocks object of a bench line: median SM clock under load, the
+    maximum, and every throttle reason seen active in any sample."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    c = bench.Clocks(0)
+    c.lines = [
+        "0, 2070, 2070, 900.1, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 1995, 2070, 1400.0, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "0, 1800, 2070, 1400.0, 0x0000000000000008, Active, Not Active, Not Active, Active",
+        "garbage line",
+        "0, [N/A], 2070, 1.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+    ]
+    s = c.summary()
+    assert s["sm_mhz"] == 1995.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 3
+    assert s["reasons"] == ["hw_slowdown", "sw_power_cap"]
+    assert bench.Clocks(0).summary() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
