@@ -383,7 +383,8 @@ def run_ours(args, dist: Dist):
         e2e_max, _ = aggregate(dist, e2e_s, 1.0)
         e2e = {"value": e2e_max, "unit": "s", "h2d_bytes_per_step": int(h_ptr.nbytes + h_col.nbytes + h_val.nbytes
                                                                           + h_b.nbytes + h_sig.nbytes),
-               "d2h_bytes_per_step": int(h_x.nbytes + h_r.nbytes), "api": "shifted_lopbicg_dynamic", "k": int(k)}
+               "d2h_bytes_per_step": int(h_x.nbytes + h_r.nbytes), "api": "shifted_lopbicg_dynamic", "k": int(k),
+               "calls_s": [round(t, 4) for t in e2e_times]}
 
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
