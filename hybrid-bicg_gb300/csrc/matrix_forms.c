@@ -727,14 +727,15 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
 /* Host-pointer product used by the matrix.h entry points: y (+)= A x with A
  * rows x cols.  Runs the CSR SpMV kernel on a process-wide context. */
 static hbicg_context *g_host_ctx = NULL;
+static pthread_mutex_t g_host_ctx_lock = PTHREAD_MUTEX_INITIALIZER;
 
 int hbicg__host_spmv(unsigned rows, unsigned cols, unsigned nnz, const unsigned *ptr, const unsigned *col,
                      const double *val, const double *x, double *y, int accumulate) {
     if (!rows) return HBICG_OK;
-    if (!g_host_ctx) {
-        int rc = hbicg_context_create(&g_host_ctx);
-        if (rc) return rc;
-    }
+    pthread_mutex_lock(&g_host_ctx_lock); /* created once, whichever thread calls first */
+    int crc = g_host_ctx ? HBICG_OK : hbicg_context_create(&g_host_ctx);
+    pthread_mutex_unlock(&g_host_ctx_lock);
+    if (crc) return crc;
     hbicg_matrix *A = NULL;
     int rc = hbicg_matrix_create(g_host_ctx, rows, nnz, ptr, col, val, HBICG_HOST, &A);
     if (rc) return rc;
