@@ -96,17 +96,29 @@ int hbicg_context_create(hbicg_context **out) {
     hbicg_context *c = calloc(1, sizeof *c);
     if (!c) return HBICG_E_NOMEM;
     c->refs = 1;
-    CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-    CUDA_TRY(cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking));
-    CUDA_TRY(cudaEventCreateWithFlags(&c->cev, cudaEventDisableTiming));
-    CUDA_TRY(cudaEventCreate(&c->ev0));
-    CUDA_TRY(cudaEventCreate(&c->ev1));
-    CUDA_TRY(cudaEventCreate(&c->evf0));
-    CUDA_TRY(cudaEventCreate(&c->evf1));
-    CUDA_TRY(cudaMallocHost((void **)&c->h_sc, sizeof(hbk_scalars)));
-    CUDA_TRY(cudaMallocHost((void **)&c->h_dbl, sizeof(double) * 64));
+    int rc = HBICG_OK;
+    CUDA_GOTO(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CUDA_GOTO(cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking));
+    CUDA_GOTO(cudaEventCreateWithFlags(&c->cev, cudaEventDisableTiming));
+    CUDA_GOTO(cudaEventCreate(&c->ev0));
+    CUDA_GOTO(cudaEventCreate(&c->ev1));
+    CUDA_GOTO(cudaEventCreate(&c->evf0));
+    CUDA_GOTO(cudaEventCreate(&c->evf1));
+    CUDA_GOTO(cudaMallocHost((void **)&c->h_sc, sizeof(hbk_scalars)));
+    CUDA_GOTO(cudaMallocHost((void **)&c->h_dbl, sizeof(double) * 64));
     *out = c;
     return HBICG_OK;
+out: /* release what was made before the failing call */
+    if (c->h_sc) cudaFreeHost(c->h_sc);
+    if (c->evf1) cudaEventDestroy(c->evf1);
+    if (c->evf0) cudaEventDestroy(c->evf0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->cev) cudaEventDestroy(c->cev);
+    if (c->cstream) cudaStreamDestroy(c->cstream);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    free(c);
+    return rc;
 }
 
 void hbicg_context_destroy(hbicg_context *c) {
