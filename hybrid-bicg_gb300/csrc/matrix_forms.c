@@ -311,6 +311,122 @@ out: /* on failure the partial matrix goes, its device arrays with it */
     *out = A;
     return HBICG_OK;
 }
+
+int hbicg_matrix_from_coo(hbicg_context *ctx, unsigned n, unsigned nnz, const unsigned *row, const unsigned *col,
+                          const double *val, int where, hbicg_matrix **out) {
+    if (!ctx || !out || (nnz && (!row || !col || !val))) return HBICG_E_ARG;
+    cudaStream_t st = ctx->stream;
+    unsigned *d_row = (unsigned *)row, *d_col = (unsigned *)col;
+    double *d_val = (double *)val;
+    unsigned *ptr = NULL, *colo = NULL;
+    double *valo = NULL;
+    void *tmp = NULL;
+    int *d_err = NULL, h_err = 0, rc = HBICG_OK;
+    cudaError_t e = cudaSuccess;
+#define FC(call)                                                                 \
+    do {                                                                         \
+        if ((e = (call)) != cudaSuccess) {                                       \
+            set_msg("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e)); \
+            rc = HBICG_E_CUDA;                                                   \
+            goto fail;                                                           \
+        }                                                                        \
+    } while (0)
+    if (where != HBICG_DEVICE) {
+        d_row = NULL;
+        d_col = NULL;
+        d_val = NULL;
+        FC(cudaMalloc((void **)&d_row, sizeof(unsigned) * ((size_t)nnz + 1)));
+        FC(cudaMalloc((void **)&d_col, sizeof(unsigned) * ((size_t)nnz + 1)));
+        FC(cudaMalloc((void **)&d_val, sizeof(double) * ((size_t)nnz + 1)));
+        if (nnz) {
+            FC(cudaMemcpyAsync(d_row, row, sizeof(unsigned) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+            FC(cudaMemcpyAsync(d_col, col, sizeof(unsigned) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+            FC(cudaMemcpyAsync(d_val, val, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+        }
+    }
+    FC(cudaMalloc((void **)&ptr, sizeof(unsigned) * ((size_t)n + 1)));
+    FC(cudaMalloc((void **)&colo, sizeof(unsigned) * ((size_t)nnz + 1)));
+    FC(cudaMalloc((void **)&valo, sizeof(double) * ((size_t)nnz + 1)));
+    FC(cudaMalloc(&tmp, hbk_coo_to_csr_tmp_bytes(nnz)));
+    FC(cudaMalloc((void **)&d_err, sizeof(int)));
+    FC(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+    FC((cudaError_t)hbk_coo_to_csr(n, nnz, d_row, d_col, d_val, ptr, colo, valo, tmp, d_err, st));
+    FC(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FC(cudaStreamSynchronize(st));
+    if (h_err) {
+        set_msg("a row or column index is >= n = %u", n);
+        rc = HBICG_E_ARG;
+        goto fail;
+    }
+    cudaFree(tmp);
+    cudaFree(d_err);
+    tmp = NULL;
+    d_err = NULL;
+    if (where != HBICG_DEVICE) {
+        cudaFree(d_row);
+        cudaFree(d_col);
+        cudaFree(d_val);
+    }
+    {
+        hbicg_matrix *A = NULL;
+        rc = hbicg_matrix_create(ctx, n, nnz, ptr, colo, valo, HBICG_DEVICE, &A);
+        if (rc != HBICG_OK) {
+            cudaFree(ptr);
+            cudaFree(colo);
+            cudaFree(valo);
+            return rc;
+        }
+        A->owns = 1;
+        *out = A;
+    }
+    return HBICG_OK;
+fail:
+    if (where != HBICG_DEVICE) {
+        cudaFree(d_row);
+        cudaFree(d_col);
+        cudaFree(d_val);
+    }
+    cudaFree(ptr);
+    cudaFree(colo);
+    cudaFree(valo);
+    cudaFree(tmp);
+    cudaFree(d_err);
+    return rc;
+#undef FC
+}
+
+int hbicg_matrix_get_csr(const hbicg_matrix *A, unsigned *ptr, unsigned *col, double *val, int where) {
+    if (!A) return HBICG_E_ARG;
+    cudaStream_t st = A->ctx->stream;
+    const enum cudaMemcpyKind kind = where == HBICG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const size_t n = A->k.n, nnz = A->k.nnz;
+    if (ptr) CUDA_TRY(cudaMemcpyAsync(ptr, A->d_ptr, sizeof(unsigned) * (n + 1), kind, st));
+    if (col && nnz) CUDA_TRY(cudaMemcpyAsync(col, A->d_col, sizeof(unsigned) * nnz, kind, st));
+    if (val && nnz) CUDA_TRY(cudaMemcpyAsync(val, A->d_val, sizeof(double) * nnz, kind, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return HBICG_OK;
+}
+
+int hbicg_matrix_load_mm(hbicg_context *ctx, const char *path, int expand_symmetric, hbicg_matrix **out) {
+    hbicg_coo c;
+    int rc = hbicg_mm_read(path, expand_symmetric, 0, &c);
+    if (rc != HBICG_OK) return rc;
+    if (c.rows != c.cols) {
+        set_msg("%s is %u x %u, not square", path, c.rows, c.cols);
+        hbicg_coo_free(&c);
+        return HBICG_E_NOT_SQUARE;
+    }
+    if (c.nnz > 0xFFFFFFFFull) {
+        set_msg("%s has %llu entries; at most 2^32 - 1 are supported", path, c.nnz);
+        hbicg_coo_free(&c);
+        return HBICG_E_ARG;
+    }
+    rc = hbicg_matrix_from_coo(ctx, c.rows, (unsigned)c.nnz, c.row, c.col, c.val, HBICG_HOST, out);
+    hbicg_coo_free(&c);
+    return rc;
+}
+
+/* frees a matrix whose creation failed before it took its context reference */
 static void hbicg_matrix_destroy_unretained(hbicg_matrix *A) {
     cudaStreamSynchronize(A->ctx->stream);
     if (A->owns) {
