@@ -593,10 +593,44 @@ def dropin_solve(variant: str, a, b, sigma, seed=0, tol=1e-12, max_iter=2000, sw
     return k, x, r
 
 
+def _check_noalloc_args(n: int, x, b, sigma, res) -> None:
+    """Shape, dtype, layout and device rules of true_residuals_noalloc."""
+    import torch
+
+    named = {"x": x, "b": b, "sigma": sigma, "res": res}
+    for name, t in named.items():
+        if not isinstance(t, torch.Tensor):
+            raise ValueError(f"{name} must be a torch tensor")
+        if t.dtype != torch.float64:
+            raise ValueError(f"{name} must be float64, got {t.dtype}")
+    if sigma.dim() != 1:
+        raise ValueError("sigma must be one-dimensional")
+    m = int(sigma.shape[0])
+    if x.dim() != 2 or int(x.shape[0]) != m:
+        raise ValueError(f"x must have shape (m, >= n) with m = {m}, got {tuple(x.shape)}")
+    if m and (int(x.shape[1]) < n or (int(x.shape[1]) > 1 and x.stride(1) != 1) or x.stride(0) < n):
+        raise ValueError(f"x must hold m rows of at least n = {n} values with unit inner stride")
+    for name, t, need in (("b", b, n), ("sigma", sigma, m), ("res", res, m)):
+        if t.numel() < need:
+            raise ValueError(f"{name} has {t.numel()} values, needs {need}")
+        if not t.is_contiguous():
+            raise ValueError(f"{name} must be contiguous")
+    for name, t in named.items():
+        if not t.is_cuda:
+            raise ValueError(f"{name} must be on a CUDA device")
+
+
 def true_residuals_noalloc(matrix: "Matrix", x, b, sigma, res, stream: int = 0) -> None:
     """hbicg_true_residuals_noalloc: res[j] = ||b - (A + sigma_j I) x_j|| / ||b||
     for device tensors x [m, ldx], b [n], sigma [m] and res [m], queued on
-    `stream` without allocating device memory (at most 64 shifts)."""
+    `stream` without allocating device memory (at most 64 shifts).
+
+    The arguments are checked here, before the call: float64 tensors on a CUDA
+    device, x two-dimensional with m rows of at least n values and unit inner
+    stride, b at least n values, sigma and res at least m values, each of b,
+    sigma and res contiguous.  A tensor that breaks a rule raises ValueError
+    instead of reaching the kernels, which would read or write past it."""
+    _check_noalloc_args(matrix.n, x, b, sigma, res)
     m = int(sigma.shape[0])
     ldx = int(x.stride(0)) if m else matrix.n
     _check(lib().hbicg_true_residuals_noalloc(matrix.h, _ptr(x), ldx, _ptr(b), _ptr(sigma), m, _ptr(res),

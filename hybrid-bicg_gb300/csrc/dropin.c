@@ -30,7 +30,15 @@ static int merged_csr(const CSR_Matrix *d, const CSR_Matrix *o, unsigned **ptr, 
     *ptr = malloc(sizeof(unsigned) * ((size_t)n + 1));
     *col = malloc(sizeof(unsigned) * ((size_t)nz + 1));
     *val = malloc(sizeof(double) * ((size_t)nz + 1));
-    if (!*ptr || !*col || !*val) return HBICG_E_NOMEM;
+    if (!*ptr || !*col || !*val) {
+        free(*ptr);
+        free(*col);
+        free(*val);
+        *ptr = NULL;
+        *col = NULL;
+        *val = NULL;
+        return HBICG_E_NOMEM;
+    }
     unsigned e = 0;
     (*ptr)[0] = 0;
     for (unsigned i = 0; i < n; i++) {

@@ -256,7 +256,8 @@ __global__ void k_flush_live(const int *__restrict__ conv_k, int m, int k_last, 
         const int j = base + (int)threadIdx.x;
         bool on = false;
         if (j < m) {
-            const int c = conv_k ? conv_k[j] : 0;
+            int c = conv_k ? conv_k[j] : 0;
+            c = c < 0 ? -c : c;  // a shift that broke down at k stopped there like a converged one
             on = c == 0 || c > k_last;
         }
         const unsigned b = __ballot_sync(0xffffffffu, on);

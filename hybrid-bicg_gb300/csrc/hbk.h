@@ -28,6 +28,7 @@ extern "C" {
 /* status bits (device and host) */
 #define HBK_ST_BREAKDOWN 1   /* a scalar of the recurrence became 0, inf or nan */
 #define HBK_ST_BASIS_FULL 2  /* deferred mode: the basis needs a flush */
+#define HBK_ST_SHIFT_FAIL 4  /* a non-seed shift broke down (its conv_k is -k) and stopped */
 
 /* SpMV row-block kinds (bits 30..31 of blk_row entries are not used; kinds
  * are a separate byte array) */
@@ -97,7 +98,7 @@ typedef struct {
     double *a_hist, *b_hist, *w_hist; /* [kcap] seed alpha / beta / omega history */
     double *pi;                 /* [m][kcap] */
     double *eta, *zeta;         /* [m] */
-    int *done, *conv_k;         /* [m] */
+    int *done, *conv_k;         /* [m]; conv_k: iteration of convergence, -k for a shift that broke down at k */
     int *act_list;              /* [m] shifts updated this iteration */
     double *coef;               /* [m][HBK_NCOEF] their coefficients */
     int *sw_k, *sw_seed;        /* [m] switch log */
@@ -157,6 +158,9 @@ int hbk_fill(unsigned n, double v, double *x, cudaStream_t st);
 /* deterministic dot: result written to *out (device), fixed summation tree */
 int hbk_dot(unsigned n, const double *x, const double *y, double *partials, unsigned *counter, double *out,
             cudaStream_t st);
+/* the same on at most grid_cap blocks (partials holds grid_cap doubles) */
+int hbk_dot_capped(unsigned n, const double *x, const double *y, int grid_cap, double *partials, unsigned *counter,
+                   double *out, cudaStream_t st);
 /* y = A x (+ sigma * x when sigma_add != 0), rows summed in stored order by one thread */
 int hbk_spmv(const hbk_matrix *A, const double *x, double *y, double sigma, int sigma_add, cudaStream_t st);
 /* y += A x (the reference's mult accumulates into y) */

@@ -268,6 +268,14 @@ int hbk_dot(unsigned n, const double *x, const double *y, double *partials, unsi
     return (int)cudaGetLastError();
 }
 
+int hbk_dot_capped(unsigned n, const double *x, const double *y, int grid_cap, double *partials, unsigned *counter,
+                   double *out, cudaStream_t st) {
+    int g = grid_for(n, 4);
+    if (grid_cap >= 1 && g > grid_cap) g = grid_cap;
+    k_dot<<<g, NT, 0, st>>>(n, x, y, partials, counter, out);
+    return (int)cudaGetLastError();
+}
+
 int hbk_spmv_grid(unsigned nblk) {
     int g = grid_for(nblk * (unsigned)NT, 1);
     return g < 1 ? 1 : g;

@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(NT) k_seed_y(Ctx c) {
 // (:278-303) and the seed switch (:312-359).
 __device__ void seed_step_scalars(const Ctx &c, double rr, double rrh) {
     __shared__ double s_bk;
-    __shared__ int s_ok, s_sw, s_t, s_nconv;
+    __shared__ int s_ok, s_sw, s_t, s_nconv, s_nfail;
     __shared__ double s_best[NW];
     __shared__ int s_bidx[NW];
     hbk_scalars *sc = c.sh.sc;
@@ -241,6 +241,7 @@ __device__ void seed_step_scalars(const Ctx &c, double rr, double rrh) {
         sc->rr_hat = rrh;
         s_bk = bk;
         s_ok = fin(bk);
+        s_nfail = 0;
         if (!s_ok) {
             sc->status |= HBK_ST_BREAKDOWN;
             sc->finished = 1;
@@ -277,20 +278,37 @@ __device__ void seed_step_scalars(const Ctx &c, double rr, double rrh) {
         const double pik1 = pij[k - 1];
         const double eta = sub(mul(c_prev, S.eta[j]), mul(mul(d, ak), pik1));
         const double pik = add(eta, pik1);
+        const double den = sub(1.0, mul(wk, d));
+        const double aj = mul(dvd(pik1, pik), ak);
+        const double wj = dvd(wk, den);
+        const double z = S.zeta[j];
+        double cn[6];
+        cn[0] = dvd(wj, mul(pik, z));
+        cn[1] = aj;
+        cn[2] = dvd(wj, mul(mul(aj, z), pik));
+        cn[3] = dvd(-wj, mul(mul(aj, z), pik1));
+        const double zn = mul(den, z);
+        const double rp = dvd(pik1, pik);
+        cn[4] = mul(mul(rp, rp), bk);
+        cn[5] = dvd(1.0, mul(pik, zn));
+        // Shift breakdown (the reference never tests for it and carries the
+        // inf or nan into x_j): pi_k = 0, 1 - omega_k d = 0, or any scalar of
+        // the update not finite.  The shift stops at its last finite iterate,
+        // counts as finished so the others run on, and records -k.
+        bool ok = pik != 0.0 && den != 0.0 && fin(eta) && fin(zn);
+#pragma unroll
+        for (int t = 0; t < 6; t++) ok = ok && fin(cn[t]);
+        if (!ok) {
+            S.done[j] = 1;
+            S.conv_k[j] = -k;
+            atomicAdd(&s_nfail, 1);
+            continue;
+        }
         pij[k] = pik;
         S.eta[j] = eta;
-        const double aj = mul(dvd(pik1, pik), ak);
-        const double wj = dvd(wk, sub(1.0, mul(wk, d)));
-        const double z = S.zeta[j];
-        co[0] = dvd(wj, mul(pik, z));
-        co[1] = aj;
-        co[2] = dvd(wj, mul(mul(aj, z), pik));
-        co[3] = dvd(-wj, mul(mul(aj, z), pik1));
-        const double zn = mul(sub(1.0, mul(wk, d)), z);
         S.zeta[j] = zn;
-        const double rp = dvd(pik1, pik);
-        co[4] = mul(mul(rp, rp), bk);
-        co[5] = dvd(1.0, mul(pik, zn));
+#pragma unroll
+        for (int t = 0; t < 6; t++) co[t] = cn[t];
     }
     __syncthreads();
 
@@ -353,7 +371,8 @@ __device__ void seed_step_scalars(const Ctx &c, double rr, double rrh) {
             }
         }
         if (bi >= 0) sc->max_sigma = bi;
-        sc->n_done += s_nconv;
+        sc->n_done += s_nconv + s_nfail;
+        if (s_nfail) sc->status |= HBK_ST_SHIFT_FAIL;
         s_sw = (sc->switching && S.done[seed] && sc->n_done < m) ? 1 : 0;
         s_t = sc->max_sigma;
         sc->next_seed = s_sw ? s_t : seed;

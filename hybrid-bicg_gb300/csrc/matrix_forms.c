@@ -199,19 +199,17 @@ int hbicg__sell_diag(hbicg_matrix *A) {
     cudaStream_t st = A->ctx->stream;
     const unsigned n = A->k.n;
     int *d_missing = NULL, missing = 0;
-    if (!A->d_sdiag) CUDA_TRY(cudaMalloc((void **)&A->d_sdiag, sizeof(unsigned long long) * ((size_t)n + 1)));
-    CUDA_TRY(cudaMalloc((void **)&d_missing, sizeof(int)));
-    CUDA_TRY(cudaMemsetAsync(d_missing, 0, sizeof(int), st));
-    int e = hbk_sell_diag(n, A->d_ptr, A->d_sptr, A->d_scol, A->d_sdiag, d_missing, st);
-    if (!e) e = (int)cudaMemcpyAsync(&missing, d_missing, sizeof(int), cudaMemcpyDeviceToHost, st);
-    if (!e) e = (int)cudaStreamSynchronize(st);
-    cudaFree(d_missing);
-    if (e) {
-        set_msg("diagonal positions: %s", cudaGetErrorString((cudaError_t)e));
-        return HBICG_E_CUDA;
-    }
+    int rc = HBICG_OK;
+    if (!A->d_sdiag) CUDA_GOTO(cudaMalloc((void **)&A->d_sdiag, sizeof(unsigned long long) * ((size_t)n + 1)));
+    CUDA_GOTO(cudaMalloc((void **)&d_missing, sizeof(int)));
+    CUDA_GOTO(cudaMemsetAsync(d_missing, 0, sizeof(int), st));
+    HBK_GOTO(hbk_sell_diag(n, A->d_ptr, A->d_sptr, A->d_scol, A->d_sdiag, d_missing, st));
+    CUDA_GOTO(cudaMemcpyAsync(&missing, d_missing, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_GOTO(cudaStreamSynchronize(st));
     A->diag_state = missing ? 2 : 1;
-    return HBICG_OK;
+out: /* d_missing is freed on every path; d_sdiag belongs to the matrix */
+    cudaFree(d_missing);
+    return rc;
 }
 
 /* row blocks of the tile form (hbk_plan_rows) */

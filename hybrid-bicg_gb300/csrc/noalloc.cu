@@ -15,9 +15,13 @@
 // library holds it (about 1 MiB) until the process exits.  All calls share it,
 // so calls whose kernels overlap on the GPU (other streams, other host
 // threads) race on it; serialise them.  The first call on a device looks up
-// the array's device address with cudaGetSymbolAddress; make that first call
-// before any stream capture.
+// the array's device address with cudaGetSymbolAddress (under a lock, once per
+// device) and keeps it; make that first call before any stream capture.  The
+// kept address belongs to the device's primary context: after
+// cudaDeviceReset on that device the process must not call this entry point
+// again.
 #include <math.h>
+#include <mutex>
 #include <string.h>
 
 #include "hbicg.h"
@@ -28,7 +32,9 @@ using namespace hbk;
 namespace {
 
 constexpr int kMaxShifts = HBICG_NOALLOC_MAX_SHIFTS;
-constexpr int kMaxGrid = 2048;  // >= the SpMV grid on one GB300 (152 SMs x 8)
+// Blocks of the residual products and of the b.b dot, whatever the device:
+// both launches are capped at this many blocks, one partial sum each.
+constexpr int kMaxGrid = 2048;
 constexpr size_t kPartials = (size_t)(kMaxShifts + 1) * kMaxGrid;  // doubles
 constexpr size_t kSums = kMaxShifts + 8;                           // doubles
 constexpr size_t kTickets = kMaxShifts + 16;                       // unsigned
@@ -41,6 +47,7 @@ static __device__ __align__(256) unsigned char g_scratch[kBytes];
 
 constexpr int kMaxDevices = 64;
 static void *g_scratch_dev[kMaxDevices];
+static std::mutex g_scratch_lock;
 
 __global__ void k_norms(const double *sq, const double *bb, int m, double *res) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -73,17 +80,22 @@ extern "C" int hbicg_true_residuals_noalloc(hbicg_matrix *A, const double *x, un
         hbicg__set_message("hbicg_true_residuals_noalloc: no usable current device");
         return HBICG_E_CUDA;
     }
-    if (!g_scratch_dev[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess || !p) {
-            hbicg__set_message(cudaGetErrorString(e));
-            return HBICG_E_CUDA;
+    void *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_scratch_lock);
+        if (!g_scratch_dev[dev]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+            if (e != cudaSuccess || !p) {
+                hbicg__set_message(cudaGetErrorString(e));
+                return HBICG_E_CUDA;
+            }
+            g_scratch_dev[dev] = p;
         }
-        g_scratch_dev[dev] = p;
+        base = g_scratch_dev[dev];
     }
     cudaStream_t st = (cudaStream_t)stream;
-    double *partials = (double *)g_scratch_dev[dev];
+    double *partials = (double *)base;
     double *sums = partials + kPartials;
     unsigned *tickets = (unsigned *)(sums + kSums);
     // the last-block tickets must start at zero (an earlier call that failed
@@ -93,8 +105,9 @@ extern "C" int hbicg_true_residuals_noalloc(hbicg_matrix *A, const double *x, un
         return HBICG_E_CUDA;
     }
     int e = hbk_true_residuals_ld(K, x, (size_t)ldx, b, sigma, m, kMaxGrid, partials, tickets, sums, st);
-    if (!e) e = hbk_dot(K->n, b, b, partials + (size_t)kMaxShifts * kMaxGrid, tickets + kMaxShifts, sums + kMaxShifts,
-                        st);
+    if (!e)
+        e = hbk_dot_capped(K->n, b, b, kMaxGrid, partials + (size_t)kMaxShifts * kMaxGrid, tickets + kMaxShifts,
+                           sums + kMaxShifts, st);
     if (!e) {
         k_norms<<<(m + 63) / 64, 64, 0, st>>>(sums, sums + kMaxShifts, m, res);
         e = (int)cudaGetLastError();

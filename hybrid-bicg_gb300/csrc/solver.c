@@ -494,7 +494,7 @@ static int run_plain(hbicg_solver *s, const double *h_sigma, int seed, plain_out
     rr = bb = rr_hat;
     ah[0] = 1.0;
     bh[0] = 0.0;
-    int k = 1, n_done = 0, argmax = seed;
+    int k = 1, n_done = 0, argmax = seed, shift_fail = 0;
     if (bb == 0.0) n_done = m; /* x = 0 is exact */
     while (n_done < m && k < kcap) {
         double *ps = v->P + (size_t)seed * ld, *xs = v->X + (size_t)seed * ld;
@@ -539,18 +539,34 @@ static int run_plain(hbicg_solver *s, const double *h_sigma, int seed, plain_out
             double *pij = pi + (size_t)j * kcap;
             double *xj = v->X + (size_t)j * ld, *pj = v->P + (size_t)j * ld;
             const double d = sig_s - h_sigma[j];
-            eta[j] = c_prev * eta[j] - d * ak * pij[k - 1];
-            pij[k] = eta[j] + pij[k - 1];
-            const double aj = (pij[k - 1] / pij[k]) * ak;
-            const double wj = wk / (1.0 - wk * d);
-            PL(hbk_axpy(n, wj / (pij[k] * zeta[j]), qc, xj, st));
+            const double e_new = c_prev * eta[j] - d * ak * pij[k - 1];
+            const double pik = e_new + pij[k - 1];
+            const double den = 1.0 - wk * d;
+            const double aj = (pij[k - 1] / pik) * ak;
+            const double wj = wk / den;
+            const double zn = den * zeta[j];
+            const double c0 = wj / (pik * zeta[j]), c2 = wj / (aj * zeta[j] * pik);
+            const double c3 = -wj / (aj * zeta[j] * pij[k - 1]);
+            const double bj = (pij[k - 1] / pik) * (pij[k - 1] / pik) * bk, c5 = 1.0 / (pik * zn);
+            /* shift breakdown: pi_k = 0, 1 - omega d = 0 or a non-finite
+             * scalar; the shift keeps its last finite iterate and stops */
+            if (pik == 0.0 || den == 0.0 || !isfinite(e_new) || !isfinite(zn) || !isfinite(c0) || !isfinite(aj) ||
+                !isfinite(c2) || !isfinite(c3) || !isfinite(bj) || !isfinite(c5)) {
+                done[j] = 1;
+                n_done++;
+                shift_fail = 1;
+                if (o->conv_k) o->conv_k[j] = -k;
+                continue;
+            }
+            eta[j] = e_new;
+            pij[k] = pik;
+            PL(hbk_axpy(n, c0, qc, xj, st));
             PL(hbk_axpy(n, aj, pj, xj, st));
-            PL(hbk_axpy(n, wj / (aj * zeta[j] * pij[k]), qc, pj, st));
-            PL(hbk_axpy(n, -wj / (aj * zeta[j] * pij[k - 1]), r_old, pj, st));
-            zeta[j] = (1.0 - wk * d) * zeta[j];
-            const double bj = (pij[k - 1] / pij[k]) * (pij[k - 1] / pij[k]) * bk;
+            PL(hbk_axpy(n, c2, qc, pj, st));
+            PL(hbk_axpy(n, c3, r_old, pj, st));
+            zeta[j] = zn;
             PL(hbk_scal(n, bj, pj, st));
-            PL(hbk_axpy(n, 1.0 / (pij[k] * zeta[j]), r, pj, st));
+            PL(hbk_axpy(n, c5, r, pj, st));
         }
         if (o->act && k < kcap) o->act[k] = active;
         double best = 1.0;
@@ -602,6 +618,10 @@ static int run_plain(hbicg_solver *s, const double *h_sigma, int seed, plain_out
     }
     o->k = k;
     o->final_seed = seed;
+    if (shift_fail && rc == HBICG_OK) {
+        rc = HBICG_E_BREAKDOWN;
+        o->status = HBICG_E_BREAKDOWN;
+    }
 out:
     o->launches = launches;
     free(ah); free(bh); free(wh); free(pi); free(eta); free(zeta); free(done);
@@ -989,7 +1009,7 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
             k = h->k;
             n_sw = h->n_sw;
             final_seed = h->seed;
-            if (h->status & HBK_ST_BREAKDOWN) status = HBICG_E_BREAKDOWN;
+            if (h->status & (HBK_ST_BREAKDOWN | HBK_ST_SHIFT_FAIL)) status = HBICG_E_BREAKDOWN;
             if (m > 0) {
                 CUDA_TRY(cudaMemcpyAsync(conv, s->sh.conv_k, sizeof(int) * m, cudaMemcpyDeviceToHost, st));
                 int nl = n_sw < m ? n_sw : m;

@@ -24,7 +24,9 @@ typedef enum {
     HBICG_OK = 0,
     HBICG_E_NOT_SQUARE = 1,
     HBICG_E_NO_DIAG = 2,
-    HBICG_E_BREAKDOWN = 3, /* (r^,s), (q,y) or a shift denominator became 0, inf or nan */
+    HBICG_E_BREAKDOWN = 3, /* (r^,s), (q,y) or a seed scalar became 0, inf or nan (the solve stops), or a
+                              non-seed shift's pi_k, 1 - omega_k (sigma_s - sigma_j) or update scalar did
+                              (that shift stops at its last finite iterate, the others run to the end) */
     HBICG_E_MAXITER = 4,   /* some shift did not converge within max_iter */
     HBICG_E_CUDA = 5,
     HBICG_E_TIMEOUT = 6,
@@ -87,7 +89,8 @@ typedef struct {
     /* optional caller-owned outputs (NULL to skip) */
     int *switch_k;            /* [m] iteration of each switch */
     int *switch_seed;         /* [m] seed chosen at each switch */
-    int *conv_k;              /* [m] iteration at which each shift met the test (0 = never) */
+    int *conv_k;              /* [m] iteration at which each shift met the test (0 = never,
+                                 -k = broke down at iteration k) */
     int *active_per_iter;     /* [max_iter + 1] non-seed shifts updated at iteration k */
     double *true_residual;    /* [m] */
     double *seed_alpha;       /* [max_iter + 1] the seed's alpha, beta, omega per iteration (as archived) */

@@ -188,8 +188,45 @@ def convergence_profile(name: str = "c2") -> None:
     print(f"{name}: k={seed_run.k} shift updates={int(act.sum())} ({secs:.0f} s)")
 
 
+DIGEST_SAMPLES = 4096
+
+
+def digest_indices(n: int, count: int = DIGEST_SAMPLES) -> np.ndarray:
+    """Rows sampled by a solution digest: seeded, sorted, first and last row included."""
+    idx = np.random.default_rng(20261204).choice(n, size=min(count, n) - 2, replace=False)
+    return np.unique(np.concatenate([idx, [0, n - 1]])).astype(np.int64)
+
+
+def solution_digest(name: str = "c2") -> None:
+    """Digest of the reference's own full solve of a named workload.
+
+    The reference (oracle/_ref/libref.so, its sources compiled single-rank) runs
+    the whole family to convergence with the workload's tolerance; the digest
+    keeps what a test needs to compare another solver's 64 solutions with it
+    without the 8.6 GB of x: k, the switch sequence, every shift's norm, sum and
+    true residual, and every shift's values at DIGEST_SAMPLES seeded rows."""
+    import oracle as O
+    import time
+
+    O.build(ref=True)
+    wl = _workloads()
+    f = wl.family(name)
+    t0 = time.perf_counter()
+    res = O.ref_solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=f.max_iter, variant="dynamic")
+    secs = time.perf_counter() - t0
+    idx = digest_indices(f.a.n)
+    tr = O.true_residuals(f.a, res.x, f.b, f.sigma)
+    sw = np.array(res.switches, dtype=np.int64).reshape(-1, 2)
+    np.savez_compressed(OUT / f"{name}_digest.npz", k=res.k, switches=sw, sigma=f.sigma, idx=idx,
+                        x_at=res.x[:, idx], norm=np.linalg.norm(res.x, axis=1), sum=res.x.sum(axis=1),
+                        true_residual=tr, r_at=res.r[idx], seconds=secs)
+    print(f"{name}: k={res.k} switches={res.switches} max true residual={tr.max():.3e} ({secs:.0f} s)")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[1] == "--profile":
         convergence_profile(sys.argv[2])
+    elif len(sys.argv) > 2 and sys.argv[1] == "--digest":
+        solution_digest(sys.argv[2])
     else:
         main()

@@ -151,3 +151,37 @@ def test_host_vector_helpers(lib):
     lib.my_daxpy(5, 2.0, x.ctypes.data_as(pd), y.ctypes.data_as(pd))
     assert np.array_equal(y, 1 + 2 * x)
     assert lib.my_ddot(5, x.ctypes.data_as(pd), y.ctypes.data_as(pd)) == float(np.dot(x, y))
+
+
+def test_noalloc_wrapper_rejects_bad_tensors(pkg):
+    """The Python wrapper of hbicg_true_residuals_noalloc refuses tensors the
+    kernels would read or write past, before any call into the library (host
+    tensors are enough to check the shape, dtype and layout rules)."""
+    torch = pytest.importorskip("torch")
+    n, m = 10, 3
+    f64 = dict(dtype=torch.float64)
+    ok = dict(x=torch.zeros(m, n, **f64), b=torch.zeros(n, **f64), sigma=torch.zeros(m, **f64),
+              res=torch.zeros(m, **f64))
+    bad_cases = [
+        dict(x=torch.zeros(m, n, dtype=torch.float32)),
+        dict(x=torch.zeros(m * n, **f64)),                    # one-dimensional x
+        dict(x=torch.zeros(m - 1, n, **f64)),                 # fewer rows than shifts
+        dict(x=torch.zeros(m, n - 1, **f64)),                 # rows shorter than n
+        dict(x=torch.zeros(n, m, **f64).t()),                 # inner stride m
+        dict(b=torch.zeros(n - 1, **f64)),
+        dict(res=torch.zeros(m - 1, **f64)),
+        dict(sigma=torch.zeros(m, 1, **f64)),
+        dict(b=torch.zeros(2 * n, **f64)[::2]),               # strided b
+        dict(res=[0.0] * m),
+    ]
+    for bad in bad_cases:
+        args = {**ok, **bad}
+        with pytest.raises(ValueError):
+            pkg._check_noalloc_args(n, args["x"], args["b"], args["sigma"], args["res"])
+    # well-formed host tensors fail only on the device rule
+    with pytest.raises(ValueError, match="CUDA"):
+        pkg._check_noalloc_args(n, ok["x"], ok["b"], ok["sigma"], ok["res"])
+    # wider rows (a leading dimension above n) are allowed
+    wide = torch.zeros(m, n + 6, **f64)
+    with pytest.raises(ValueError, match="CUDA"):
+        pkg._check_noalloc_args(n, wide, ok["b"], ok["sigma"], ok["res"])
