@@ -173,6 +173,16 @@ def workload(name: str, scale):
     return pkg, pkg.workloads.family(name, scale)
 
 
+def workload_config(args, f, world: int) -> dict:
+    """The `config` object of a bench line: the workload alone, identical for
+    both arms (how each arm computes it is reported outside `config`)."""
+    m = len(f.sigma)
+    return {"workload": f"{args.workload}: {f.a.n} rows, {f.a.nnz} nonzeros, {MATRIX_KIND.get(args.workload, '')}"
+                        f"{m} shifts in [{f.sigma.min():g}, {f.sigma.max():g}], tol {f.tol:g}, seed {f.seed}",
+            "mode": args.mode, "parallelism": f"replicas x{world}",
+            "l2": "working set >> 129 MB L2 (no flush needed)"}
+
+
 def spmv_bytes(n: int, nnz: int) -> float:
     """Compulsory HBM bytes of one y = (A + sigma I) x: values and column
     indices once (12 B per nonzero), row pointers once, x read once, y written
@@ -220,6 +230,40 @@ def load_profile(name: str, f):
         return None
     d["source"] = f"reference-algorithm profile {p.name}"
     return d
+
+
+def load_digest(name: str):
+    """Digest of the reference's own full solve of a named workload
+    (tests/golden/<name>_digest.npz, made by tests/golden/make_golden.py
+    --digest <name>): k, the switch sequence, and every shift's values at
+    seeded rows, norm and true residual."""
+    p = ROOT / "tests" / "golden" / f"{name}_digest.npz"
+    if not p.exists():
+        return None
+    d = np.load(p, allow_pickle=False)
+    return {k: d[k] for k in d.files}
+
+
+def digest_compare(dig: dict, x, k: int, switches) -> dict:
+    """Solutions against the reference's at the digest's rows (x: (m, n) host
+    or device array): max over shifts of max |x_j - x_ref_j| / max |x_ref_j|
+    at those rows, the relative error of ||x_j||, k and the switch sequence."""
+    idx = dig["idx"]
+    if hasattr(x, "index_select"):  # a torch tensor: gather on its device
+        import torch
+
+        xs = x.index_select(1, torch.as_tensor(idx, device=x.device)).cpu().numpy()
+        nrm = torch.linalg.vector_norm(x, dim=1).cpu().numpy()
+    else:
+        xs = np.asarray(x)[:, idx]
+        nrm = np.linalg.norm(x, axis=1)
+    want = dig["x_at"]
+    err = np.max(np.abs(xs - want), axis=1) / np.maximum(np.max(np.abs(want), axis=1), 1e-300)
+    want_sw = [tuple(int(v) for v in row) for row in dig["switches"].reshape(-1, 2)]
+    return {"max_rel_err_at_rows": float(np.max(err)), "rows": int(len(idx)),
+            "max_rel_err_norm": float(np.max(np.abs(nrm - dig["norm"]) / dig["norm"])),
+            "k": int(k), "k_reference": int(dig["k"]),
+            "switches_match": [tuple(s) for s in switches] == want_sw}
 
 
 def _cpu_baseline_child(name, scale, profile):
@@ -329,10 +373,38 @@ def run_ours(args, dist: Dist):
     step_s = ev0.elapsed_time(ev1) / 1e3 / args.steps
     step_max, units = aggregate(dist, step_s, 1.0)
 
-    # verification solve (not timed): every shift's true residual
+    # verification solve (not timed): every shift's true residual, and the
+    # solutions against the reference's own full solve where its digest exists
     ver = pkg.Solver(A, m, **{**kw, "true_residuals": True})
     vres = ver.run(b, sig, seed=f.seed, x=x)
     ver.close()
+    dig = load_digest(args.workload) if args.scale is None else None
+    parity = digest_compare(dig, x, vres.k, vres.switches) if dig is not None else None
+
+    # the plain per-kernel GPU form on the same GPU (shifted_lopbicg_static's
+    # form: one launch per step of the reference's iteration, the scalars on
+    # the host), same matrix and settings: one untimed solve, one timed, then
+    # every shift's true residual without allocating
+    plain = None
+    if form == "fused" and not args.no_plain:
+        ps = pkg.Solver(A, m, **{**kw, "form": "plain", "use_graph": False})
+        ps.run(b, sig, seed=f.seed, x=x)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        pres = ps.run(b, sig, seed=f.seed, x=x)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        ps.close()
+        plain_s = p0.elapsed_time(p1) / 1e3
+        tres = torch.empty(m, dtype=torch.float64, device="cuda")
+        if m <= 64:
+            pkg.true_residuals_noalloc(A, x, b, sig, tres, stream=ctx.stream)
+            torch.cuda.synchronize()
+        plain = {"value": plain_s, "unit": "s", "iterations": pres.k, "launches": pres.launches,
+                 "refined_shifts": pres.refined,
+                 "max_true_residual": float(tres.max().item()) if m <= 64 else None,
+                 "fused_speedup": plain_s / step_max}
 
     # SpMV kernel alone (same kernel as the solve's two products), CUDA events
     xs = torch.randn(n, dtype=torch.float64, device="cuda")
@@ -385,6 +457,15 @@ def run_ours(args, dist: Dist):
                                                                           + h_b.nbytes + h_sig.nbytes),
                "d2h_bytes_per_step": int(h_x.nbytes + h_r.nbytes), "api": "shifted_lopbicg_dynamic", "k": int(k),
                "calls_s": [round(t, 4) for t in e2e_times]}
+        if plain is not None:
+            # the same call through shifted_lopbicg_static (the plain form), once
+            h_x.zero_()
+            h_r.copy_(h_b)
+            t0 = time.perf_counter()
+            kp = pkg.dropin_raw("static", h_ptr, h_col, h_val, h_x, h_r, h_sig, f.seed, f.tol, f.max_iter)
+            plain["e2e"] = {"value": time.perf_counter() - t0, "unit": "s", "api": "shifted_lopbicg_static",
+                            "k": int(kp)}
+            plain["fused_e2e_speedup"] = plain["e2e"]["value"] / e2e_max
 
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
@@ -398,16 +479,14 @@ def run_ours(args, dist: Dist):
         "metric": METRIC, "value": step_max, "unit": "s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_max * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator; the reference ships no matrices)",
-        "config": {"workload": f"{args.workload}: {f.a.n} rows, {f.a.nnz} nonzeros, {MATRIX_KIND.get(args.workload, '')}"
-                   f"{m} shifts in [{f.sigma.min():g}, {f.sigma.max():g}], tol {f.tol:g}, seed {f.seed}",
-                   "mode": args.mode, "shift_mode": res.shift_mode, "refine": not args.no_refine,
-                   "spmv_format": res_format,
-                   "parallelism": f"replicas x{dist.world}",
-                   "l2": "working set >> 129 MB L2 (no flush needed)"},
+        "config": workload_config(args, f, dist.world),
+        "implementation": {"form": form, "graphs": use_graph, "shift_mode": res.shift_mode,
+                           "refine": not args.no_refine, "spmv_format": res_format},
         "iterations": res.k, "switches": res.switches, "refined_shifts": res.refined,
         "max_true_residual": vres.max_true_residual,
         "all_converged": bool(np.all(vres.conv_k > 0)),
         "solve_breakdown_ms": {"flush": flush_ms / args.steps},
+        "vs_reference_digest": parity, "plain": plain,
         "roofline": roofline, "roofline_spmv": spmv, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }
@@ -415,25 +494,66 @@ def run_ours(args, dist: Dist):
 
 
 def run_reference(args, dist: Dist):
-    """The reference's CPU path on the host cores (rank 0 only)."""
+    """The reference's CPU path on the host cores (rank 0 only), measured to
+    convergence: the reference's algorithm and OpenMP layout (the oracle's C
+    restatement, bit-identical to the reference's own sources where those
+    compile) solves the whole family once, on all host threads.  The timed
+    steps partition that one solve: the solver stamps the wall clock after
+    every iteration, step i covers iterations [k_i, k_(i+1)) of K near-equal
+    consecutive ranges, the first step also carries the set-up (allocation,
+    the copies of b into every p_j) and the last the teardown.  `value` is the
+    whole solve (the sum of the steps); the warm-up steps are untimed
+    one-iteration solves of the same family.  Where a quick projection says
+    the full solve would not end within `--ref-budget` seconds, the bounded
+    sample and cost model of cpu_baseline stand in, labelled as an estimate."""
     if dist.rank != 0:
         return None
     _, f = workload(args.workload, args.scale)
-    vals = []
-    info = None
+    orc = graft.load_oracle()
+    orc.build(ref=False)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    base = {"impl": "reference", "metric": METRIC, "unit": "s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded generator; the reference ships no matrices)",
+            "config": workload_config(args, f, dist.world),
+            "implementation": {"code": "reference algorithm, C restatement + OpenMP (oracle/)", "cores": cores}}
+    for _ in range(max(1, args.warmup)):
+        orc.solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=1)
+    # projection: two iterations with every shift running, times the expected count
+    t0 = time.perf_counter()
+    orc.solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=2)
+    per_iter = (time.perf_counter() - t0) / 2.0
     prof = load_profile(args.workload, f) if args.scale is None else None
-    warm = max(1, args.warmup)
-    for i in range(warm + args.steps):
+    k_expect = int(prof["k"]) if prof else f.max_iter
+    projected = per_iter * k_expect
+    if projected > args.ref_budget:
         info = cpu_baseline(f, prof)
-        if i >= warm:
-            vals.append(info["value"])
-    v = float(np.median(vals))
-    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": dist.world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "implementation": "reference algorithm, C restatement + OpenMP"},
-            "cpu_baseline": {**info, "value": v},
-            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        v = info["value"]
+        return {**base, "value": v, "ms_per_step": v * 1e3, "measured": False,
+                "projection_s": projected,
+                "cpu_baseline": {**info, "kind": "port", "sample": "estimate (full solve projected beyond "
+                                 f"{args.ref_budget:.0f} s): " + info["sample"]},
+                "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    t0 = time.perf_counter()
+    res = orc.solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=f.max_iter)
+    total = time.perf_counter() - t0
+    stamps = np.asarray(res.hist["t"], dtype=np.float64)  # [0]: iterations start, [k]: end of iteration k
+    kk = len(stamps) - 1  # iterations done
+    cuts = np.linspace(0, kk, args.steps + 1).round().astype(int)
+    steps = [float(stamps[b] - stamps[a]) for a, b in zip(cuts[:-1], cuts[1:])]
+    steps[0] += total - float(stamps[-1] - stamps[0])  # set-up and teardown outside the stamps
+    tr = orc.true_residuals(f.a, res.x, f.b, f.sigma)
+    sample = (f"one complete solve ({res.k - 1} iterations, all {len(f.sigma)} shifts, {cores} threads); "
+              f"the {args.steps} timed steps are consecutive iteration ranges of it")
+    line = {**base, "value": total, "ms_per_step": total / args.steps * 1e3, "measured": True,
+            "step_s": [round(t, 3) for t in steps], "timed_region_s": total, "iterations": int(res.k),
+            "switches": res.switches, "max_true_residual": float(np.max(tr)), "projection_s": projected,
+            "cpu_baseline": {"value": total, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": total, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    dig = load_digest(args.workload) if args.scale is None else None
+    if dig is not None:
+        line["vs_reference_digest"] = digest_compare(dig, res.x, res.k, res.switches)
+    return line
 
 
 def run_batch_c4(args, dist: Dist):
@@ -617,7 +737,7 @@ def run_spmv_kernel(args):
     default = A.format
     out = {"kernel": "k_spmv", "workload": args.workload, "n": n, "nnz": nnz, "default_format": default,
            "bytes_per_launch": byt, "peak_kind": kind, "forms": {}}
-    for fmt in [default] + [g for g in ("tile", "sell", "hyb") if g != default]:
+    for fmt in [default] + [g for g in ("tile", "sell", "hyb", "merge") if g != default]:
         try:
             A.set_format(fmt)
         except RuntimeError:
@@ -759,6 +879,7 @@ def main(argv=None):
     ap.add_argument("--flush", default="auto", choices=["auto", "fp64", "tensor"])
     ap.add_argument("--basis-block", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain per-kernel form beside the fused")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-refine", action="store_true", help="keep the reference's x (no true-residual correction)")
     ap.add_argument("--row-classes", action="store_true",
@@ -767,6 +888,8 @@ def main(argv=None):
                     help="time one kernel alone on random data instead of the solve")
     ap.add_argument("--n", type=int, default=2097152, help="elements for --kernel")
     ap.add_argument("--workers", type=int, default=8, help="host workers for --workload c4")
+    ap.add_argument("--ref-budget", type=float, default=1500.0,
+                    help="--impl reference: longest projected full CPU solve (s) to measure; beyond it, estimate")
     args = ap.parse_args(argv)
     if args.kernel:
         run = {"flush": run_flush_kernel, "spmv": run_spmv_kernel, "coo2csr": run_coo2csr_kernel,

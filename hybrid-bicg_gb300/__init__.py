@@ -210,7 +210,7 @@ def params(tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="a
 
 
 # SpMV storage forms (hbicg_spmv_format)
-_FORMATS = {0: "tile", 1: "sell", 2: "hyb"}
+_FORMATS = {0: "tile", 1: "sell", 2: "hyb", 3: "merge"}
 
 
 @dataclass

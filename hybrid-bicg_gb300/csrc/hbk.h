@@ -42,6 +42,10 @@ extern "C" {
 #define HBK_FMT_HYB 2        /* short rows in SELL-32 slices (length-sorted inside windows), long rows one warp each */
 #define HBK_HYB_SHORT 32     /* longest row of a HYB slice */
 #define HBK_HYB_WINDOW 256   /* rows are sorted by length only inside windows of this many consecutive rows */
+#define HBK_FMT_MERGE 3      /* CSR; rows up to HBK_MERGE_LONG entries in merge-path blocks, longer rows one warp each */
+#define HBK_MERGE_IPT 6      /* merge items (row ends + nonzeros) per thread of a block */
+#define HBK_MERGE_ITEMS (HBK_THREADS * HBK_MERGE_IPT) /* items per block */
+#define HBK_MERGE_LONG 192   /* longest row a merge block takes */
 
 typedef struct {
     unsigned n, nnz;
@@ -61,6 +65,10 @@ typedef struct {
     unsigned nslice;           /* HYB: slices of short rows */
     const unsigned *wrow;      /* HYB: rows longer than HBK_HYB_SHORT, longest first, one warp each */
     unsigned nwrow;
+    const unsigned *mblk;      /* MERGE: [2 nmblk] first and end row of each block of short rows */
+    unsigned nmblk;
+    const unsigned *mlong;     /* MERGE: rows longer than HBK_MERGE_LONG, longest first, one warp each */
+    unsigned nmlong;
 } hbk_matrix;
 
 /* Device-resident scalars of one solve. */

@@ -225,6 +225,111 @@ __device__ __forceinline__ void spmv_rows_hyb(const hbk_matrix &A, const double 
     }
 }
 
+// MERGE path: nonzero-balanced work inside row blocks (merge-path
+// decomposition).  The host cuts the short rows (<= HBK_MERGE_LONG entries)
+// into blocks of consecutive rows with rows + nonzeros <= HBK_MERGE_ITEMS;
+// rows longer than that are listed apart (longest first).  Work units, in
+// order: groups of NW long rows (one warp per row, lanes take every 32nd entry
+// in stored order, fixed shuffle tree), then the blocks.  A block is staged in
+// shared memory with coalesced loads (values, the gathered x values, the row
+// end offsets); thread t then walks items [t IPT, (t + 1) IPT) of the merge of
+// the row ends with the nonzeros, so every thread gets the same number of
+// (row end + nonzero) items whatever the row lengths.  A row that starts and
+// ends inside one thread is summed by that thread in stored order with FMAs
+// from 0 (the other paths' arithmetic); a row cut between threads is the sum,
+// in thread order, of its pieces (each an FMA chain in stored order).  Either
+// way `epi(row, acc)` runs once per row.
+struct MergeSmem {
+    double val[HBK_MERGE_ITEMS];
+    double xv[HBK_MERGE_ITEMS];
+    unsigned rend[HBK_MERGE_ITEMS];  // end of each row of the block, relative to its first nonzero
+    double cv[NT];                   // piece of the row a thread leaves open
+    unsigned cr[NT];                 // that row (relative), or ~0u
+};
+
+template <class Epi>
+__device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const double *__restrict__ x, Epi &epi,
+                                                MergeSmem &sm) {
+    const unsigned *__restrict__ ptr = A.ptr;
+    const unsigned *__restrict__ col = A.col;
+    const double *__restrict__ val = A.val;
+    const unsigned tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned long_units = (A.nmlong + NW - 1) / NW;
+    const unsigned units = long_units + A.nmblk;
+    for (unsigned u = blockIdx.x; u < units; u += gridDim.x) {
+        if (u < long_units) {
+            const unsigned it = u * NW + warp;
+            if (it < A.nmlong) {
+                const unsigned r = __ldg(A.mlong + it);
+                const unsigned e1 = __ldg(ptr + r + 1);
+                double acc = 0.0;
+                for (unsigned e = __ldg(ptr + r) + lane; e < e1; e += 32)
+                    acc = fma(__ldg(val + e), __ldg(x + __ldg(col + e)), acc);
+                acc = warp_sum(acc);
+                if (lane == 0) epi(r, acc);
+            }
+            continue;  // warp-uniform: no barrier in this unit
+        }
+        const unsigned b = u - long_units;
+        const unsigned r0 = __ldg(A.mblk + 2 * b), r1 = __ldg(A.mblk + 2 * b + 1);
+        const unsigned e0 = __ldg(ptr + r0);
+        const unsigned nr = r1 - r0, nz = __ldg(ptr + r1) - e0;
+        for (unsigned e = tid; e < nz; e += NT) {
+            const unsigned c = __ldg(col + e0 + e);
+            sm.val[e] = __ldg(val + e0 + e);
+            sm.xv[e] = __ldg(x + c);
+        }
+        for (unsigned i = tid; i < nr; i += NT) sm.rend[i] = __ldg(ptr + r0 + i + 1) - e0;
+        __syncthreads();
+        const unsigned tot = nr + nz;
+        const unsigned d0 = min(tid * (unsigned)HBK_MERGE_IPT, tot);
+        const unsigned d1 = min(d0 + (unsigned)HBK_MERGE_IPT, tot);
+        // merge-path search: i row ends and d0 - i nonzeros precede item d0
+        unsigned lo = d0 > nz ? d0 - nz : 0, hi = min(d0, nr);
+        while (lo < hi) {
+            const unsigned mid = (lo + hi) >> 1;
+            if (sm.rend[mid] <= d0 - 1 - mid) lo = mid + 1;
+            else hi = mid;
+        }
+        unsigned i = lo, e = d0 - lo;
+        // the thread starts inside row i when entries of that row precede e
+        const bool head_open = e > (i ? sm.rend[i - 1] : 0u);
+        bool head = head_open, open = false;
+        unsigned head_row = ~0u;
+        double head_v = 0.0, acc = 0.0;
+        for (unsigned d = d0; d < d1; ++d) {
+            if (i < nr && sm.rend[i] <= e) {
+                if (head) {
+                    head_row = i;
+                    head_v = acc;
+                    head = false;
+                } else {
+                    epi(r0 + i, acc);
+                }
+                acc = 0.0;
+                open = false;
+                ++i;
+            } else {
+                acc = fma(sm.val[e], sm.xv[e], acc);
+                ++e;
+                open = true;
+            }
+        }
+        sm.cr[tid] = open ? i : ~0u;
+        sm.cv[tid] = acc;
+        __syncthreads();
+        if (head_row != ~0u) {
+            // the pieces of this row left open by the threads before, in order
+            int t = (int)tid - 1;
+            while (t >= 0 && sm.cr[t] == head_row) --t;
+            double s = 0.0;
+            for (int v = t + 1; v < (int)tid; ++v) s += sm.cv[v];
+            epi(r0 + head_row, s + head_v);
+        }
+        __syncthreads();
+    }
+}
+
 // Format chosen at compile time so the SELL kernels carry no shared-memory
 // tile (full occupancy); launchers pick the instantiation from A.fmt.
 template <int FMT, class Epi>
@@ -233,6 +338,9 @@ __device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__r
         spmv_rows_sell(A, x, epi);
     } else if constexpr (FMT == HBK_FMT_HYB) {
         spmv_rows_hyb(A, x, epi);
+    } else if constexpr (FMT == HBK_FMT_MERGE) {
+        __shared__ MergeSmem sm;
+        spmv_rows_merge(A, x, epi, sm);
     } else {
         __shared__ SpmvSmem sm;
         spmv_rows_tile(A, x, epi, sm);
@@ -244,6 +352,7 @@ __device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__r
     do {                                                                                    \
         if ((A).fmt == HBK_FMT_SELL) kern<HBK_FMT_SELL><<<grid, block, 0, stream>>>(__VA_ARGS__); \
         else if ((A).fmt == HBK_FMT_HYB) kern<HBK_FMT_HYB><<<grid, block, 0, stream>>>(__VA_ARGS__); \
+        else if ((A).fmt == HBK_FMT_MERGE) kern<HBK_FMT_MERGE><<<grid, block, 0, stream>>>(__VA_ARGS__); \
         else kern<HBK_FMT_TILE><<<grid, block, 0, stream>>>(__VA_ARGS__);                  \
     } while (0)
 

@@ -40,6 +40,10 @@ struct hbicg_matrix {
     size_t slen_off;                    /* entries of the map before the lengths */
     unsigned long long *d_hsptr;
     unsigned nslice, nwrow;
+    /* MERGE form (hbk.h HBK_FMT_MERGE): block row ranges, then the long rows,
+     * in one allocation */
+    unsigned *d_merge;
+    unsigned nmblk, nmlong;
 };
 
 /* message of the last failed call on this thread (hbicg_last_message) */

@@ -909,6 +909,10 @@ int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shi
         k_seed_s<HBK_FMT_SELL><<<wave_grid<k_seed_s<HBK_FMT_SELL>>(A->grid), NT, 0, st>>>(c);
         k_seed_q<<<wave_grid<k_seed_q>(gv), NT, 0, st>>>(c);
         k_seed_y<HBK_FMT_SELL><<<wave_grid<k_seed_y<HBK_FMT_SELL>>(A->grid), NT, 0, st>>>(c);
+    } else if (A->fmt == HBK_FMT_MERGE) {
+        k_seed_s<HBK_FMT_MERGE><<<wave_grid<k_seed_s<HBK_FMT_MERGE>>(A->grid), NT, 0, st>>>(c);
+        k_seed_q<<<wave_grid<k_seed_q>(gv), NT, 0, st>>>(c);
+        k_seed_y<HBK_FMT_MERGE><<<wave_grid<k_seed_y<HBK_FMT_MERGE>>(A->grid), NT, 0, st>>>(c);
     } else if (A->fmt == HBK_FMT_HYB) {
         k_seed_s<HBK_FMT_HYB><<<wave_grid<k_seed_s<HBK_FMT_HYB>>(A->grid), NT, 0, st>>>(c);
         k_seed_q<<<wave_grid<k_seed_q>(gv), NT, 0, st>>>(c);

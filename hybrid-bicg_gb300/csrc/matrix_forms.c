@@ -144,6 +144,99 @@ static void use_hyb(hbicg_matrix *A) {
     A->k.grid = hbk_spmv_grid((A->k.n + HBK_THREADS - 1) / HBK_THREADS);
 }
 
+/* MERGE: rows of at most HBK_MERGE_LONG entries in blocks of consecutive
+ * rows with rows + nonzeros <= HBK_MERGE_ITEMS (a block ends where the next
+ * row would not fit and before every long row); rows above HBK_MERGE_LONG in
+ * a list, longest first (stable), one warp each.  The device splits every
+ * block among its threads along the merge path of row ends and nonzeros, so
+ * each thread gets the same number of items whatever the row lengths: for
+ * power-law rows this needs no sorting, padding or copy of the values. */
+static int build_merge(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
+    if (!n || A->d_merge) return HBICG_OK;
+    size_t nlong = 0, nblk = 0;
+    unsigned items = 0;
+    int open = 0;
+    for (unsigned r = 0; r < n; ++r) {
+        const unsigned len = h_ptr[r + 1] - h_ptr[r];
+        if (len > HBK_MERGE_LONG) {
+            nlong++;
+            open = 0;
+            continue;
+        }
+        if (!open || items + len + 1 > HBK_MERGE_ITEMS) {
+            nblk++;
+            open = 1;
+            items = 0;
+        }
+        items += len + 1;
+    }
+    const size_t words = 2 * nblk + nlong + 1;
+    unsigned *h = malloc(sizeof(unsigned) * words);
+    unsigned long long *key = malloc(sizeof(unsigned long long) * (nlong + 1));
+    int rc = HBICG_OK;
+    if (!h || !key) {
+        rc = HBICG_E_NOMEM;
+        goto done;
+    }
+    {
+        size_t b = 0, l = 0;
+        open = 0;
+        items = 0;
+        for (unsigned r = 0; r < n; ++r) {
+            const unsigned len = h_ptr[r + 1] - h_ptr[r];
+            if (len > HBK_MERGE_LONG) {
+                /* longest first, then by row */
+                key[l++] = ((unsigned long long)(0xFFFFFFFFu - len) << 32) | r;
+                if (open) h[2 * b - 1] = r;
+                open = 0;
+                continue;
+            }
+            if (!open || items + len + 1 > HBK_MERGE_ITEMS) {
+                if (open) h[2 * b - 1] = r;
+                h[2 * b] = r;
+                b++;
+                open = 1;
+                items = 0;
+            }
+            items += len + 1;
+        }
+        if (open) h[2 * b - 1] = n;
+        qsort(key, nlong, sizeof *key, cmp_u64);
+        for (size_t i = 0; i < nlong; ++i) h[2 * nblk + i] = (unsigned)(key[i] & 0xFFFFFFFFu);
+        h[words - 1] = 0;
+    }
+    {
+        cudaStream_t st = A->ctx->stream;
+        cudaError_t e = cudaMalloc((void **)&A->d_merge, sizeof(unsigned) * words);
+        if (!e) e = cudaMemcpyAsync(A->d_merge, h, sizeof(unsigned) * words, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaStreamSynchronize(st);
+        if (e) {
+            set_msg("merge plan: %s", cudaGetErrorString(e));
+            rc = e == cudaErrorMemoryAllocation ? HBICG_E_NOMEM : HBICG_E_CUDA;
+            cudaFree(A->d_merge);
+            A->d_merge = NULL;
+            goto done;
+        }
+    }
+    A->nmblk = (unsigned)nblk;
+    A->nmlong = (unsigned)nlong;
+done:
+    free(h);
+    free(key);
+    return rc;
+}
+
+/* point the kernel view at the MERGE plan */
+static void use_merge(hbicg_matrix *A) {
+    A->k.fmt = HBK_FMT_MERGE;
+    A->k.mblk = A->d_merge;
+    A->k.nmblk = A->nmblk;
+    A->k.mlong = A->d_merge ? A->d_merge + 2 * (size_t)A->nmblk : NULL;
+    A->k.nmlong = A->nmlong;
+    const unsigned units = (A->nmlong + HBK_THREADS / 32 - 1) / (HBK_THREADS / 32) + A->nmblk;
+    A->k.grid = hbk_spmv_grid(units ? units : 1);
+}
+
 /* SELL-32 when every row fits in HBK_SELL_MAX_LEN and padding stays under a
  * third of the nonzeros (rows are short and regular, as in stencils); the CSR
  * row-block path otherwise.  HBICG_SPMV_FORMAT=tile|sell overrides. */
@@ -443,6 +536,7 @@ static void hbicg_matrix_destroy_unretained(hbicg_matrix *A) {
     cudaFree(A->d_srow);
     cudaFree(A->d_wrow);
     cudaFree(A->d_sdiag);
+    cudaFree(A->d_merge);
     free(A);
 }
 
@@ -465,6 +559,7 @@ void hbicg_matrix_destroy(hbicg_matrix *A) {
     cudaFree(A->d_srow);
     cudaFree(A->d_wrow);
     cudaFree(A->d_sdiag);
+    cudaFree(A->d_merge);
     hbicg_context *ctx = A->ctx;
     free(A);
     hbicg__ctx_release(ctx);
@@ -511,7 +606,12 @@ int hbicg_matrix_time_spmv(hbicg_matrix *A, const double *x, double *y, double s
 }
 
 int hbicg_matrix_format(const hbicg_matrix *A) {
-    return A->k.fmt == HBK_FMT_SELL ? HBICG_SPMV_SELL : A->k.fmt == HBK_FMT_HYB ? HBICG_SPMV_HYB : HBICG_SPMV_TILE;
+    switch (A->k.fmt) {
+    case HBK_FMT_SELL: return HBICG_SPMV_SELL;
+    case HBK_FMT_HYB: return HBICG_SPMV_HYB;
+    case HBK_FMT_MERGE: return HBICG_SPMV_MERGE;
+    default: return HBICG_SPMV_TILE;
+    }
 }
 
 static unsigned *host_ptr_copy(hbicg_matrix *A) {
@@ -526,7 +626,19 @@ static unsigned *host_ptr_copy(hbicg_matrix *A) {
 }
 
 int hbicg_matrix_set_format(hbicg_matrix *A, int fmt) {
-    if (!A || (fmt != HBICG_SPMV_TILE && fmt != HBICG_SPMV_SELL && fmt != HBICG_SPMV_HYB)) return HBICG_E_ARG;
+    if (!A || (fmt != HBICG_SPMV_TILE && fmt != HBICG_SPMV_SELL && fmt != HBICG_SPMV_HYB && fmt != HBICG_SPMV_MERGE))
+        return HBICG_E_ARG;
+    if (fmt == HBICG_SPMV_MERGE) {
+        if (!A->d_merge && A->k.n) {
+            unsigned *hp = host_ptr_copy(A);
+            if (!hp) return HBICG_E_NOMEM;
+            int rc = build_merge(A, hp, A->k.n);
+            free(hp);
+            if (rc) return rc;
+        }
+        use_merge(A);
+        return HBICG_OK;
+    }
     if (fmt == HBICG_SPMV_TILE) {
         if (!A->d_blk_row) {
             unsigned *hp = host_ptr_copy(A);
@@ -603,7 +715,7 @@ static int tune_lookup(const char *path, const char *key, double *tile_ms, doubl
         double t, sl;
         if (line[0] == '#') continue;
         if (sscanf(line, "%255s %15s %lf %lf", k, fmt, &t, &sl) == 4 && !strcmp(k, key)) {
-            found = !strcmp(fmt, "sell") ? 1 : !strcmp(fmt, "hyb") ? 2 : 0;
+            found = !strcmp(fmt, "sell") ? 1 : !strcmp(fmt, "hyb") ? 2 : !strcmp(fmt, "merge") ? 3 : 0;
             *tile_ms = t;
             *sell_ms = sl;
         }
@@ -641,26 +753,31 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
         }
         int rc = hbicg_matrix_set_format(A, HBICG_SPMV_TILE);
         if (!rc) rc = hbicg_matrix_time_spmv(A, x, y, 0.0, 10, &t_tile);
-        double t_s = -1.0, t_h = -1.0;
+        double t_s = -1.0, t_h = -1.0, t_m = -1.0;
         if (!rc && hbicg_matrix_set_format(A, HBICG_SPMV_SELL) == HBICG_OK)
             rc = hbicg_matrix_time_spmv(A, x, y, 0.0, 10, &t_s);
         if (!rc && hbicg_matrix_set_format(A, HBICG_SPMV_HYB) == HBICG_OK)
             rc = hbicg_matrix_time_spmv(A, x, y, 0.0, 10, &t_h);
+        if (!rc && hbicg_matrix_set_format(A, HBICG_SPMV_MERGE) == HBICG_OK)
+            rc = hbicg_matrix_time_spmv(A, x, y, 0.0, 10, &t_m);
         cudaFree(x);
         cudaFree(y);
         if (rc) return rc;
         pick = 0;
         double best = t_tile;
-        if (t_s >= 0.0 && t_s < best) {
-            pick = 1;
-            best = t_s;
-        }
-        if (t_h >= 0.0 && t_h < best) pick = 2;
-        /* the packed form's time: SELL-32 where it exists and was not beaten by HYB */
-        t_sell = pick == 2 || t_s < 0.0 ? t_h : t_s;
+        const double tt[4] = {t_tile, t_s, t_h, t_m};
+        for (int f = 1; f < 4; ++f)
+            if (tt[f] >= 0.0 && tt[f] < best) {
+                pick = f;
+                best = tt[f];
+            }
+        /* the packed form's time: the fastest of SELL-32, HYB and MERGE */
+        t_sell = -1.0;
+        for (int f = 1; f < 4; ++f)
+            if (tt[f] >= 0.0 && (t_sell < 0.0 || tt[f] < t_sell)) t_sell = tt[f];
         if (cache_path && *cache_path) {
             char line[512];
-            static const char *names[3] = {"tile", "sell", "hyb"};
+            static const char *names[4] = {"tile", "sell", "hyb", "merge"};
             const int len = snprintf(line, sizeof line, "%s %s %.6f %.6f\n", key, names[pick], t_tile, t_sell);
             pthread_mutex_lock(&g_tune_lock);
             const int fd = open(cache_path, O_WRONLY | O_CREAT | O_APPEND, 0644);
@@ -678,7 +795,8 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
             pthread_mutex_unlock(&g_tune_lock);
         }
     }
-    int rc = hbicg_matrix_set_format(A, pick == 1 ? HBICG_SPMV_SELL : pick == 2 ? HBICG_SPMV_HYB : HBICG_SPMV_TILE);
+    static const int fmts[4] = {HBICG_SPMV_TILE, HBICG_SPMV_SELL, HBICG_SPMV_HYB, HBICG_SPMV_MERGE};
+    int rc = hbicg_matrix_set_format(A, fmts[pick]);
     if (rc) return rc;
     /* give the memory of the forms not chosen back; the kernel view keeps
      * only pointers into the chosen form (SELL-32 and HYB share its
@@ -720,7 +838,16 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
         A->d_scol = NULL;
         A->d_sptr = NULL;
     }
-    if (chosen) *chosen = pick == 1 ? HBICG_SPMV_SELL : pick == 2 ? HBICG_SPMV_HYB : HBICG_SPMV_TILE;
+    if (pick != 3 && A->d_merge) { /* the MERGE plan is not used */
+        cudaStreamSynchronize(A->ctx->stream);
+        cudaFree(A->d_merge);
+        A->d_merge = NULL;
+        A->k.mblk = NULL;
+        A->k.mlong = NULL;
+        A->k.nmblk = 0;
+        A->k.nmlong = 0;
+    }
+    if (chosen) *chosen = fmts[pick];
     if (tile_ms) *tile_ms = t_tile;
     if (sell_ms) *sell_ms = t_sell;
     return HBICG_OK;

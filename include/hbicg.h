@@ -128,11 +128,13 @@ int hbicg_matrix_time_spmv(hbicg_matrix *A, const double *x, double *y, double s
 
 /* SpMV form of a matrix: CSR row blocks staged in shared memory (TILE);
  * SELL-32, slices of 32 consecutive rows padded to their longest row (rows of
- * at most 64 entries, padding under a third of the nonzeros); or HYB, rows of
+ * at most 64 entries, padding under a third of the nonzeros); HYB, rows of
  * at most 32 entries in SELL-32 slices sorted by length inside windows of 256
- * rows and longer rows one warp each.  A new matrix takes SELL-32 where it
- * qualifies, else HYB. */
-typedef enum { HBICG_SPMV_TILE = 0, HBICG_SPMV_SELL = 1, HBICG_SPMV_HYB = 2 } hbicg_spmv_format;
+ * rows and longer rows one warp each; or MERGE, rows of at most 192 entries in
+ * blocks of 1536 row ends + nonzeros split evenly among 256 threads along the
+ * merge path (nonzero-balanced, no copy of the values), longer rows one warp
+ * each.  A new matrix takes SELL-32 where it qualifies, else MERGE. */
+typedef enum { HBICG_SPMV_TILE = 0, HBICG_SPMV_SELL = 1, HBICG_SPMV_HYB = 2, HBICG_SPMV_MERGE = 3 } hbicg_spmv_format;
 int hbicg_matrix_format(const hbicg_matrix *A);
 /* Switch the SpMV form (builds that form's copy if needed; HBICG_E_ARG when a
  * row is too long for SELL-32).  Call before creating solvers on A. */

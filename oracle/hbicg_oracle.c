@@ -16,6 +16,7 @@
 #include "hbicg_oracle.h"
 
 #include <math.h>
+#include <omp.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -168,6 +169,7 @@ int hbo_shifted_bicgstab(unsigned n, const unsigned *ptr, const unsigned *col, c
     if (tr) {
         tr->n_sw = 0;
         if (tr->conv_k) memset(tr->conv_k, 0, sizeof(int) * m);
+        if (tr->t_iter && tr->t_cap > 0) tr->t_iter[0] = omp_get_wtime();
     }
 
 #pragma omp parallel
@@ -318,6 +320,7 @@ int hbo_shifted_bicgstab(unsigned n, const unsigned *ptr, const unsigned *col, c
                     }
                     if (tr) tr->n_sw++;
                 }
+                if (tr && tr->t_iter && k < tr->t_cap) tr->t_iter[k] = omp_get_wtime();
                 k++;
             }
 #pragma omp barrier

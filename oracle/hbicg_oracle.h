@@ -42,6 +42,10 @@ typedef struct {
      * a switch) and (r, r) at the end of iteration k */
     double *a_hist, *b_hist, *w_hist, *rr_hist;
     int hist_cap;
+    /* optional wall-clock stamps (omp_get_wtime, seconds): t_iter[0] when the
+     * iterations start (after the set-up), t_iter[k] at the end of iteration k */
+    double *t_iter;
+    int t_cap;
 } hbo_trace;
 
 /* y = A x for a square CSR matrix (32-bit indices): each row summed in stored

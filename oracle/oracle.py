@@ -43,7 +43,7 @@ class _Opts(C.Structure):
 class _Trace(C.Structure):
     _fields_ = [("sw_k", _PI), ("sw_seed", _PI), ("sw_cap", C.c_int), ("n_sw", C.c_int), ("act", _PI),
                 ("act_cap", C.c_int), ("conv_k", _PI), ("final_seed", C.c_int), ("a_hist", _PD), ("b_hist", _PD),
-                ("w_hist", _PD), ("rr_hist", _PD), ("hist_cap", C.c_int)]
+                ("w_hist", _PD), ("rr_hist", _PD), ("hist_cap", C.c_int), ("t_iter", _PD), ("t_cap", C.c_int)]
 
 
 @dataclass
@@ -122,10 +122,10 @@ def solve(a, b, sigma, seed=0, tol=1e-12, max_iter=2000, switching=True, schedul
     sws = np.zeros(cap, dtype=np.int32)
     act = np.zeros(max_iter + 2, dtype=np.int32)
     conv = np.zeros(max(m, 1), dtype=np.int32)
-    hist = {key: np.zeros(max_iter + 2) for key in ("alpha", "beta", "omega", "rr")}
+    hist = {key: np.zeros(max_iter + 2) for key in ("alpha", "beta", "omega", "rr", "t")}
     tr = _Trace(_p(swk, _PI), _p(sws, _PI), cap, 0, _p(act, _PI), act.shape[0], _p(conv, _PI), 0,
                 _p(hist["alpha"], _PD), _p(hist["beta"], _PD), _p(hist["omega"], _PD), _p(hist["rr"], _PD),
-                max_iter + 2)
+                max_iter + 2, _p(hist["t"], _PD), max_iter + 2)
     opts = _Opts(float(tol), int(max_iter), 1 if switching else 0, SCHEDULES[schedule])
     k = lib().hbo_shifted_bicgstab(n, _p(ptr, _PU), _p(col, _PU), _p(val, _PD), _p(x, _PD), _p(r, _PD),
                                    _p(sig, _PD), m, int(seed), C.byref(opts), C.byref(tr))

@@ -25,6 +25,21 @@ def _check_line(d):
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == "s"
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    # one complete solve measured, its steps consecutive iteration ranges of it
+    assert d["measured"] is True
+    assert len(d["step_s"]) == d["steps"] and abs(sum(d["step_s"]) - d["value"]) < 0.01 + 1e-3 * d["value"]
+    assert d["timed_region_s"] == d["value"] and d["max_true_residual"] <= 1e-10 * 1.01
+    assert d["config"]["workload"].startswith("c1: 1000 rows")
+
+
+def test_reference_arm_splits_one_solve_into_steps():
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "c1", "--scale", "12",
+                        "--steps", "5", "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    (d,) = _json_lines(r.stdout)
+    assert d["steps"] == 5 and len(d["step_s"]) == 5 and all(t >= 0 for t in d["step_s"])
+    assert abs(sum(d["step_s"]) - d["value"]) < 0.01 + 1e-3 * d["value"]
+    assert abs(d["ms_per_step"] - d["value"] * 1e3 / 5) < 1e-6 * d["value"] * 1e3
 
 
 def test_reference_arm_one_process():

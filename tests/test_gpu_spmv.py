@@ -156,3 +156,113 @@ def test_dropin_mult_accumulates(cuda, pkg, oracle):
     y0 = np.random.default_rng(9).standard_normal(a.n)
     y = pkg.mult(a, x, y0.copy())
     assert np.max(np.abs(y - (y0 + oracle.spmv_fma(a, x)))) <= 1e-14 * np.max(np.abs(y))
+
+
+# ---- MERGE form: nonzero-balanced blocks (merge-path split among threads)
+MERGE_IPT, MERGE_ITEMS, MERGE_LONG = 6, 256 * 6, 192
+
+
+def merge_whole_rows(ptr):
+    """Rows the MERGE form sums in one thread (same bits as the stored-order
+    FMA sum): the host plan (blocks of consecutive rows of <= 192 entries with
+    rows + nonzeros <= 1536, cut before every longer row) restated, then
+    inside a block row i's nonzeros are merge items i + ptr-offsets and its end
+    item i + end offset; the row is whole when its first nonzero and its end
+    item fall in the same thread's run of 6 items.  Empty rows are exact zeros
+    whoever ends them."""
+    lens = np.diff(ptr.astype(np.int64))
+    n = lens.shape[0]
+    whole = np.zeros(n, dtype=bool)
+    blocks, open_, items, r0 = [], False, 0, 0
+    for r in range(n):
+        ln = int(lens[r])
+        if ln > MERGE_LONG:
+            if open_:
+                blocks.append((r0, r))
+            open_ = False
+            continue
+        if not open_ or items + ln + 1 > MERGE_ITEMS:
+            if open_:
+                blocks.append((r0, r))
+            r0, open_, items = r, True, 0
+        items += ln + 1
+    if open_:
+        blocks.append((r0, n))
+    for (a, b) in blocks:
+        rel_end = ptr[a + 1:b + 1].astype(np.int64) - int(ptr[a])
+        rel_start = ptr[a:b].astype(np.int64) - int(ptr[a])
+        i = np.arange(b - a)
+        first = (i + rel_start) // MERGE_IPT
+        last = (i + rel_end) // MERGE_IPT
+        whole[a:b] = (first == last) | (rel_end == rel_start)
+    return whole, lens > MERGE_LONG
+
+
+def _check_merge(y, want, a, x):
+    whole, long_ = merge_whole_rows(a.ptr)
+    assert np.array_equal(y[whole], want[whole])
+    lens = np.diff(a.ptr.astype(np.int64))
+    scale = np.abs(a.val).max(initial=0.0) * np.abs(x).max() * np.maximum(lens, 1)
+    assert np.all(np.abs(y - want) <= 1e-15 * scale)
+    return whole, long_
+
+
+def test_merge_powerlaw(cuda, pkg, oracle):
+    """Power-law rows in the MERGE form: rows a thread sums whole are
+    bit-exact, rows cut between threads (a sum of stored-order FMA pieces in
+    thread order) and long rows (one warp, fixed tree) within rounding."""
+    a = pkg.workloads.irregular_powerlaw(200000, seed=2)
+    x = np.random.default_rng(1).standard_normal(a.n)
+    y = _gpu_spmv(pkg, a, x, fmt="merge", want_fmt="merge")
+    whole, long_ = _check_merge(y, oracle.spmv_fma(a, x), a, x)
+    assert whole.sum() > 0.2 * a.n and (~whole & ~long_).sum() > 0 and long_.sum() > 0
+
+
+@pytest.mark.parametrize("case", ["boundaries", "all_long", "all_empty", "one_row", "full_blocks", "mixed_empty"])
+def test_merge_shapes(cuda, pkg, oracle, case):
+    """MERGE edge cases: rows of exactly 192 and 193 entries (the long-row
+    limit), blocks filled to the last item, only long rows, only empty rows,
+    a single row, runs of empty rows between long ones."""
+    rng = np.random.default_rng(len(case) + 11)
+    if case == "boundaries":
+        n = 3000
+        lens = rng.choice([0, 1, 5, 6, 7, 191, 192, 193, 194, 1500], size=n)
+    elif case == "all_long":
+        n = 200
+        lens = rng.integers(193, 3000, n)
+    elif case == "all_empty":
+        n = 4000
+        lens = np.zeros(n, dtype=np.int64)
+    elif case == "one_row":
+        n = 1
+        lens = np.array([1])
+    elif case == "full_blocks":
+        n = 64
+        lens = np.full(n, 191)  # 8 rows x 192 items = one full block
+    else:
+        n = 5000
+        lens = np.where(rng.random(n) < 0.02, 400, 0)
+        lens[rng.random(n) < 0.3] = 3
+    a = _random_csr(pkg, n, lens, seed=5)
+    x = rng.standard_normal(n)
+    y = _gpu_spmv(pkg, a, x, fmt="merge", want_fmt="merge")
+    _check_merge(y, oracle.spmv_fma(a, x), a, x)
+
+
+def test_merge_in_the_solver(cuda, pkg, oracle):
+    """A shifted solve with the matrix in the MERGE form (fused, incremental
+    and deferred) reaches the reference's solutions."""
+    g = golden("irregular_fixed_seed")
+    a = GoldenCsr(g)
+    for mode in ("incremental", "deferred"):
+        ctx = pkg.Context()
+        A = pkg.Matrix(ctx, a.ptr, a.col, a.val)
+        A.set_format("merge")
+        s = pkg.Solver(A, len(g["sigma"]), tol=float(g["tol"]), max_iter=int(g["max_iter"]),
+                       switching=bool(g["switching"]), shift_mode=mode, refine=False)
+        res = s.run(g["b"], g["sigma"], seed=int(g["seed"]))
+        s.close()
+        A.close()
+        ctx.close()
+        err = np.max(np.abs(np.asarray(res.x) - g["x"])) / np.max(np.abs(g["x"]))
+        assert err < 1e-8, (mode, err)
