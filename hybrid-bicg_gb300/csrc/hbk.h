@@ -42,10 +42,10 @@ extern "C" {
 #define HBK_FMT_HYB 2        /* short rows in SELL-32 slices (length-sorted inside windows), long rows one warp each */
 #define HBK_HYB_SHORT 32     /* longest row of a HYB slice */
 #define HBK_HYB_WINDOW 256   /* rows are sorted by length only inside windows of this many consecutive rows */
-#define HBK_FMT_MERGE 3      /* CSR; rows up to HBK_MERGE_LONG entries in merge-path blocks, longer rows one warp each */
+#define HBK_FMT_MERGE 3      /* CSR; rows up to HBK_MERGE_LONG entries in merge-path blocks, longer rows one CTA each */
 #define HBK_MERGE_IPT 6      /* merge items (row ends + nonzeros) per thread of a block */
 #define HBK_MERGE_ITEMS (HBK_THREADS * HBK_MERGE_IPT) /* items per block */
-#define HBK_MERGE_LONG 192   /* longest row a merge block takes */
+#define HBK_MERGE_LONG (HBK_MERGE_ITEMS - 1) /* longest row a merge block takes (the row and its end fill it) */
 
 typedef struct {
     unsigned n, nnz;
@@ -67,7 +67,7 @@ typedef struct {
     unsigned nwrow;
     const unsigned *mblk;      /* MERGE: [2 nmblk] first and end row of each block of short rows */
     unsigned nmblk;
-    const unsigned *mlong;     /* MERGE: rows longer than HBK_MERGE_LONG, longest first, one warp each */
+    const unsigned *mlong;     /* MERGE: rows longer than HBK_MERGE_LONG, longest first, one CTA each */
     unsigned nmlong;
 } hbk_matrix;
 
@@ -178,6 +178,8 @@ int hbk_spmv_accumulate(const hbk_matrix *A, const double *x, double *y, cudaStr
 /* Host: split rows into blocks (counts only when blk_row is NULL). */
 unsigned hbk_plan_rows(unsigned n, const unsigned *ptr_host, unsigned *blk_row, unsigned char *blk_kind);
 int hbk_spmv_grid(unsigned nblk);
+/* MERGE form: CTAs of one wave of the product kernel, at most `units` */
+int hbk_merge_grid(unsigned units);
 /* SELL-32 build on the device: widths of the ceil(n/32) slices into w ... */
 int hbk_sell_widths(unsigned n, const unsigned *ptr, unsigned *w, cudaStream_t st);
 /* ... then, with sptr = exclusive prefix sum of 32*w (host), fill the arrays */

@@ -226,26 +226,34 @@ __device__ __forceinline__ void spmv_rows_hyb(const hbk_matrix &A, const double 
 }
 
 // MERGE path: nonzero-balanced work inside row blocks (merge-path
-// decomposition).  The host cuts the short rows (<= HBK_MERGE_LONG entries)
-// into blocks of consecutive rows with rows + nonzeros <= HBK_MERGE_ITEMS;
-// rows longer than that are listed apart (longest first).  Work units, in
-// order: groups of NW long rows (one warp per row, lanes take every 32nd entry
-// in stored order, fixed shuffle tree), then the blocks.  A block is staged in
+// decomposition).  The host cuts the rows of at most HBK_MERGE_LONG entries
+// into blocks of consecutive rows with rows + nonzeros <= HBK_MERGE_ITEMS and
+// lists the longer rows apart (longest first).  Work units, in order: the long
+// rows, one CTA each (thread t sums entries t, t + NT, ... in stored order with
+// FMAs, then a fixed tree over the CTA), then the blocks.  A block is staged in
 // shared memory with coalesced loads (values, the gathered x values, the row
-// end offsets); thread t then walks items [t IPT, (t + 1) IPT) of the merge of
-// the row ends with the nonzeros, so every thread gets the same number of
-// (row end + nonzero) items whatever the row lengths.  A row that starts and
-// ends inside one thread is summed by that thread in stored order with FMAs
-// from 0 (the other paths' arithmetic); a row cut between threads is the sum,
-// in thread order, of its pieces (each an FMA chain in stored order).  Either
-// way `epi(row, acc)` runs once per row.
+// end offsets; every load of a thread issued before the first one is used);
+// thread t then walks items [t IPT, (t + 1) IPT) of the merge of the row ends
+// with the nonzeros, so every thread gets the same number of (row end +
+// nonzero) items whatever the row lengths.  A row that starts and ends inside
+// one thread is summed by that thread in stored order with FMAs from 0 (the
+// other paths' arithmetic); a row cut between threads is the sum of its
+// pieces (each an FMA chain in stored order) over a fixed segmented-scan tree.
+// Either way `epi(row, acc)` runs once per row.  Units are dealt to the CTAs
+// round-robin, the grid is one wave.
 struct MergeSmem {
     double val[HBK_MERGE_ITEMS];
     double xv[HBK_MERGE_ITEMS];
     unsigned rend[HBK_MERGE_ITEMS];  // end of each row of the block, relative to its first nonzero
-    double cv[NT];                   // piece of the row a thread leaves open
-    unsigned cr[NT];                 // that row (relative), or ~0u
+    double inc[NT];                  // per thread: running sum of its open row's pieces up to itself
+    unsigned key[NT];                // that row (relative), or a value >= 2^31 when none
+    double wv[NW];                   // per warp: the same at its last lane
+    unsigned wk[NW];
+    int wf[NW];                      // the warp's last run starts inside the warp
+    double red[2 * NW];
 };
+
+constexpr unsigned kNoRow = 0x80000000u;
 
 template <class Epi>
 __device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const double *__restrict__ x, Epi &epi,
@@ -254,32 +262,57 @@ __device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const doubl
     const unsigned *__restrict__ col = A.col;
     const double *__restrict__ val = A.val;
     const unsigned tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const unsigned long_units = (A.nmlong + NW - 1) / NW;
-    const unsigned units = long_units + A.nmblk;
+    const unsigned units = A.nmlong + A.nmblk;
     for (unsigned u = blockIdx.x; u < units; u += gridDim.x) {
-        if (u < long_units) {
-            const unsigned it = u * NW + warp;
-            if (it < A.nmlong) {
-                const unsigned r = __ldg(A.mlong + it);
-                const unsigned e1 = __ldg(ptr + r + 1);
-                double acc = 0.0;
-                for (unsigned e = __ldg(ptr + r) + lane; e < e1; e += 32)
-                    acc = fma(__ldg(val + e), __ldg(x + __ldg(col + e)), acc);
-                acc = warp_sum(acc);
-                if (lane == 0) epi(r, acc);
+        if (u < A.nmlong) {
+            // one long row, the whole CTA: four loads ahead, one FMA chain per thread
+            const unsigned r = __ldg(A.mlong + u);
+            const unsigned e0 = __ldg(ptr + r), e1 = __ldg(ptr + r + 1);
+            double acc = 0.0;
+            for (unsigned e = e0 + tid; e < e1; e += 4 * NT) {
+                double v[4], xx[4];
+                unsigned c[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const unsigned ek = e + k * NT;
+                    c[k] = ek < e1 ? __ldg(col + ek) : 0u;
+                    v[k] = ek < e1 ? __ldg(val + ek) : 0.0;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) xx[k] = e + k * NT < e1 ? __ldg(x + c[k]) : 0.0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (e + k * NT < e1) acc = fma(v[k], xx[k], acc);
             }
-            continue;  // warp-uniform: no barrier in this unit
+            acc = block_sum(acc, sm.red);
+            if (tid == 0) epi(r, acc);
+            __syncthreads();
+            continue;
         }
-        const unsigned b = u - long_units;
+        const unsigned b = u - A.nmlong;
         const unsigned r0 = __ldg(A.mblk + 2 * b), r1 = __ldg(A.mblk + 2 * b + 1);
         const unsigned e0 = __ldg(ptr + r0);
         const unsigned nr = r1 - r0, nz = __ldg(ptr + r1) - e0;
-        for (unsigned e = tid; e < nz; e += NT) {
-            const unsigned c = __ldg(col + e0 + e);
-            sm.val[e] = __ldg(val + e0 + e);
-            sm.xv[e] = __ldg(x + c);
+        {
+            unsigned c[HBK_MERGE_IPT], re[HBK_MERGE_IPT];
+            double v[HBK_MERGE_IPT];
+#pragma unroll
+            for (int k = 0; k < HBK_MERGE_IPT; ++k) {
+                const unsigned e = tid + k * NT;
+                c[k] = e < nz ? __ldg(col + e0 + e) : 0u;
+                v[k] = e < nz ? __ldg(val + e0 + e) : 0.0;
+                re[k] = e < nr ? __ldg(ptr + r0 + e + 1) : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < HBK_MERGE_IPT; ++k) {
+                const unsigned e = tid + k * NT;
+                if (e < nz) {
+                    sm.xv[e] = __ldg(x + c[k]);
+                    sm.val[e] = v[k];
+                }
+                if (e < nr) sm.rend[e] = re[k] - e0;
+            }
         }
-        for (unsigned i = tid; i < nr; i += NT) sm.rend[i] = __ldg(ptr + r0 + i + 1) - e0;
         __syncthreads();
         const unsigned tot = nr + nz;
         const unsigned d0 = min(tid * (unsigned)HBK_MERGE_IPT, tot);
@@ -293,9 +326,8 @@ __device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const doubl
         }
         unsigned i = lo, e = d0 - lo;
         // the thread starts inside row i when entries of that row precede e
-        const bool head_open = e > (i ? sm.rend[i - 1] : 0u);
-        bool head = head_open, open = false;
-        unsigned head_row = ~0u;
+        bool head = e > (i ? sm.rend[i - 1] : 0u), open = false;
+        unsigned head_row = kNoRow;
         double head_v = 0.0, acc = 0.0;
         for (unsigned d = d0; d < d1; ++d) {
             if (i < nr && sm.rend[i] <= e) {
@@ -315,20 +347,49 @@ __device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const doubl
                 open = true;
             }
         }
-        sm.cr[tid] = open ? i : ~0u;
-        sm.cv[tid] = acc;
+        // segmented inclusive scan of the open pieces over the threads, keyed
+        // by row: inside the warp by shuffles, then across warps
+        const unsigned key = open ? i : (kNoRow | tid);
+        double s = open ? acc : 0.0;
+        const unsigned kprev = __shfl_up_sync(0xffffffffu, key, 1);
+        bool f = lane > 0 && kprev != key;  // a run starts here (lane 0: maybe not)
+#pragma unroll
+        for (int dd = 1; dd < 32; dd <<= 1) {
+            const double so = __shfl_up_sync(0xffffffffu, s, dd);
+            const bool fo = __shfl_up_sync(0xffffffffu, f, dd);
+            if ((int)lane >= dd && !f) {
+                s = so + s;
+                f = fo;
+            }
+        }
+        if (lane == 31) {
+            sm.wk[warp] = key;
+            sm.wv[warp] = s;
+            sm.wf[warp] = f;
+        }
         __syncthreads();
-        if (head_row != ~0u) {
-            // the pieces of this row left open by the threads before, in order
-            int t = (int)tid - 1;
-            while (t >= 0 && sm.cr[t] == head_row) --t;
-            double s = 0.0;
-            for (int v = t + 1; v < (int)tid; ++v) s += sm.cv[v];
-            epi(r0 + head_row, s + head_v);
+        if (!f && !(key & kNoRow)) {
+            // the run reaches lane 0: add what the earlier warps hold of it
+            double carry = 0.0;
+            for (int w = (int)warp - 1; w >= 0; --w) {
+                if (sm.wk[w] != key) break;
+                carry = sm.wv[w] + carry;
+                if (sm.wf[w]) break;
+            }
+            s = carry + s;
+        }
+        sm.key[tid] = key;
+        sm.inc[tid] = s;
+        __syncthreads();
+        if (head_row != kNoRow) {
+            // the pieces of this row left open by the threads before
+            const double before = (tid > 0 && sm.key[tid - 1] == head_row) ? sm.inc[tid - 1] : 0.0;
+            epi(r0 + head_row, before + head_v);
         }
         __syncthreads();
     }
 }
+
 
 // Format chosen at compile time so the SELL kernels carry no shared-memory
 // tile (full occupancy); launchers pick the instantiation from A.fmt.

@@ -281,6 +281,14 @@ int hbk_spmv_grid(unsigned nblk) {
     return g < 1 ? 1 : g;
 }
 
+// MERGE form: one wave of the product kernel (its units are dealt round-robin,
+// so a second wave would wait for whole CTAs of the first)
+int hbk_merge_grid(unsigned units) {
+    const int w = wave_grid<k_spmv<HBK_FMT_MERGE>>(HBK_MAX_GRID);
+    const int g = units < (unsigned)w ? (int)units : w;
+    return g < 1 ? 1 : g;
+}
+
 int hbk_spmv(const hbk_matrix *A, const double *x, double *y, double sigma, int sigma_add, cudaStream_t st) {
     if (!A->n) return 0;
     HBK_LAUNCH_FMT(*A, k_spmv, A->grid, NT, st, *A, x, y, sigma, sigma_add);

@@ -430,7 +430,9 @@ __device__ void seed_step_scalars(const Ctx &c, double rr, double rrh) {
 }
 
 // K4: x_s += alpha p_s + omega q ; r_k = q - omega y ; (r,r), (r^,r)
-__global__ void __launch_bounds__(NT) k_seed_update(Ctx c) {
+// (at least 4 CTAs per SM: the streaming loop needs the warps; the scalar
+// stage that runs in one CTA per iteration may spill)
+__global__ void __launch_bounds__(NT, 4) k_seed_update(Ctx c) {
     __shared__ double sh[2 * NW];
     __shared__ unsigned long long smx[NW];
     hbk_scalars *sc = c.sh.sc;

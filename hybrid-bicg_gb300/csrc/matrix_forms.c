@@ -147,7 +147,7 @@ static void use_hyb(hbicg_matrix *A) {
 /* MERGE: rows of at most HBK_MERGE_LONG entries in blocks of consecutive
  * rows with rows + nonzeros <= HBK_MERGE_ITEMS (a block ends where the next
  * row would not fit and before every long row); rows above HBK_MERGE_LONG in
- * a list, longest first (stable), one warp each.  The device splits every
+ * a list, longest first (stable), one CTA each.  The device splits every
  * block among its threads along the merge path of row ends and nonzeros, so
  * each thread gets the same number of items whatever the row lengths: for
  * power-law rows this needs no sorting, padding or copy of the values. */
@@ -233,8 +233,7 @@ static void use_merge(hbicg_matrix *A) {
     A->k.nmblk = A->nmblk;
     A->k.mlong = A->d_merge ? A->d_merge + 2 * (size_t)A->nmblk : NULL;
     A->k.nmlong = A->nmlong;
-    const unsigned units = (A->nmlong + HBK_THREADS / 32 - 1) / (HBK_THREADS / 32) + A->nmblk;
-    A->k.grid = hbk_spmv_grid(units ? units : 1);
+    A->k.grid = hbk_merge_grid(A->nmlong + A->nmblk);
 }
 
 /* SELL-32 when every row fits in HBK_SELL_MAX_LEN and padding stays under a

@@ -197,8 +197,9 @@ def digest_indices(n: int, count: int = DIGEST_SAMPLES) -> np.ndarray:
     return np.unique(np.concatenate([idx, [0, n - 1]])).astype(np.int64)
 
 
-def solution_digest(name: str = "c2") -> None:
-    """Digest of the reference's own full solve of a named workload.
+def solution_digest(name: str = "c2", scale: int | None = None) -> None:
+    """Digest of the reference's own full solve of a named workload (at its
+    full size, or at grid side `scale`: file <name>_<scale>_digest.npz).
 
     The reference (oracle/_ref/libref.so, its sources compiled single-rank) runs
     the whole family to convergence with the workload's tolerance; the digest
@@ -210,23 +211,24 @@ def solution_digest(name: str = "c2") -> None:
 
     O.build(ref=True)
     wl = _workloads()
-    f = wl.family(name)
+    f = wl.family(name, scale)
     t0 = time.perf_counter()
     res = O.ref_solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=f.max_iter, variant="dynamic")
     secs = time.perf_counter() - t0
     idx = digest_indices(f.a.n)
     tr = O.true_residuals(f.a, res.x, f.b, f.sigma)
     sw = np.array(res.switches, dtype=np.int64).reshape(-1, 2)
-    np.savez_compressed(OUT / f"{name}_digest.npz", k=res.k, switches=sw, sigma=f.sigma, idx=idx,
+    tag = name if scale is None else f"{name}_{scale}"
+    np.savez_compressed(OUT / f"{tag}_digest.npz", k=res.k, switches=sw, sigma=f.sigma, idx=idx,
                         x_at=res.x[:, idx], norm=np.linalg.norm(res.x, axis=1), sum=res.x.sum(axis=1),
                         true_residual=tr, r_at=res.r[idx], seconds=secs)
-    print(f"{name}: k={res.k} switches={res.switches} max true residual={tr.max():.3e} ({secs:.0f} s)")
+    print(f"{tag}: k={res.k} switches={res.switches} max true residual={tr.max():.3e} ({secs:.0f} s)")
 
 
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[1] == "--profile":
         convergence_profile(sys.argv[2])
     elif len(sys.argv) > 2 and sys.argv[1] == "--digest":
-        solution_digest(sys.argv[2])
+        solution_digest(sys.argv[2], int(sys.argv[3]) if len(sys.argv) > 3 else None)
     else:
         main()

@@ -159,13 +159,14 @@ def test_dropin_mult_accumulates(cuda, pkg, oracle):
 
 
 # ---- MERGE form: nonzero-balanced blocks (merge-path split among threads)
-MERGE_IPT, MERGE_ITEMS, MERGE_LONG = 6, 256 * 6, 192
+MERGE_IPT, MERGE_ITEMS = 6, 256 * 6
+MERGE_LONG = MERGE_ITEMS - 1
 
 
 def merge_whole_rows(ptr):
     """Rows the MERGE form sums in one thread (same bits as the stored-order
-    FMA sum): the host plan (blocks of consecutive rows of <= 192 entries with
-    rows + nonzeros <= 1536, cut before every longer row) restated, then
+    FMA sum): the host plan (blocks of consecutive rows of <= 1535 entries
+    with rows + nonzeros <= 1536, cut before every longer row) restated, then
     inside a block row i's nonzeros are merge items i + ptr-offsets and its end
     item i + end offset; the row is whole when its first nonzero and its end
     item fall in the same thread's run of 6 items.  Empty rows are exact zeros
@@ -220,16 +221,17 @@ def test_merge_powerlaw(cuda, pkg, oracle):
 
 @pytest.mark.parametrize("case", ["boundaries", "all_long", "all_empty", "one_row", "full_blocks", "mixed_empty"])
 def test_merge_shapes(cuda, pkg, oracle, case):
-    """MERGE edge cases: rows of exactly 192 and 193 entries (the long-row
-    limit), blocks filled to the last item, only long rows, only empty rows,
-    a single row, runs of empty rows between long ones."""
+    """MERGE edge cases: rows of exactly 1535 and 1536 entries (the long-row
+    limit: a row and its end fill a block), rows cut across many threads and
+    warps, blocks filled to the last item, only long rows, only empty rows, a
+    single row, runs of empty rows between long ones."""
     rng = np.random.default_rng(len(case) + 11)
     if case == "boundaries":
         n = 3000
-        lens = rng.choice([0, 1, 5, 6, 7, 191, 192, 193, 194, 1500], size=n)
+        lens = rng.choice([0, 1, 5, 6, 7, 191, 192, 193, 700, 1534, 1535, 1536, 1537, 4000], size=n)
     elif case == "all_long":
         n = 200
-        lens = rng.integers(193, 3000, n)
+        lens = rng.integers(1536, 6000, n)
     elif case == "all_empty":
         n = 4000
         lens = np.zeros(n, dtype=np.int64)
@@ -241,8 +243,9 @@ def test_merge_shapes(cuda, pkg, oracle, case):
         lens = np.full(n, 191)  # 8 rows x 192 items = one full block
     else:
         n = 5000
-        lens = np.where(rng.random(n) < 0.02, 400, 0)
+        lens = np.where(rng.random(n) < 0.02, 2000, 0)
         lens[rng.random(n) < 0.3] = 3
+        lens[rng.random(n) < 0.05] = 400
     a = _random_csr(pkg, n, lens, seed=5)
     x = rng.standard_normal(n)
     y = _gpu_spmv(pkg, a, x, fmt="merge", want_fmt="merge")
