@@ -595,6 +595,12 @@ def run_batch_c4(args, dist: Dist):
                                                                              + 8 * len(f.sigma) for f in fams)),
                     "d2h_bytes_per_step": int(sum(8 * len(f.sigma) * f.a.n for f in fams))},
             "clocks": clk.summary(), "cpu_baseline": None}
+    # the same families one after another through the same API on the same
+    # GPU (one worker: one family on the device at a time), once
+    seq_res, seq_wall = pkg.batch_solve(fams, workers=1, **kw)
+    line["sequential"] = {"value": seq_wall, "unit": "s", "families_per_s": 256 / seq_wall,
+                          "status_failures": sum(r.status != 0 for r in seq_res),
+                          "batched_speedup": seq_wall / value}
     if not args.no_cpu_baseline:
         orc = graft.load_oracle()
         orc.build(ref=False)

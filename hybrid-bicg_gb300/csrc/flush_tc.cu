@@ -25,9 +25,10 @@
 // values for all shifts lie in one contiguous block); 128 output rows per
 // group of 64 shifts, ordered so that
 // TMEM lanes 32q..32q+15 hold the x rows of shifts 16q..16q+15 and lanes
-// 32q+16..32q+31 their p rows.  Warps 0-3 make the basis digits of a tile
-// and thread 0 issues its MMAs (M=128, N up to 256, K=16; 52 per tile) into
-// nine accumulators; warps 4-15 empty the accumulators into registers first, so
+// 32q+16..32q+31 their p rows.  Warps 0-2 make the basis digits of a tile;
+// one thread of warp 3 issues its MMAs (M=128, N up to 256, K=16; 52 per
+// tile) into nine accumulators, so that the digit builders never wait behind
+// the MMA issue; warps 4-15 empty the accumulators into registers first, so
 // that the next tile's MMAs run while they round, add the own-vector terms
 // and write x and p.  Every wait is bounded: a timeout sets an error flag,
 // the CTA skips its remaining work and still frees its TMEM.
@@ -57,13 +58,15 @@ constexpr int A_SLICE = TC_M * TC_K * 2;  // 16384 B
 constexpr int B_SLICE = TC_N * TC_K * 2;  // 6144 B
 constexpr int A_BYTES = NDIG * A_SLICE;   // 147456 B
 constexpr int B_BYTES = NDIG * B_SLICE;   // 55296 B
-constexpr int BUILD_WARPS = 4;            // warps 0-3: basis digits + MMA issue
+constexpr int BUILD_WARPS = 3;            // warps 0-2: basis digits
+constexpr int MMA_WARP = 3;               // warp 3: coefficient copy + MMA issue (one thread)
+constexpr int EPI_WARP0 = MMA_WARP + 1;   // first epilogue warp (a multiple of 4: warp w reads TMEM quadrant w % 4)
 constexpr int EPI_WARPS = 12;             // warps 4-15: epilogue
-constexpr int TC_THREADS = 32 * (BUILD_WARPS + EPI_WARPS);
+constexpr int TC_THREADS = 32 * (BUILD_WARPS + 1 + EPI_WARPS);
 constexpr int BUILD_THREADS = 32 * BUILD_WARPS;
 constexpr int EPI_COLS = TC_N / (EPI_WARPS / 4);  // 16 columns per epilogue thread
 constexpr int ITEMS = (TC_K / 8) * TC_N;          // (slot octet, element) pairs per tile
-constexpr int ITEMS_PER = ITEMS / BUILD_THREADS;  // 3
+constexpr int ITEMS_PER = ITEMS / BUILD_THREADS;  // 4
 constexpr int TMEM_COLS = 512;
 constexpr int SMEM_MISC = 6144;
 constexpr int SMEM_BYTES = A_BYTES + B_BYTES + SMEM_MISC;
@@ -80,6 +83,8 @@ constexpr uint64_t MID_BIAS = (uint64_t)MAGIC_BITS * 66052ull;   // * (2^16 + 2^
 constexpr uint64_t T_BIAS = (HI_BIAS << 23) + MID_BIAS;          // (mod 2^64)
 
 static_assert(ITEMS % BUILD_THREADS == 0, "builder items");
+static_assert(EPI_WARP0 % 4 == 0 && EPI_WARP0 + EPI_WARPS == TC_THREADS / 32, "epilogue warps: whole quadrant sets");
+static_assert((TC_THREADS / 32 - 1 - EPI_WARP0) / 4 == EPI_WARPS / 4 - 1, "epilogue column groups");
 static_assert(EPI_COLS % 4 == 0 && TC_N % 8 == 0, "epilogue columns");
 static_assert(NDIAG * TC_N <= TMEM_COLS, "accumulators fit TMEM");
 
@@ -406,24 +411,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
     const unsigned ntiles = (n + TC_N - 1) / TC_N;
     const size_t ld = a.ld;
     bool a_ok = true;
-    int issued = 0;  // thread 0: MMA batches committed
+    int issued = 0;  // the MMA thread: MMA batches committed
 
     if (warp < BUILD_WARPS) {
-        // the coefficient digits of this group: one bulk copy per slice
-        if (tid == 0) {
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar_a)),
-                         "r"((uint32_t)A_BYTES)
-                         : "memory");
-            const unsigned char *src = a.aimg + (size_t)g * A_BYTES;
-            for (int s = 0; s < NDIG; ++s)
-                asm volatile(
-                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                        smem_u32(sA + s * A_SLICE)),
-                    "l"(src + (size_t)s * A_SLICE), "r"((uint32_t)A_SLICE), "r"(smem_u32(bar_a))
-                    : "memory");
-            a_ok = mbar_wait(bar_a, 0, s_fail);
-            if (!a_ok) atomicExch(s_fail, 1);
-        }
+        // ---- builders: the basis digits of every tile.  They never issue
+        // MMAs, so their work for the next tile (loads, exponents) runs while
+        // the tensor core works through the current one.
         // item (octet o, element i): slots 8o..8o+7 of element i0 + i
         int io[ITEMS_PER], ii[ITEMS_PER];
 #pragma unroll
@@ -443,13 +436,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                     v[u][w] = (l < a.L && i0 + ii[u] < n) ? __ldcs(a.V + (size_t)l * ld + i0 + ii[u]) : 0.0;
                 }
         };
-        const uint64_t ad0 = umma_desc(smem_u32(sA)), bd0 = umma_desc(smem_u32(sB));
         int it = 0;
         if (blockIdx.x < ntiles) load_tile(blockIdx.x);
         for (unsigned t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
             if (*(volatile int *)s_fail) break;
-            // phase A (overlaps the previous tile's MMAs): element exponents and
-            // fixed-point values; s_cexp alternates between two buffers
+            // phase A (overlaps the previous tile's MMAs): element exponents;
+            // s_cexp alternates between two buffers
             int *cexp = s_cexp + (it & 1) * ITEMS;
             int em[ITEMS_PER];
 #pragma unroll
@@ -471,18 +463,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                 break;
             }
             int Fv[ITEMS_PER];
-            uint64_t U[ITEMS_PER][8];
 #pragma unroll
             for (int u = 0; u < ITEMS_PER; ++u) {
                 int F = em[u];
 #pragma unroll
                 for (int o = 0; o < TC_K / 8; ++o) F = max(F, cexp[o * TC_N + ii[u]]);
                 Fv[u] = F;
-#pragma unroll
-                for (int w = 0; w < 8; ++w) {
-                    const uint64_t bits = (uint64_t)__double_as_longlong(v[u][w]);
-                    U[u][w] = biased62(bits, F + s_slotexp[8 * io[u] + w]);
-                }
             }
             // phase B: the digit buffer is free once the previous tile's MMAs are done
             if (it > 0 && !mbar_wait(bar_mma, (it - 1) & 1, s_fail)) {
@@ -491,16 +477,39 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
             }
 #pragma unroll
             for (int u = 0; u < ITEMS_PER; ++u) {
+                uint64_t U[8];
+#pragma unroll
+                for (int w = 0; w < 8; ++w)
+                    U[w] = biased62((uint64_t)__double_as_longlong(v[u][w]), Fv[u] + s_slotexp[8 * io[u] + w]);
                 if (io[u] == 0) s_F[(it & 3) * TC_N + ii[u]] = Fv[u];
-                store_digits<0>(sB, umma_off(ii[u], 8 * io[u]), U[u]);
+                store_digits<0>(sB, umma_off(ii[u], 8 * io[u]), U);
             }
             // digits written by threads must be visible to the tensor core (async proxy)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(bar_full);
             // the next tile's basis values are in flight during this tile's MMAs
             if (t + gridDim.x < ntiles) load_tile(t + gridDim.x);
-            if (tid == 0) {
-                bool ok = a_ok && mbar_wait(bar_full, it & 1, s_fail);
+        }
+    } else if (warp == MMA_WARP) {
+        // ---- one thread loads the coefficient digits and issues every MMA
+        if (lane == 0) {
+            // the coefficient digits of this group: one bulk copy per slice
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar_a)),
+                         "r"((uint32_t)A_BYTES)
+                         : "memory");
+            const unsigned char *src = a.aimg + (size_t)g * A_BYTES;
+            for (int s = 0; s < NDIG; ++s)
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32(sA + s * A_SLICE)),
+                    "l"(src + (size_t)s * A_SLICE), "r"((uint32_t)A_SLICE), "r"(smem_u32(bar_a))
+                    : "memory");
+            a_ok = mbar_wait(bar_a, 0, s_fail);
+            if (!a_ok) atomicExch(s_fail, 1);
+            const uint64_t ad0 = umma_desc(smem_u32(sA)), bd0 = umma_desc(smem_u32(sB));
+            int it = 0;
+            for (unsigned t = blockIdx.x; t < ntiles && a_ok; t += gridDim.x, ++it) {
+                bool ok = mbar_wait(bar_full, it & 1, s_fail);
                 // the previous tile's accumulators must have been read out
                 if (ok && it > 0) ok = mbar_wait(bar_tfree, (it - 1) & 1, s_fail);
                 if (!ok) {
@@ -545,13 +554,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                 mbar_arrive(bar_ready);
             }
         }
+        __syncwarp();
     } else if ((warp & 3) < live_quads) {
         // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, columns
         // 16 c .. 16 c + 15 with c = (w - 4) / 4; lane u < 16 holds the x row
         // of live shift 16 (w % 4) + u of the group, lane u + 16 its p row.
         // (Warps of a quadrant without live rows skip this loop; the
         // accumulator-free barrier counts only the others.)
-        const int q = warp & 3, cg = (warp - BUILD_WARPS) >> 2;
+        const int q = warp & 3, cg = (warp - EPI_WARP0) >> 2;
         const int r = 32 * q + lane;
         const int which = row_which(r);
         const int pos = g * 64 + row_shift(r);
@@ -649,7 +659,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
     // every path ends here: let copies and MMAs still in flight after a
     // timeout finish (bounded), then free TMEM
     __syncthreads();
-    if (tid == 0 && *(volatile int *)s_fail) {
+    if (tid == 32 * MMA_WARP && *(volatile int *)s_fail) {
         int dummy = 0;
         if (!a_ok) mbar_wait(bar_a, 0, &dummy);
         if (issued > 0) mbar_wait(bar_mma, (issued - 1) & 1, &dummy);

@@ -42,9 +42,9 @@ extern "C" {
 #define HBK_FMT_HYB 2        /* short rows in SELL-32 slices (length-sorted inside windows), long rows one warp each */
 #define HBK_HYB_SHORT 32     /* longest row of a HYB slice */
 #define HBK_HYB_WINDOW 256   /* rows are sorted by length only inside windows of this many consecutive rows */
-#define HBK_FMT_MERGE 3      /* CSR; rows up to HBK_MERGE_LONG entries in merge-path blocks, longer rows one CTA each */
-#define HBK_MERGE_IPT 6      /* merge items (row ends + nonzeros) per thread of a block */
-#define HBK_MERGE_ITEMS (HBK_THREADS * HBK_MERGE_IPT) /* items per block */
+#define HBK_FMT_MERGE 3      /* CSR; rows up to HBK_MERGE_LONG entries in merge-path blocks, longer rows one warp each */
+#define HBK_MERGE_IPT 8      /* merge items (row ends + nonzeros) per lane of a block */
+#define HBK_MERGE_ITEMS (32 * HBK_MERGE_IPT) /* items per block (one warp) */
 #define HBK_MERGE_LONG (HBK_MERGE_ITEMS - 1) /* longest row a merge block takes (the row and its end fill it) */
 
 typedef struct {
@@ -67,7 +67,7 @@ typedef struct {
     unsigned nwrow;
     const unsigned *mblk;      /* MERGE: [2 nmblk] first and end row of each block of short rows */
     unsigned nmblk;
-    const unsigned *mlong;     /* MERGE: rows longer than HBK_MERGE_LONG, longest first, one CTA each */
+    const unsigned *mlong;     /* MERGE: rows longer than HBK_MERGE_LONG, longest first, one warp each */
     unsigned nmlong;
 } hbk_matrix;
 

@@ -225,32 +225,31 @@ __device__ __forceinline__ void spmv_rows_hyb(const hbk_matrix &A, const double 
     }
 }
 
-// MERGE path: nonzero-balanced work inside row blocks (merge-path
-// decomposition).  The host cuts the rows of at most HBK_MERGE_LONG entries
-// into blocks of consecutive rows with rows + nonzeros <= HBK_MERGE_ITEMS and
-// lists the longer rows apart (longest first).  Work units, in order: the long
-// rows, one CTA each (thread t sums entries t, t + NT, ... in stored order with
-// FMAs, then a fixed tree over the CTA), then the blocks.  A block is staged in
-// shared memory with coalesced loads (values, the gathered x values, the row
-// end offsets; every load of a thread issued before the first one is used);
-// thread t then walks items [t IPT, (t + 1) IPT) of the merge of the row ends
-// with the nonzeros, so every thread gets the same number of (row end +
-// nonzero) items whatever the row lengths.  A row that starts and ends inside
-// one thread is summed by that thread in stored order with FMAs from 0 (the
-// other paths' arithmetic); a row cut between threads is the sum of its
-// pieces (each an FMA chain in stored order) over a fixed segmented-scan tree.
-// Either way `epi(row, acc)` runs once per row.  Units are dealt to the CTAs
-// round-robin, the grid is one wave.
-struct MergeSmem {
+// MERGE path: nonzero-balanced work (merge-path decomposition), one warp per
+// work unit.  The host cuts the rows of at most HBK_MERGE_LONG entries into
+// blocks of consecutive rows with rows + nonzeros <= HBK_MERGE_ITEMS (32
+// lanes x HBK_MERGE_IPT items) and lists the longer rows apart (longest
+// first).  Units, in order: the long rows (one warp each: four FMA chains per
+// lane, entries in stored order within a chain, then a fixed tree), then the
+// blocks; unit u goes to warp u mod (warps of the grid), so no warp waits for
+// another and the assignment, hence every sum, is the same on every run.  A
+// block is staged in the warp's own shared memory with coalesced loads
+// (values, the gathered x values, the row end offsets; a lane's loads all
+// issue before the first is used); lane l then walks items [l IPT, (l + 1)
+// IPT) of the merge of the row ends with the nonzeros, so every lane gets the
+// same number of (row end + nonzero) items whatever the row lengths.  A row
+// that starts and ends inside one lane is summed by that lane in stored order
+// with FMAs from 0 (the other paths' arithmetic); a row cut between lanes is
+// the sum of its pieces (each an FMA chain in stored order) over a fixed
+// shuffle tree.  The row values are then written to shared memory and
+// `epi(row, acc)` runs once per row, in row order across the lanes.
+struct MergeWarpSmem {
     double val[HBK_MERGE_ITEMS];
-    double xv[HBK_MERGE_ITEMS];
+    double xv[HBK_MERGE_ITEMS];      // gathered x; after the walk, the rows' values
     unsigned rend[HBK_MERGE_ITEMS];  // end of each row of the block, relative to its first nonzero
-    double inc[NT];                  // per thread: running sum of its open row's pieces up to itself
-    unsigned key[NT];                // that row (relative), or a value >= 2^31 when none
-    double wv[NW];                   // per warp: the same at its last lane
-    unsigned wk[NW];
-    int wf[NW];                      // the warp's last run starts inside the warp
-    double red[2 * NW];
+};
+struct MergeSmem {
+    MergeWarpSmem w[NW];
 };
 
 constexpr unsigned kNoRow = 0x80000000u;
@@ -258,35 +257,34 @@ constexpr unsigned kNoRow = 0x80000000u;
 template <class Epi>
 __device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const double *__restrict__ x, Epi &epi,
                                                 MergeSmem &sm) {
+    constexpr int IPT = HBK_MERGE_IPT;
     const unsigned *__restrict__ ptr = A.ptr;
     const unsigned *__restrict__ col = A.col;
     const double *__restrict__ val = A.val;
-    const unsigned tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    MergeWarpSmem &ws = sm.w[warp];
+    const unsigned nwarps = gridDim.x * NW;
     const unsigned units = A.nmlong + A.nmblk;
-    for (unsigned u = blockIdx.x; u < units; u += gridDim.x) {
+    for (unsigned u = blockIdx.x * NW + warp; u < units; u += nwarps) {
         if (u < A.nmlong) {
-            // one long row, the whole CTA: four loads ahead, one FMA chain per thread
             const unsigned r = __ldg(A.mlong + u);
             const unsigned e0 = __ldg(ptr + r), e1 = __ldg(ptr + r + 1);
-            double acc = 0.0;
-            for (unsigned e = e0 + tid; e < e1; e += 4 * NT) {
-                double v[4], xx[4];
-                unsigned c[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const unsigned ek = e + k * NT;
-                    c[k] = ek < e1 ? __ldg(col + ek) : 0u;
-                    v[k] = ek < e1 ? __ldg(val + ek) : 0.0;
-                }
-#pragma unroll
-                for (int k = 0; k < 4; ++k) xx[k] = e + k * NT < e1 ? __ldg(x + c[k]) : 0.0;
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (e + k * NT < e1) acc = fma(v[k], xx[k], acc);
+            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+            for (unsigned e = e0 + lane; e < e1; e += 128) {
+                const bool h1 = e + 32 < e1, h2 = e + 64 < e1, h3 = e + 96 < e1;
+                const unsigned c0 = __ldg(col + e), c1 = h1 ? __ldg(col + e + 32) : 0u;
+                const unsigned c2 = h2 ? __ldg(col + e + 64) : 0u, c3 = h3 ? __ldg(col + e + 96) : 0u;
+                const double v0 = __ldg(val + e), v1 = h1 ? __ldg(val + e + 32) : 0.0;
+                const double v2 = h2 ? __ldg(val + e + 64) : 0.0, v3 = h3 ? __ldg(val + e + 96) : 0.0;
+                const double x0 = __ldg(x + c0), x1 = h1 ? __ldg(x + c1) : 0.0;
+                const double x2 = h2 ? __ldg(x + c2) : 0.0, x3 = h3 ? __ldg(x + c3) : 0.0;
+                a0 = fma(v0, x0, a0);
+                if (h1) a1 = fma(v1, x1, a1);
+                if (h2) a2 = fma(v2, x2, a2);
+                if (h3) a3 = fma(v3, x3, a3);
             }
-            acc = block_sum(acc, sm.red);
-            if (tid == 0) epi(r, acc);
-            __syncthreads();
+            const double acc = warp_sum((a0 + a1) + (a2 + a3));
+            if (lane == 0) epi(r, acc);
             continue;
         }
         const unsigned b = u - A.nmlong;
@@ -294,67 +292,77 @@ __device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const doubl
         const unsigned e0 = __ldg(ptr + r0);
         const unsigned nr = r1 - r0, nz = __ldg(ptr + r1) - e0;
         {
-            unsigned c[HBK_MERGE_IPT], re[HBK_MERGE_IPT];
-            double v[HBK_MERGE_IPT];
+            unsigned c[IPT], re[IPT];
+            double v[IPT];
 #pragma unroll
-            for (int k = 0; k < HBK_MERGE_IPT; ++k) {
-                const unsigned e = tid + k * NT;
+            for (int k = 0; k < IPT; ++k) {
+                const unsigned e = lane + 32u * k;
                 c[k] = e < nz ? __ldg(col + e0 + e) : 0u;
                 v[k] = e < nz ? __ldg(val + e0 + e) : 0.0;
                 re[k] = e < nr ? __ldg(ptr + r0 + e + 1) : 0u;
             }
 #pragma unroll
-            for (int k = 0; k < HBK_MERGE_IPT; ++k) {
-                const unsigned e = tid + k * NT;
+            for (int k = 0; k < IPT; ++k) {
+                const unsigned e = lane + 32u * k;
                 if (e < nz) {
-                    sm.xv[e] = __ldg(x + c[k]);
-                    sm.val[e] = v[k];
+                    ws.xv[e] = __ldg(x + c[k]);
+                    ws.val[e] = v[k];
                 }
-                if (e < nr) sm.rend[e] = re[k] - e0;
+                if (e < nr) ws.rend[e] = re[k] - e0;
             }
         }
-        __syncthreads();
+        __syncwarp();
         const unsigned tot = nr + nz;
-        const unsigned d0 = min(tid * (unsigned)HBK_MERGE_IPT, tot);
-        const unsigned d1 = min(d0 + (unsigned)HBK_MERGE_IPT, tot);
+        const unsigned d0 = min(lane * (unsigned)IPT, tot);
+        const unsigned d1 = min(d0 + (unsigned)IPT, tot);
         // merge-path search: i row ends and d0 - i nonzeros precede item d0
         unsigned lo = d0 > nz ? d0 - nz : 0, hi = min(d0, nr);
         while (lo < hi) {
             const unsigned mid = (lo + hi) >> 1;
-            if (sm.rend[mid] <= d0 - 1 - mid) lo = mid + 1;
+            if (ws.rend[mid] <= d0 - 1 - mid) lo = mid + 1;
             else hi = mid;
         }
         unsigned i = lo, e = d0 - lo;
-        // the thread starts inside row i when entries of that row precede e
-        bool head = e > (i ? sm.rend[i - 1] : 0u), open = false;
+        // the lane starts inside row i when entries of that row precede e
+        bool head = e > (i ? ws.rend[i - 1] : 0u), open = false;
         unsigned head_row = kNoRow;
         double head_v = 0.0, acc = 0.0;
-        for (unsigned d = d0; d < d1; ++d) {
-            if (i < nr && sm.rend[i] <= e) {
+        unsigned rr[IPT];
+        double rv[IPT];
+#pragma unroll
+        for (int q = 0; q < IPT; ++q) {
+            rr[q] = kNoRow;
+            rv[q] = 0.0;
+            const bool valid = d0 + q < d1;
+            const bool is_end = valid && i < nr && ws.rend[i] <= e;
+            if (is_end) {
                 if (head) {
                     head_row = i;
                     head_v = acc;
                     head = false;
                 } else {
-                    epi(r0 + i, acc);
+                    rr[q] = i;
+                    rv[q] = acc;
                 }
                 acc = 0.0;
                 open = false;
                 ++i;
-            } else {
-                acc = fma(sm.val[e], sm.xv[e], acc);
+            } else if (valid) {
+                acc = fma(ws.val[e], ws.xv[e], acc);
                 ++e;
                 open = true;
             }
         }
-        // segmented inclusive scan of the open pieces over the threads, keyed
-        // by row: inside the warp by shuffles, then across warps
-        const unsigned key = open ? i : (kNoRow | tid);
+        // pieces of rows cut between lanes: segmented inclusive scan of the
+        // open (tail) pieces keyed by row, with as many steps as the longest
+        // chain of lanes needs
+        const unsigned key = open ? i : (kNoRow | lane);
         double s = open ? acc : 0.0;
         const unsigned kprev = __shfl_up_sync(0xffffffffu, key, 1);
-        bool f = lane > 0 && kprev != key;  // a run starts here (lane 0: maybe not)
-#pragma unroll
+        bool f = lane == 0 || kprev != key;  // a run of the key starts here
+#pragma unroll 1
         for (int dd = 1; dd < 32; dd <<= 1) {
+            if (__all_sync(0xffffffffu, f)) break;
             const double so = __shfl_up_sync(0xffffffffu, s, dd);
             const bool fo = __shfl_up_sync(0xffffffffu, f, dd);
             if ((int)lane >= dd && !f) {
@@ -362,34 +370,18 @@ __device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const doubl
                 f = fo;
             }
         }
-        if (lane == 31) {
-            sm.wk[warp] = key;
-            sm.wv[warp] = s;
-            sm.wf[warp] = f;
-        }
-        __syncthreads();
-        if (!f && !(key & kNoRow)) {
-            // the run reaches lane 0: add what the earlier warps hold of it
-            double carry = 0.0;
-            for (int w = (int)warp - 1; w >= 0; --w) {
-                if (sm.wk[w] != key) break;
-                carry = sm.wv[w] + carry;
-                if (sm.wf[w]) break;
-            }
-            s = carry + s;
-        }
-        sm.key[tid] = key;
-        sm.inc[tid] = s;
-        __syncthreads();
-        if (head_row != kNoRow) {
-            // the pieces of this row left open by the threads before
-            const double before = (tid > 0 && sm.key[tid - 1] == head_row) ? sm.inc[tid - 1] : 0.0;
-            epi(r0 + head_row, before + head_v);
-        }
-        __syncthreads();
+        const unsigned pk = __shfl_up_sync(0xffffffffu, key, 1);
+        const double ps = __shfl_up_sync(0xffffffffu, s, 1);
+        __syncwarp();  // every lane is done with the staged values
+#pragma unroll
+        for (int q = 0; q < IPT; ++q)
+            if (rr[q] != kNoRow) ws.xv[rr[q]] = rv[q];
+        if (head_row != kNoRow) ws.xv[head_row] = ((lane > 0 && pk == head_row) ? ps : 0.0) + head_v;
+        __syncwarp();
+        for (unsigned q = lane; q < nr; q += 32) epi(r0 + q, ws.xv[q]);
+        __syncwarp();  // before the next unit overwrites this warp's staging
     }
 }
-
 
 // Format chosen at compile time so the SELL kernels carry no shared-memory
 // tile (full occupancy); launchers pick the instantiation from A.fmt.

@@ -24,6 +24,7 @@ struct hbicg_matrix {
     unsigned *d_ptr, *d_col;
     double *d_val;
     int owns;
+    int pooled; /* d_ptr, d_col, d_val came from the library's pool (hbicg__dev_alloc) */
     unsigned *d_blk_row;
     unsigned char *d_blk_kind;
     double *d_sval;
@@ -57,6 +58,9 @@ void hbicg__ctx_release(hbicg_context *c);
 
 /* positions of A's SELL-32 diagonal entries (computed once per layout) */
 int hbicg__sell_diag(hbicg_matrix *A);
+/* device arrays from the library's stream-ordered pool (solver.c) */
+cudaError_t hbicg__dev_alloc(void **p, size_t bytes, cudaStream_t st);
+void hbicg__dev_free(void *p, cudaStream_t st);
 const hbk_matrix *hbicg__matrix_kernel_view(const hbicg_matrix *A);
 hbicg_context *hbicg__matrix_context(const hbicg_matrix *A);
 /* y (+)= A x for host arrays, on a process-wide context (matrix.h's mult) */

@@ -285,7 +285,8 @@ int hbk_spmv_grid(unsigned nblk) {
 // so a second wave would wait for whole CTAs of the first)
 int hbk_merge_grid(unsigned units) {
     const int w = wave_grid<k_spmv<HBK_FMT_MERGE>>(HBK_MAX_GRID);
-    const int g = units < (unsigned)w ? (int)units : w;
+    const unsigned need = (units + NW - 1) / NW;  // a unit per warp
+    const int g = need < (unsigned)w ? (int)need : w;
     return g < 1 ? 1 : g;
 }
 

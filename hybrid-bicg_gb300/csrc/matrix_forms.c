@@ -147,9 +147,9 @@ static void use_hyb(hbicg_matrix *A) {
 /* MERGE: rows of at most HBK_MERGE_LONG entries in blocks of consecutive
  * rows with rows + nonzeros <= HBK_MERGE_ITEMS (a block ends where the next
  * row would not fit and before every long row); rows above HBK_MERGE_LONG in
- * a list, longest first (stable), one CTA each.  The device splits every
- * block among its threads along the merge path of row ends and nonzeros, so
- * each thread gets the same number of items whatever the row lengths: for
+ * a list, longest first (stable), one warp each.  A block is one warp's unit:
+ * the device splits it among the lanes along the merge path of row ends and
+ * nonzeros, so each lane gets the same number of items whatever the row lengths: for
  * power-law rows this needs no sorting, padding or copy of the values. */
 static int build_merge(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
     if (!n || A->d_merge) return HBICG_OK;
@@ -265,9 +265,9 @@ static int build_sell(hbicg_matrix *A, const unsigned *h_ptr, unsigned n, unsign
     for (unsigned i = 0; i < ns; i++) h_sp[i + 1] = h_sp[i] + 32ull * h_w[i];
     const unsigned long long padded = h_sp[ns];
     if (!env && (double)padded > 1.34 * (double)nnz + 4096.0) goto out; /* too much padding: not SELL-32 */
-    CUDA_GOTO(cudaMalloc((void **)&A->d_sptr, sizeof(unsigned long long) * ((size_t)ns + 1)));
-    CUDA_GOTO(cudaMalloc((void **)&A->d_sval, sizeof(double) * (padded + 1)));
-    CUDA_GOTO(cudaMalloc((void **)&A->d_scol, sizeof(unsigned) * (padded + 1)));
+    CUDA_GOTO(hbicg__dev_alloc((void **)&A->d_sptr, sizeof(unsigned long long) * ((size_t)ns + 1), st));
+    CUDA_GOTO(hbicg__dev_alloc((void **)&A->d_sval, sizeof(double) * (padded + 1), st));
+    CUDA_GOTO(hbicg__dev_alloc((void **)&A->d_scol, sizeof(unsigned) * (padded + 1), st));
     CUDA_GOTO(cudaMemcpyAsync(A->d_sptr, h_sp, sizeof(unsigned long long) * ((size_t)ns + 1), cudaMemcpyHostToDevice,
                               st));
     HBK_GOTO(hbk_sell_fill(n, A->d_ptr, A->d_col, A->d_val, A->d_sptr, A->d_sval, A->d_scol, st));
@@ -292,7 +292,7 @@ int hbicg__sell_diag(hbicg_matrix *A) {
     const unsigned n = A->k.n;
     int *d_missing = NULL, missing = 0;
     int rc = HBICG_OK;
-    if (!A->d_sdiag) CUDA_GOTO(cudaMalloc((void **)&A->d_sdiag, sizeof(unsigned long long) * ((size_t)n + 1)));
+    if (!A->d_sdiag) CUDA_GOTO(hbicg__dev_alloc((void **)&A->d_sdiag, sizeof(unsigned long long) * ((size_t)n + 1), st));
     CUDA_GOTO(cudaMalloc((void **)&d_missing, sizeof(int)));
     CUDA_GOTO(cudaMemsetAsync(d_missing, 0, sizeof(int), st));
     HBK_GOTO(hbk_sell_diag(n, A->d_ptr, A->d_sptr, A->d_scol, A->d_sdiag, d_missing, st));
@@ -360,9 +360,10 @@ int hbicg_matrix_create(hbicg_context *ctx, unsigned n, unsigned nnz, const unsi
         CUDA_GOTO(cudaStreamSynchronize(st));
     } else {
         A->owns = 1;
-        CUDA_GOTO(cudaMalloc((void **)&A->d_ptr, sizeof(unsigned) * ((size_t)n + 1)));
-        CUDA_GOTO(cudaMalloc((void **)&A->d_col, sizeof(unsigned) * ((size_t)nnz + 1)));
-        CUDA_GOTO(cudaMalloc((void **)&A->d_val, sizeof(double) * ((size_t)nnz + 1)));
+        A->pooled = 1;
+        CUDA_GOTO(hbicg__dev_alloc((void **)&A->d_ptr, sizeof(unsigned) * ((size_t)n + 1), st));
+        CUDA_GOTO(hbicg__dev_alloc((void **)&A->d_col, sizeof(unsigned) * ((size_t)nnz + 1), st));
+        CUDA_GOTO(hbicg__dev_alloc((void **)&A->d_val, sizeof(double) * ((size_t)nnz + 1), st));
         CUDA_GOTO(cudaMemcpyAsync(A->d_ptr, ptr, sizeof(unsigned) * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
         if (nnz) {
             CUDA_GOTO(cudaMemcpyAsync(A->d_col, col, sizeof(unsigned) * (size_t)nnz, cudaMemcpyHostToDevice, st));
@@ -517,48 +518,45 @@ int hbicg_matrix_load_mm(hbicg_context *ctx, const char *path, int expand_symmet
 }
 
 /* frees a matrix whose creation failed before it took its context reference */
-static void hbicg_matrix_destroy_unretained(hbicg_matrix *A) {
-    cudaStreamSynchronize(A->ctx->stream);
+/* the matrix's device arrays: the CSR copy (when it owns one), the SELL-32
+ * form and the diagonal positions from the pool, the rest plain */
+static void free_device_arrays(hbicg_matrix *A) {
+    cudaStream_t st = A->ctx->stream;
+    cudaStreamSynchronize(st);
     if (A->owns) {
-        cudaFree(A->d_ptr);
-        cudaFree(A->d_col);
-        cudaFree(A->d_val);
+        if (A->pooled) {
+            hbicg__dev_free(A->d_ptr, st);
+            hbicg__dev_free(A->d_col, st);
+            hbicg__dev_free(A->d_val, st);
+        } else {
+            cudaFree(A->d_ptr);
+            cudaFree(A->d_col);
+            cudaFree(A->d_val);
+        }
     }
     cudaFree(A->d_blk_row);
     cudaFree(A->d_blk_kind);
-    cudaFree(A->d_sval);
-    cudaFree(A->d_scol);
-    cudaFree(A->d_sptr);
+    hbicg__dev_free(A->d_sval, st);
+    hbicg__dev_free(A->d_scol, st);
+    hbicg__dev_free(A->d_sptr, st);
     cudaFree(A->d_hval);
     cudaFree(A->d_hcol);
     cudaFree(A->d_hsptr);
     cudaFree(A->d_srow);
     cudaFree(A->d_wrow);
-    cudaFree(A->d_sdiag);
+    hbicg__dev_free(A->d_sdiag, st);
     cudaFree(A->d_merge);
+    cudaStreamSynchronize(st);
+}
+
+static void hbicg_matrix_destroy_unretained(hbicg_matrix *A) {
+    free_device_arrays(A);
     free(A);
 }
 
 void hbicg_matrix_destroy(hbicg_matrix *A) {
     if (!A) return;
-    cudaStreamSynchronize(A->ctx->stream);
-    if (A->owns) {
-        cudaFree(A->d_ptr);
-        cudaFree(A->d_col);
-        cudaFree(A->d_val);
-    }
-    cudaFree(A->d_blk_row);
-    cudaFree(A->d_blk_kind);
-    if (A->d_sval) cudaFree(A->d_sval);
-    if (A->d_scol) cudaFree(A->d_scol);
-    if (A->d_sptr) cudaFree(A->d_sptr);
-    cudaFree(A->d_hval);
-    cudaFree(A->d_hcol);
-    cudaFree(A->d_hsptr);
-    cudaFree(A->d_srow);
-    cudaFree(A->d_wrow);
-    cudaFree(A->d_sdiag);
-    cudaFree(A->d_merge);
+    free_device_arrays(A);
     hbicg_context *ctx = A->ctx;
     free(A);
     hbicg__ctx_release(ctx);
@@ -830,12 +828,16 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
             A->k.scol = NULL;
             A->k.sptr = NULL;
         }
-        cudaFree(A->d_sval);
-        cudaFree(A->d_scol);
-        cudaFree(A->d_sptr);
+        hbicg__dev_free(A->d_sval, A->ctx->stream);
+        hbicg__dev_free(A->d_scol, A->ctx->stream);
+        hbicg__dev_free(A->d_sptr, A->ctx->stream);
+        hbicg__dev_free(A->d_sdiag, A->ctx->stream); /* positions in the SELL-32 arrays */
+        cudaStreamSynchronize(A->ctx->stream);
         A->d_sval = NULL;
         A->d_scol = NULL;
         A->d_sptr = NULL;
+        A->d_sdiag = NULL;
+        A->diag_state = 0;
     }
     if (pick != 3 && A->d_merge) { /* the MERGE plan is not used */
         cudaStreamSynchronize(A->ctx->stream);

@@ -262,6 +262,16 @@ static cudaError_t pool_alloc(void **p, size_t bytes, cudaStream_t st) {
     return e;
 }
 
+/* the same pool for the matrices' device arrays (the CSR copy and the SELL-32
+ * form): a one-shot call such as the reference's entry points then reuses the
+ * memory of the previous call instead of mapping ~3 GB again at 256^3 */
+cudaError_t hbicg__dev_alloc(void **p, size_t bytes, cudaStream_t st) { return pool_alloc(p, bytes, st); }
+
+/* back to the pool in stream order (p from hbicg__dev_alloc, or NULL) */
+void hbicg__dev_free(void *p, cudaStream_t st) {
+    if (p) cudaFreeAsync(p, st);
+}
+
 void hbicg_release(void) {
     pthread_mutex_lock(&g_pool_lock);
     for (int d = 0; d < HBICG_MAX_DEVICES; ++d)

@@ -136,15 +136,32 @@ def irregular_powerlaw(n: int, mean_len: float = 16.0, max_len: int = 4000, zipf
     +-band of the row; duplicates and the diagonal are removed.  Off-diagonal
     values are N(0,1); the diagonal is 1.1 x the row's absolute off-diagonal
     sum (1.0 for a row with no off-diagonal entry), so A is strictly
-    diagonally dominant."""
+    diagonally dominant.  Removing duplicate columns shortens rows (most of all
+    the long ones, whose near-diagonal draws collide in the +-band window), so
+    the drawn lengths aim at a mean that is raised until the mean after
+    de-duplication is mean_len (within 0.5 %, at most six passes)."""
+    aim = mean_len
+    for _ in range(6):
+        a = _powerlaw_draw(n, aim, mean_len, max_len, zipf_a, band, band_frac, seed)
+        got = a.nnz / n
+        if abs(got - mean_len) <= 0.005 * mean_len:
+            break
+        aim *= mean_len / got
+    return a
+
+
+def _powerlaw_draw(n: int, aim: float, mean_len: float, max_len: int, zipf_a: float, band: int, band_frac: float,
+                   seed: int) -> Csr:
+    """One draw of irregular_powerlaw with the row lengths (before duplicate
+    columns are removed) scaled to mean `aim`."""
     rng = np.random.default_rng(seed)
     z = rng.zipf(zipf_a, size=n).astype(np.float64)
     z = np.minimum(z, float(max_len))
-    lo, hi = 0.01, 100.0
+    lo, hi = 0.01, 1000.0
     for _ in range(60):
         c = 0.5 * (lo + hi)
         mean = np.clip(np.rint(c * z), 1, max_len).mean()
-        if mean < mean_len:
+        if mean < aim:
             lo = c
         else:
             hi = c
@@ -157,7 +174,8 @@ def irregular_powerlaw(n: int, mean_len: float = 16.0, max_len: int = 4000, zipf
     cols_band = rows + rng.integers(-band, band + 1, size=tot, dtype=np.int64)
     cols = np.where(in_band, np.clip(cols_band, 0, n - 1), cols)
     keep = cols != rows
-    key = np.unique(rows[keep] * n + cols[keep])
+    key = np.sort(rows[keep] * n + cols[keep])
+    key = key[np.concatenate(([True], key[1:] != key[:-1]))] if key.size else key
     rows_o, cols_o = key // n, key % n
     vals_o = rng.standard_normal(rows_o.shape[0])
     absrow = np.bincount(rows_o, weights=np.abs(vals_o), minlength=n)

@@ -159,18 +159,18 @@ def test_dropin_mult_accumulates(cuda, pkg, oracle):
 
 
 # ---- MERGE form: nonzero-balanced blocks (merge-path split among threads)
-MERGE_IPT, MERGE_ITEMS = 6, 256 * 6
+MERGE_IPT, MERGE_ITEMS = 8, 32 * 8
 MERGE_LONG = MERGE_ITEMS - 1
 
 
 def merge_whole_rows(ptr):
-    """Rows the MERGE form sums in one thread (same bits as the stored-order
-    FMA sum): the host plan (blocks of consecutive rows of <= 1535 entries
-    with rows + nonzeros <= 1536, cut before every longer row) restated, then
-    inside a block row i's nonzeros are merge items i + ptr-offsets and its end
-    item i + end offset; the row is whole when its first nonzero and its end
-    item fall in the same thread's run of 6 items.  Empty rows are exact zeros
-    whoever ends them."""
+    """Rows the MERGE form sums in one lane (same bits as the stored-order
+    FMA sum): the host plan (blocks of consecutive rows of <= 255 entries with
+    rows + nonzeros <= 256, one warp each, cut before every longer row)
+    restated, then inside a block row i's nonzeros are merge items i +
+    ptr-offsets and its end item i + end offset; the row is whole when its
+    first nonzero and its end item fall in the same lane's run of 8 items.
+    Empty rows are exact zeros whoever ends them."""
     lens = np.diff(ptr.astype(np.int64))
     n = lens.shape[0]
     whole = np.zeros(n, dtype=bool)
@@ -221,17 +221,18 @@ def test_merge_powerlaw(cuda, pkg, oracle):
 
 @pytest.mark.parametrize("case", ["boundaries", "all_long", "all_empty", "one_row", "full_blocks", "mixed_empty"])
 def test_merge_shapes(cuda, pkg, oracle, case):
-    """MERGE edge cases: rows of exactly 1535 and 1536 entries (the long-row
-    limit: a row and its end fill a block), rows cut across many threads and
-    warps, blocks filled to the last item, only long rows, only empty rows, a
-    single row, runs of empty rows between long ones."""
+    """MERGE edge cases: rows of exactly 255 and 256 entries (the long-row
+    limit: a row and its end fill a warp's block), rows cut across many lanes,
+    blocks filled to the last item, only long rows (one warp each, lengths
+    around the four-chain stride), only empty rows, a single row, runs of empty
+    rows between long ones."""
     rng = np.random.default_rng(len(case) + 11)
     if case == "boundaries":
         n = 3000
-        lens = rng.choice([0, 1, 5, 6, 7, 191, 192, 193, 700, 1534, 1535, 1536, 1537, 4000], size=n)
+        lens = rng.choice([0, 1, 5, 7, 8, 9, 31, 32, 33, 100, 254, 255, 256, 257, 4000], size=n)
     elif case == "all_long":
         n = 200
-        lens = rng.integers(1536, 6000, n)
+        lens = rng.choice([256, 300, 383, 384, 385, 511, 512, 513, 2000, 6000], size=n)
     elif case == "all_empty":
         n = 4000
         lens = np.zeros(n, dtype=np.int64)
@@ -240,12 +241,12 @@ def test_merge_shapes(cuda, pkg, oracle, case):
         lens = np.array([1])
     elif case == "full_blocks":
         n = 64
-        lens = np.full(n, 191)  # 8 rows x 192 items = one full block
+        lens = np.full(n, 31)  # 8 rows x 32 items = one full block
     else:
         n = 5000
         lens = np.where(rng.random(n) < 0.02, 2000, 0)
         lens[rng.random(n) < 0.3] = 3
-        lens[rng.random(n) < 0.05] = 400
+        lens[rng.random(n) < 0.05] = 150
     a = _random_csr(pkg, n, lens, seed=5)
     x = rng.standard_normal(n)
     y = _gpu_spmv(pkg, a, x, fmt="merge", want_fmt="merge")
