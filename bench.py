@@ -655,6 +655,18 @@ def run_adjoint_c5(args, dist: Dist):
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": int(12 * nnz + 4 * (n + 1) + 16 * n + 16 * m),
                     "d2h_bytes_per_step": int(8 * (nnz + n + m + m * n))},
             "clocks": clk.summary(), "cpu_baseline": None}
+    # the forward family alone through the same kind of call (host arrays in,
+    # every x_j out), for the cost of the gradients relative to the solve
+    for _ in range(max(1, args.warmup)):
+        pkg.solve(f.a, f.b, f.sigma, **kw)
+    ftimes = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        fwd = pkg.solve(f.a, f.b, f.sigma, **kw)
+        ftimes.append(time.perf_counter() - t0)
+    line["forward"] = {"value": float(np.median(ftimes)), "unit": "s", "iterations": int(fwd.k),
+                       "api": "hbicg_solve (host arrays in, x out)"}
+    line["adjoint_over_forward"] = value / line["forward"]["value"]
     if not args.no_cpu_baseline:
         fwd = pkg.solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=f.max_iter)
         prof = {"k": int(fwd.k), "shift_updates": int(np.sum(fwd.active)), "source": "the GPU forward solve's profile"}

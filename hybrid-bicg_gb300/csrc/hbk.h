@@ -98,6 +98,7 @@ typedef struct {
     int slot_cap;
     int need_ps;        /* deferred mode: the new seed's p must be formed from the basis */
     double rs_switch;   /* (r^, r_k) after the switch rescale */
+    int loops;          /* bodies of the device-side iteration loop run in this solve (bound on the loop) */
 } hbk_scalars;
 
 typedef struct {
@@ -200,6 +201,10 @@ int hbk_sell_fill(unsigned n, const unsigned *ptr, const unsigned *col, const do
 int hbk_fused_init(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, const double *b, int seed,
                    double tol, cudaStream_t st);
 int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, cudaStream_t st);
+/* end of one body of a CUDA graph's conditional while loop over iterations:
+ * sets the loop's condition to "not finished", and to 0 once the solve has run
+ * loop_cap bodies (a bound on the loop whatever the scalars say) */
+int hbk_loop_condition(const hbk_shifts *sh, cudaGraphConditionalHandle cond, int loop_cap, cudaStream_t st);
 /* deferred mode: x_j (and p_j when keep_p) = coefficients x basis, then reset the basis */
 int hbk_deferred_flush(const hbk_vectors *v, const hbk_shifts *sh, int keep_p, cudaStream_t st);
 /* ||b - (A + sigma_j I) x_j||^2 for every shift into out[m] (device) */

@@ -85,6 +85,7 @@ __global__ void __launch_bounds__(NT) k_init(Ctx c, int seed, double tol) {
         sc->n_active = 0;
         sc->status = 0;
         sc->n_sw = 0;
+        sc->loops = 0;
         sc->max_sigma = seed;
         sc->m = m;
         sc->kcap = kcap;
@@ -811,6 +812,14 @@ __global__ void __launch_bounds__(NT) k_absmax(const double *__restrict__ x, uns
     block_max_to(mx, smx, out);
 }
 
+// End of a while-loop body in a CUDA graph: run again while the solve goes on
+// (not finished: converged, at max_iter, broken down or waiting for a basis
+// flush), and never more than loop_cap bodies per solve.
+__global__ void k_loop_condition(hbk_scalars *sc, cudaGraphConditionalHandle cond, int loop_cap) {
+    const int loops = ++sc->loops;
+    cudaGraphSetConditional(cond, (!sc->finished && loops < loop_cap) ? 1u : 0u);
+}
+
 // x[i] = element i of system j of the panel-major Xp (runs of HBK_PANEL)
 __global__ void __launch_bounds__(NT) k_panel_row(const double *__restrict__ Xp, int m, unsigned n, int j,
                                                   double *__restrict__ x) {
@@ -932,6 +941,11 @@ int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shi
         k_coef_update<<<grid_for((unsigned)((size_t)sh->m * v->slot_cap), 1), NT, 0, st>>>(c);
         k_materialize_ps<<<wave_grid<k_materialize_ps>(gv), NT, 0, st>>>(c);
     }
+    return (int)cudaGetLastError();
+}
+
+int hbk_loop_condition(const hbk_shifts *sh, cudaGraphConditionalHandle cond, int loop_cap, cudaStream_t st) {
+    k_loop_condition<<<1, 1, 0, st>>>(sh->sc, cond, loop_cap);
     return (int)cudaGetLastError();
 }
 

@@ -157,6 +157,8 @@ struct hbicg_solver {
     double *d_rold, *d_qcopy, *d_r, *d_dot;
     /* fused form graphs */
     cudaGraphExec_t graph;
+    int graph_loop;    /* graph is one conditional while loop over iterations */
+    int no_loop_graph; /* the runtime refused the loop graph: chunks of iterations */
     int chunk;
     void *tc_ws;      /* tensor-core flush workspace (deferred mode) */
     int *d_tc_err;    /* set by the tensor-core flush on a bounded-wait timeout */
@@ -643,9 +645,55 @@ out:
 /* ------------------------------------------------------------------------ */
 /* fused form */
 
+/* The iterations as one conditional while node: its body is one iteration
+ * followed by a one-thread kernel that sets the loop's condition to "not
+ * finished", so a graph launch runs iterations until the solve converges,
+ * reaches max_iter, breaks down or needs a basis flush, with no host round
+ * trip in between.  The loop is also bounded by a count of bodies per solve
+ * (2 kcap + 64: every relaunch after a flush adds at most one body that finds
+ * the solve stopped).  Returns nonzero, with nothing left behind, when the
+ * runtime refuses any step; the caller then captures chunks of iterations. */
+static int capture_loop_graph(hbicg_solver *s) {
+    cudaStream_t st = s->ctx->stream;
+    cudaGraph_t g = NULL, body_out = NULL;
+    cudaGraphExec_t ex = NULL;
+    cudaGraphConditionalHandle cond;
+    cudaGraphNode_t node;
+    struct cudaGraphNodeParams np;
+    int capturing = 0, ok = 0;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) goto out;
+    if (cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) goto out;
+    memset(&np, 0, sizeof np);
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    if (cudaGraphAddNode(&node, g, NULL, NULL, 0, &np) != cudaSuccess) goto out;
+    if (cudaStreamBeginCaptureToGraph(st, np.conditional.phGraph_out[0], NULL, NULL, 0,
+                                      cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        goto out;
+    capturing = 1;
+    if (hbk_fused_iteration(&s->A->k, &s->v, &s->sh, st)) goto out;
+    if (hbk_loop_condition(&s->sh, cond, 2 * s->kcap + 64, st)) goto out;
+    capturing = 0;
+    if (cudaStreamEndCapture(st, &body_out) != cudaSuccess) goto out;
+    if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) goto out;
+    s->graph = ex;
+    s->graph_loop = 1;
+    ok = 1;
+out:
+    if (capturing) cudaStreamEndCapture(st, &body_out);
+    if (g) cudaGraphDestroy(g);
+    if (!ok) cudaGetLastError(); /* a refused step leaves no error behind for later calls */
+    return ok ? 0 : 1;
+}
+
 static int capture_graph(hbicg_solver *s) {
     cudaStream_t st = s->ctx->stream;
     cudaGraph_t g;
+    if (!s->no_loop_graph && getenv("HBICG_NO_LOOP_GRAPH") == NULL && capture_loop_graph(s) == 0) return HBICG_OK;
+    s->no_loop_graph = 1; /* refused once: chunks from now on */
+    s->graph_loop = 0;
     CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int i = 0; i < s->chunk; i++) {
         int e = hbk_fused_iteration(&s->A->k, &s->v, &s->sh, st);
@@ -719,23 +767,31 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, dou
     long guard = 0;
     const long guard_max = 4L * s->kcap / s->chunk + 64;
     int k_flushed = 0; /* last iteration covered by a flush */
+    int loops_seen = 0; /* loop-graph bodies counted so far (k_init zeroes the device count) */
     for (;;) {
         if (++guard > guard_max) {
             set_msg("fused loop made no progress after %ld chunks", guard_max);
             return HBICG_E_TIMEOUT;
         }
+        int looped = 0;
         if (use_graph) {
             if (!s->graph) {
                 int rc = capture_graph(s);
                 if (rc) return rc;
             }
             CUDA_TRY(cudaGraphLaunch(s->graph, st));
+            looped = s->graph_loop;
         } else {
             for (int i = 0; i < s->chunk; i++) HBK_TRY(hbk_fused_iteration(&s->A->k, &s->v, &s->sh, st));
         }
-        *launches += s->chunk * s->launches_per_iter;
         CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
+        if (looped) { /* every body: one iteration's kernels and the condition kernel */
+            *launches += (h->loops - loops_seen) * (s->launches_per_iter + 1);
+            loops_seen = h->loops;
+        } else {
+            *launches += s->chunk * s->launches_per_iter;
+        }
         if (!h->finished) continue;
         if ((h->status & HBK_ST_BASIS_FULL) && !(h->status & HBK_ST_BREAKDOWN)) {
             int rc = ensure_pmat(s);
