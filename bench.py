@@ -457,6 +457,27 @@ def run_ours(args, dist: Dist):
                                                                           + h_b.nbytes + h_sig.nbytes),
                "d2h_bytes_per_step": int(h_x.nbytes + h_r.nbytes), "api": "shifted_lopbicg_dynamic", "k": int(k),
                "calls_s": [round(t, 4) for t in e2e_times]}
+        # where the end-to-end time goes: the same sequence as the drop-in call
+        # (context, matrix from host arrays, solver, solve with every x_j
+        # copied out, teardown) through the extended API, phase by phase, once
+        ph = {}
+        h_x.zero_()
+        t0 = time.perf_counter()
+        pctx = pkg.Context()
+        pA = pkg.Matrix(pctx, h_ptr.numpy(), h_col.numpy(), h_val.numpy())
+        t1 = time.perf_counter()
+        ps_ = pkg.Solver(pA, m, tol=f.tol, max_iter=f.max_iter, refine=False)
+        t2 = time.perf_counter()
+        pres = ps_.run(h_b.numpy(), h_sig.numpy(), seed=f.seed, x=h_x.numpy(), r=h_r.numpy())
+        t3 = time.perf_counter()
+        ps_.close()
+        pA.close()
+        pctx.close()
+        t4 = time.perf_counter()
+        ph = {"context_and_matrix_upload_s": t1 - t0, "solver_setup_s": t2 - t1,
+              "solve_and_copy_out_s": t3 - t2, "device_solve_s": pres.solve_ms / 1e3, "teardown_s": t4 - t3,
+              "total_s": t4 - t0}
+        e2e["breakdown"] = ph
         if plain is not None:
             # the same call through shifted_lopbicg_static (the plain form), once
             h_x.zero_()

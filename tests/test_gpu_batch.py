@@ -113,3 +113,27 @@ def test_manifest_runner_end_to_end(cuda, pkg, tmp_path):
     x = np.load(tmp_path / "x" / "file_seed7.npy")
     assert abs(lines[1]["k"] - one.k) <= 1 and np.max(np.abs(x - one.x)) <= 1e-9 * np.max(np.abs(one.x))
     assert (tmp_path / "tune.txt").exists()
+
+
+def test_config4_families_against_the_oracle(cuda, pkg, oracle):
+    """Families of the 256-family batch itself (the eight smallest, 2-D and
+    3-D stencils with 8..64 shifts), solved together by the batch and each
+    checked against the oracle (the reference's algorithm) on the same inputs:
+    every x_j within 1e-8 relative, k within 2 % or the oracle's rounding
+    envelope, every shift's true residual at tol or within 1.5x the
+    reference's own (no true-residual correction: the reference's x)."""
+    fams = pkg.workloads.batched_families(256)
+    small = sorted(range(256), key=lambda i: fams[i].a.n)[:8]
+    sel = [fams[i] for i in small]
+    res, _ = pkg.batch_solve(sel, workers=4, tol=1e-10, max_iter=10000, true_residuals=True, refine=False)
+    for f, r in zip(sel, res):
+        assert r.status == 0, (f.name, r.status)
+        want = oracle.solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=f.max_iter)
+        err = np.max(np.abs(r.x - want.x)) / np.max(np.abs(want.x))
+        assert err < 1e-8, (f.name, err)
+        ks = [want.k] + [oracle.solve(f.a, f.b * (1 + 1e-14 * np.random.default_rng(t).standard_normal(f.a.n)),
+                                      f.sigma, seed=f.seed, tol=f.tol, max_iter=f.max_iter).k for t in (1, 2, 3)]
+        assert min(ks) - max(1, int(0.02 * min(ks))) <= r.k <= max(ks) + max(1, int(0.02 * max(ks))), (f.name, r.k, ks)
+        tr = oracle.true_residuals(f.a, r.x, f.b, f.sigma)
+        tr_ref = oracle.true_residuals(f.a, want.x, f.b, f.sigma)
+        assert np.all(tr <= np.maximum(f.tol * 1.02, 1.5 * tr_ref)), (f.name, tr.max(), tr_ref.max())

@@ -72,7 +72,10 @@ def test_headline_shape_vs_reference_digest(cuda, pkg, side):
     name = "c2_digest" if side == 256 else f"c2_{side}_digest"
     d = np.load(GOLDEN / f"{name}.npz", allow_pickle=False)
     f = pkg.workloads.family("c2", None if side == 256 else side)
-    assert np.array_equal(d["sigma"], f.sigma)
+    # the shifts come from a power function whose last bit may differ between
+    # hosts' math libraries: solve with exactly the reference's shifts
+    assert np.allclose(d["sigma"], f.sigma, rtol=1e-14, atol=0)
+    f.sigma = np.array(d["sigma"], dtype=np.float64)
     res, x, tres, h = _solve_device(pkg, torch, f)
     _close(h)
     assert res.shift_mode == "deferred" and res.flushes >= 3
