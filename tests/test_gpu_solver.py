@@ -203,16 +203,15 @@ def test_solver_reuse_device_pointers(cuda, pkg, oracle):
 
 @pytest.mark.parametrize("shift_mode", ["incremental", "deferred"])
 @pytest.mark.parametrize("name", ["stencil2d_two_switches", "stencil8_maxiter5", "stencil2d_seed8"])
-def test_loop_graph_equals_chunked_graph(cuda, pkg, monkeypatch, name, shift_mode):
-    """The iterations as one conditional while node in a CUDA graph (the
-    default) and as replayed chunks of iterations (HBICG_NO_LOOP_GRAPH) run the
-    same kernels in the same order: identical k, switches, convergence
+def test_loop_graph_equals_chunked_graph(cuda, pkg, name, shift_mode):
+    """The iterations as one conditional while node in a CUDA graph
+    (use_graph="loop") and as replayed chunks of iterations (the default) run
+    the same kernels in the same order: identical k, switches, convergence
     iterations and bits of x; and both end at the reference's answer."""
     g = golden(name)
     kw = dict(seed=int(g["seed"]), tol=float(g["tol"]), max_iter=int(g["max_iter"]), switching=bool(g["switching"]),
               shift_mode=shift_mode, refine=False)
-    loop = pkg.solve(GoldenCsr(g), g["b"], g["sigma"], **kw)
-    monkeypatch.setenv("HBICG_NO_LOOP_GRAPH", "1")
+    loop = pkg.solve(GoldenCsr(g), g["b"], g["sigma"], use_graph="loop", **kw)
     chunk = pkg.solve(GoldenCsr(g), g["b"], g["sigma"], **kw)
     assert loop.k == chunk.k and loop.switches == chunk.switches
     assert np.array_equal(loop.conv_k, chunk.conv_k)
