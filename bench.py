@@ -582,13 +582,18 @@ def run_batch_c4(args, dist: Dist):
     in [1e4, 5e5], 8..64 shifts each) through hbicg_batch_solve: a step is the
     whole batch, from host arrays (matrices, b, sigma in; every x_j out), so
     the copies are inside the timed region and `value` is also the end-to-end
-    figure.  CPU baseline: the reference's algorithm (oracle/) solved to
-    convergence on a bounded sample of the cheapest families, costed per
-    (nnz + 6 m n) x iterations and scaled to all 256 with the GPU's counts."""
+    figure.  The families that take the incremental shift mode share one
+    persistent launch unless --no-persistent; the line also reports the same
+    batch without it and the sequential per-family loop (one worker, one
+    family on the GPU at a time).  CPU baseline: the reference's algorithm
+    (oracle/) solved to convergence on a bounded sample of the cheapest
+    families, costed per (nnz + 6 m n) x iterations and scaled to all 256 with
+    the GPU's counts."""
     pkg = graft.load_package()
     fams = pkg.workloads.batched_families(256)
     kw = dict(tol=1e-10, max_iter=10000, shift_mode=args.shift_mode, flush=args.flush, true_residuals=True,
-              refine=not args.no_refine, basis_block=args.basis_block)
+              refine=not args.no_refine, basis_block=args.basis_block, persistent=not args.no_persistent,
+              persistent_ctas=args.persistent_ctas)
     for _ in range(max(1, args.warmup)):
         pkg.batch_solve(fams, workers=args.workers, **kw)
     walls, res = [], None
@@ -608,7 +613,10 @@ def run_batch_c4(args, dist: Dist):
             "config": {"workload": "c4: 256 families, n log-uniform in [1e4, 5e5] (2-D 5-point / 3-D 7-point "
                                    "convection-diffusion), 8..64 shifts uniform in [1e-3, 1], b ~ N(0,1)",
                        "workers": args.workers, "shift_mode": args.shift_mode, "refine": not args.no_refine,
+                       "persistent": not args.no_persistent, "persistent_ctas": args.persistent_ctas,
                        "l2": "every family's working set is re-read from HBM"},
+            "persistent_families": sum(1 for f in fams if f.a.n * len(f.sigma) < (1 << 21))
+            if not args.no_persistent and args.shift_mode == "auto" else 0,
             "families_per_s": 256 / value, "total_iterations": iters, "status_failures": status_bad,
             "families_over_tol": over, "max_true_residual": max(r.max_true_residual for r in res),
             "sum_device_solve_s": sum(r.solve_ms for r in res) / 1e3,
@@ -616,9 +624,15 @@ def run_batch_c4(args, dist: Dist):
                                                                              + 8 * len(f.sigma) for f in fams)),
                     "d2h_bytes_per_step": int(sum(8 * len(f.sigma) * f.a.n for f in fams))},
             "clocks": clk.summary(), "cpu_baseline": None}
+    # the same batch with every family on the workers (no shared launch), once
+    if not args.no_persistent:
+        w_res, w_wall = pkg.batch_solve(fams, workers=args.workers, **{**kw, "persistent": False})
+        line["workers_only"] = {"value": w_wall, "unit": "s", "families_per_s": 256 / w_wall,
+                                "status_failures": sum(r.status != 0 for r in w_res),
+                                "persistent_speedup": w_wall / value}
     # the same families one after another through the same API on the same
-    # GPU (one worker: one family on the device at a time), once
-    seq_res, seq_wall = pkg.batch_solve(fams, workers=1, **kw)
+    # GPU (one worker, no shared launch: one family on the device at a time), once
+    seq_res, seq_wall = pkg.batch_solve(fams, workers=1, **{**kw, "persistent": False})
     line["sequential"] = {"value": seq_wall, "unit": "s", "families_per_s": 256 / seq_wall,
                           "status_failures": sum(r.status != 0 for r in seq_res),
                           "batched_speedup": seq_wall / value}
@@ -927,6 +941,9 @@ def main(argv=None):
                     help="time one kernel alone on random data instead of the solve")
     ap.add_argument("--n", type=int, default=2097152, help="elements for --kernel")
     ap.add_argument("--workers", type=int, default=8, help="host workers for --workload c4")
+    ap.add_argument("--no-persistent", action="store_true",
+                    help="--workload c4: every family on the workers (no shared persistent launch)")
+    ap.add_argument("--persistent-ctas", type=int, default=0, help="CTAs of c4's persistent launch (0: one wave)")
     ap.add_argument("--ref-budget", type=float, default=1500.0,
                     help="--impl reference: longest projected full CPU solve (s) to measure; beyond it, estimate")
     args = ap.parse_args(argv)

@@ -97,6 +97,12 @@ class Family(C.Structure):
                 ("wall_ms", C.c_double), ("max_true_residual", C.c_double)]
 
 
+class BatchOpts(C.Structure):
+    """hbicg_batch_opts (include/hbicg.h)"""
+    _fields_ = [("workers", C.c_int), ("persistent", C.c_int), ("persistent_ctas", C.c_int),
+                ("autotune_cache", C.c_char_p)]
+
+
 _lib = None
 
 
@@ -139,6 +145,9 @@ def lib() -> C.CDLL:
                                             C.POINTER(C.c_double)]),
         "hbicg_batch_solve": (C.c_int, [C.POINTER(Family), C.c_int, C.POINTER(Params), C.c_int, C.c_char_p,
                                         C.POINTER(C.c_double)]),
+        "hbicg_batch_opts_default": (None, [C.POINTER(BatchOpts)]),
+        "hbicg_batch_solve_opts": (C.c_int, [C.POINTER(Family), C.c_int, C.POINTER(Params), C.POINTER(BatchOpts),
+                                             C.POINTER(C.c_double)]),
         "hbicg_matrix_spmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
         "hbicg_matrix_time_spmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
                                              C.POINTER(C.c_double)]),
@@ -351,9 +360,11 @@ class FamilyResult:
 
 
 def batch_solve(families, workers: int = 8, autotune: bool = False, autotune_cache: str | None = None,
-                **kw) -> tuple[list, float]:
-    """hbicg_batch_solve over workloads.Family-like objects (a, b, sigma,
-    seed): every family solved with the same parameters (kw as params()).
+                persistent: bool = True, persistent_ctas: int = 0, **kw) -> tuple[list, float]:
+    """hbicg_batch_solve_opts over workloads.Family-like objects (a, b,
+    sigma, seed): every family solved with the same parameters (kw as
+    params()); persistent: the incremental-mode families share one persistent
+    launch (persistent_ctas caps its CTAs, 0 = one wave).
     Returns ([FamilyResult], wall seconds)."""
     p = params(**kw)
     want_res = bool(kw.get("true_residuals", False))
@@ -375,8 +386,13 @@ def batch_solve(families, workers: int = 8, autotune: bool = False, autotune_cac
         fa.x = x.ctypes.data_as(_PD)
         fa.true_residual = res.ctypes.data_as(_PD) if want_res else None
     wall = C.c_double()
-    lib().hbicg_batch_solve(arr, len(families), C.byref(p), int(workers),
-                            str(autotune_cache).encode() if autotune_cache else None, C.byref(wall))
+    opts = BatchOpts()
+    lib().hbicg_batch_opts_default(C.byref(opts))
+    opts.workers = int(workers)
+    opts.persistent = 1 if persistent else 0
+    opts.persistent_ctas = int(persistent_ctas)
+    opts.autotune_cache = str(autotune_cache).encode() if autotune_cache else None
+    lib().hbicg_batch_solve_opts(arr, len(families), C.byref(p), C.byref(opts), C.byref(wall))
     out = []
     for i in range(len(families)):
         fa = arr[i]

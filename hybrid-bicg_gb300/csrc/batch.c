@@ -10,6 +10,12 @@
  * nnz * m first) and runs them concurrently: the GPU interleaves the kernels of
  * several families.  Each family is a complete reference-semantics solve
  * (hbicg_solver_run), with the optional SpMV-form autotuner in front.
+ *
+ * Small families (incremental shift mode: n m < 2^21 with the automatic mode)
+ * are latency-bound when each runs its own short kernels: they instead go to
+ * one host thread that sets all of them up on one context and runs all their
+ * iterations in ONE persistent cooperative launch (hbicg__group_solve,
+ * hbk_group_run), while the workers take the larger families.
  * Failures are per family (status), never global. */
 #define _GNU_SOURCE
 #include <pthread.h>
@@ -18,6 +24,7 @@
 #include <time.h>
 
 #include "hbicg.h"
+#include "host_internal.h"
 
 typedef struct {
     hbicg_family *fams;
@@ -60,6 +67,93 @@ static void solve_one(hbicg_context *ctx, hbicg_family *f, const hbicg_params *p
     f->wall_ms = now_ms() - t0;
 }
 
+static void family_stats(hbicg_family *f, const hbicg_stats *st) {
+    f->k = st->k;
+    f->n_switches = st->n_switches;
+    f->final_seed = st->final_seed;
+    f->solve_ms = st->solve_ms;
+    f->max_true_residual = st->max_true_residual;
+}
+
+/* families of one persistent launch (see the file comment) */
+typedef struct {
+    hbicg_family *fams;
+    const int *idx;
+    int count;
+    const hbicg_params *p;
+    int ctas;
+} group_t;
+
+static void *group_run(void *arg) {
+    group_t *g = arg;
+    const double t0 = now_ms();
+    const int n = g->count;
+    hbicg_context *ctx = NULL;
+    int crc = hbicg_context_create(&ctx);
+    hbicg_matrix **A = calloc((size_t)n, sizeof *A);
+    hbicg_solver **S = calloc((size_t)n, sizeof *S), **GS = calloc((size_t)n, sizeof *GS);
+    const double **B = calloc((size_t)n, sizeof *B), **SG = calloc((size_t)n, sizeof *SG);
+    double **X = calloc((size_t)n, sizeof *X);
+    int *seed = calloc((size_t)n, sizeof *seed), *rc = calloc((size_t)n, sizeof *rc), *who = calloc((size_t)n, sizeof *who);
+    hbicg_stats *ST = calloc((size_t)n, sizeof *ST);
+    if (!A || !S || !GS || !B || !SG || !X || !seed || !rc || !who || !ST) crc = HBICG_E_NOMEM;
+    int ng = 0;
+    for (int i = 0; i < n; ++i) {
+        hbicg_family *f = &g->fams[g->idx[i]];
+        if (crc != HBICG_OK) {
+            f->status = crc;
+            continue;
+        }
+        f->status = hbicg_matrix_create(ctx, f->n, f->nnz, f->ptr, f->col, f->val, HBICG_HOST, &A[i]);
+        if (f->status == HBICG_OK) {
+            f->spmv_format = hbicg_matrix_format(A[i]);
+            f->status = hbicg_solver_create(ctx, A[i], f->m, g->p, &S[i]);
+        }
+        if (f->status != HBICG_OK) continue;
+        if (hbicg__group_eligible(S[i])) {
+            GS[ng] = S[i];
+            B[ng] = f->b;
+            SG[ng] = f->sigma;
+            X[ng] = f->x;
+            seed[ng] = f->seed;
+            ST[ng].true_residual = f->true_residual;
+            who[ng++] = g->idx[i];
+        } else { /* another form after all (e.g. rows too long for SELL-32): a solve of its own */
+            hbicg_stats st;
+            memset(&st, 0, sizeof st);
+            st.true_residual = f->true_residual;
+            f->status = hbicg_solver_run(S[i], f->b, f->sigma, f->seed, HBICG_HOST, f->x, f->r, HBICG_HOST, &st);
+            family_stats(f, &st);
+        }
+    }
+    if (ng) {
+        const int grc = hbicg__group_solve(GS, ng, B, SG, seed, X, ST, rc, g->ctas);
+        for (int q = 0; q < ng; ++q) {
+            hbicg_family *f = &g->fams[who[q]];
+            f->status = grc != HBICG_OK ? grc : rc[q];
+            family_stats(f, &ST[q]);
+        }
+    }
+    for (int i = 0; i < n && S && A; ++i) {
+        hbicg_solver_destroy(S[i]);
+        hbicg_matrix_destroy(A[i]);
+    }
+    if (ctx) hbicg_context_destroy(ctx);
+    const double wall = now_ms() - t0;
+    for (int i = 0; i < n; ++i) g->fams[g->idx[i]].wall_ms = wall;
+    free(A);
+    free(S);
+    free(GS);
+    free(B);
+    free(SG);
+    free(X);
+    free(seed);
+    free(rc);
+    free(who);
+    free(ST);
+    return NULL;
+}
+
 static void *worker(void *arg) {
     batch_t *b = arg;
     hbicg_context *ctx = NULL;
@@ -86,17 +180,39 @@ static int by_cost_desc(const void *x, const void *y) {
     return *(const int *)x - *(const int *)y;
 }
 
+void hbicg_batch_opts_default(hbicg_batch_opts *o) {
+    memset(o, 0, sizeof *o);
+    o->workers = 8;
+    o->persistent = 1;
+}
+
 int hbicg_batch_solve(hbicg_family *fams, int count, const hbicg_params *p, int workers, const char *autotune_cache,
                       double *wall_ms) {
-    if (count < 0 || (count && !fams)) return HBICG_E_ARG;
+    hbicg_batch_opts o;
+    hbicg_batch_opts_default(&o);
+    o.workers = workers;
+    o.autotune_cache = autotune_cache;
+    return hbicg_batch_solve_opts(fams, count, p, &o, wall_ms);
+}
+
+int hbicg_batch_solve_opts(hbicg_family *fams, int count, const hbicg_params *p, const hbicg_batch_opts *opts,
+                           double *wall_ms) {
+    if (count < 0 || (count && !fams) || !opts) return HBICG_E_ARG;
     const double t0 = now_ms();
     hbicg_params def;
     if (!p) {
         hbicg_params_default(&def);
         p = &def;
     }
+    int workers = opts->workers;
+    const char *autotune_cache = opts->autotune_cache;
     int *order = malloc(sizeof(int) * (size_t)(count > 0 ? count : 1));
-    if (!order) return HBICG_E_NOMEM;
+    int *grp = malloc(sizeof(int) * (size_t)(count > 0 ? count : 1));
+    if (!order || !grp) {
+        free(order);
+        free(grp);
+        return HBICG_E_NOMEM;
+    }
     for (int i = 0; i < count; i++) {
         order[i] = i;
         fams[i].status = -1;
@@ -106,6 +222,23 @@ int hbicg_batch_solve(hbicg_family *fams, int count, const hbicg_params *p, int 
     g_sort_base = fams;
     qsort(order, (size_t)count, sizeof(int), by_cost_desc);
     pthread_mutex_unlock(&sort_lock);
+    /* the families of the persistent launch leave the workers' queue */
+    int ng = 0, nw = 0;
+    for (int i = 0; i < count; i++) {
+        const hbicg_family *f = &fams[order[i]];
+        const int small = opts->persistent && p->form == HBICG_FORM_FUSED && !f->autotune && !f->r && f->m > 0 &&
+                          hbicg__shift_mode_for(p, f->n, f->m) == HBICG_SHIFTS_INCREMENTAL;
+        if (small) grp[ng++] = order[i];
+        else order[nw++] = order[i];
+    }
+    count = nw;
+    group_t gr = {fams, grp, ng, p, opts->persistent_ctas};
+    pthread_t gth;
+    int g_started = 0;
+    if (ng) {
+        if (pthread_create(&gth, NULL, group_run, &gr) == 0) g_started = 1;
+        else group_run(&gr);
+    }
     if (workers < 1) workers = 8;
     if (workers > count) workers = count > 0 ? count : 1;
     if (workers > 64) workers = 64;
@@ -116,9 +249,12 @@ int hbicg_batch_solve(hbicg_family *fams, int count, const hbicg_params *p, int 
         if (pthread_create(&th[t], NULL, worker, &b) != 0) break;
         started++;
     }
-    if (!started) worker(&b); /* no threads: run in the caller */
+    if (!started && count) worker(&b); /* no threads: run in the caller */
     for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+    if (g_started) pthread_join(gth, NULL);
+    count = nw + ng;
     free(order);
+    free(grp);
     if (wall_ms) *wall_ms = now_ms() - t0;
     for (int i = 0; i < count; i++)
         if (fams[i].status != HBICG_OK) return fams[i].status < 0 ? HBICG_E_ARG : fams[i].status;

@@ -47,17 +47,57 @@ __device__ __forceinline__ double2 block_sum2(double2 v, double *sh) {
 }
 
 // Writes this block's partial(s) and takes a ticket; returns true in every
-// thread of the block that arrives last.  That block then sums the partials
-// in block-index order (fixed tree), so results do not depend on timing.
-__device__ __forceinline__ bool take_ticket(unsigned *counter) {
+// thread of the block that arrives last of `nb` blocks (the launch's grid by
+// default).  That block then sums the partials in block-index order (fixed
+// tree), so results do not depend on timing.
+__device__ __forceinline__ bool take_ticket(unsigned *counter, unsigned nb) {
     __shared__ int s_last;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    if (threadIdx.x == 0) s_last = (atomicAdd(counter, 1u) == nb - 1);
     __syncthreads();
     if (s_last) __threadfence();
     return s_last != 0;
 }
+__device__ __forceinline__ bool take_ticket(unsigned *counter) { return take_ticket(counter, gridDim.x); }
+
+// Which block of how many: the launch's own grid (HwGrid), or a virtual grid
+// of `vnb` blocks that one CTA of a persistent launch plays in turn (VGrid).
+// Loads of vectors that the same launch also writes go through ld/ldx: a
+// plain load (and the read-only path for the SpMV gather) in a kernel that
+// runs one step, an L2 load in a persistent kernel, where the read-only
+// cache may still hold a value from an earlier step.
+struct HwGrid {
+    static constexpr bool hw = true;
+    __device__ __forceinline__ unsigned b() const { return blockIdx.x; }
+    __device__ __forceinline__ unsigned nb() const { return gridDim.x; }
+    template <class T>
+    __device__ static __forceinline__ T ld(const T *p) { return *p; }
+    template <class T>
+    __device__ static __forceinline__ T ldx(const T *p) { return __ldg(p); }
+};
+// element i of a vector the launch also writes (p indexed directly in a
+// one-step kernel, so its code is what it was without grid views)
+#define HBK_LD(G, p, i) ((G::hw) ? (p)[i] : __ldcg((p) + (i)))
+
+template <class G>
+struct is_hw_grid {
+    static constexpr bool value = false;
+};
+template <>
+struct is_hw_grid<HwGrid> {
+    static constexpr bool value = true;
+};
+struct VGrid {
+    static constexpr bool hw = false;
+    unsigned vb, vnb;
+    __device__ __forceinline__ unsigned b() const { return vb; }
+    __device__ __forceinline__ unsigned nb() const { return vnb; }
+    template <class T>
+    __device__ static __forceinline__ T ld(const T *p) { return __ldcg(p); }
+    template <class T>
+    __device__ static __forceinline__ T ldx(const T *p) { return __ldcg(p); }
+};
 
 // Called by the last block: sums partials[0..nparts) in a fixed order.
 __device__ __forceinline__ double sum_partials(const double *partials, int nparts, double *sh) {
@@ -122,15 +162,16 @@ struct SpmvSmem {
 // of column indices, so every load is coalesced and no shared memory or
 // barrier is needed; each row is still summed in stored order with FMAs from
 // 0, exactly as in the TILE path (padding entries are skipped by row length).
-template <class Epi>
-__device__ __forceinline__ void spmv_rows_sell(const hbk_matrix &A, const double *__restrict__ x, Epi &epi) {
+template <class Epi, class G = HwGrid>
+__device__ __forceinline__ void spmv_rows_sell(const hbk_matrix &A, const double *__restrict__ x, Epi &epi,
+                                               const G &g = G()) {
     const unsigned *__restrict__ ptr = A.ptr;
     const double *__restrict__ sval = A.sval;
     const unsigned *__restrict__ scol = A.scol;
     const unsigned n = A.n;
     const unsigned ns = (n + 31) / 32;
-    const unsigned stride = gridDim.x * NT;
-    for (unsigned r0 = blockIdx.x * NT; r0 < n; r0 += stride) {
+    const unsigned stride = g.nb() * NT;
+    for (unsigned r0 = g.b() * NT; r0 < n; r0 += stride) {
         const unsigned r = r0 + threadIdx.x;
         const unsigned s = r >> 5, lane = r & 31;
         unsigned long long base = 0;
@@ -145,7 +186,7 @@ __device__ __forceinline__ void spmv_rows_sell(const hbk_matrix &A, const double
         double acc = 0.0;
 #pragma unroll 4
         for (unsigned e = 0; e < w; ++e) {
-            if (e < len) acc = fma(__ldg(vv + 32 * (size_t)e), __ldg(x + __ldg(cc + 32 * (size_t)e)), acc);
+            if (e < len) acc = fma(__ldg(vv + 32 * (size_t)e), G::ldx(x + __ldg(cc + 32 * (size_t)e)), acc);
         }
         if (r < n) epi(r, acc);
     }
@@ -385,10 +426,13 @@ __device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const doubl
 
 // Format chosen at compile time so the SELL kernels carry no shared-memory
 // tile (full occupancy); launchers pick the instantiation from A.fmt.
-template <int FMT, class Epi>
-__device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__restrict__ x, Epi &epi) {
+// (the virtual grids of a persistent launch take the SELL-32 form only)
+template <int FMT, class Epi, class G = HwGrid>
+__device__ __forceinline__ void spmv_rows(const hbk_matrix &A, const double *__restrict__ x, Epi &epi,
+                                          const G &g = G()) {
+    static_assert(FMT == HBK_FMT_SELL || is_hw_grid<G>::value, "virtual grids take the SELL-32 form only");
     if constexpr (FMT == HBK_FMT_SELL) {
-        spmv_rows_sell(A, x, epi);
+        spmv_rows_sell(A, x, epi, g);
     } else if constexpr (FMT == HBK_FMT_HYB) {
         spmv_rows_hyb(A, x, epi);
     } else if constexpr (FMT == HBK_FMT_MERGE) {

@@ -61,6 +61,12 @@ int hbicg__sell_diag(hbicg_matrix *A);
 /* device arrays from the library's stream-ordered pool (solver.c) */
 cudaError_t hbicg__dev_alloc(void **p, size_t bytes, cudaStream_t st);
 void hbicg__dev_free(void *p, cudaStream_t st);
+/* the shift mode a solver made with p takes for n rows and m shifts */
+int hbicg__shift_mode_for(const hbicg_params *p, unsigned n, int m);
+/* many families' iterations in one persistent launch (solver.c) */
+int hbicg__group_eligible(const hbicg_solver *s);
+int hbicg__group_solve(hbicg_solver **S, int nf, const double *const *b, const double *const *sigma, const int *seed,
+                       double *const *x, hbicg_stats *st, int *rc, int max_ctas);
 const hbk_matrix *hbicg__matrix_kernel_view(const hbicg_matrix *A);
 hbicg_context *hbicg__matrix_context(const hbicg_matrix *A);
 /* y (+)= A x for host arrays, on a process-wide context (matrix.h's mult) */

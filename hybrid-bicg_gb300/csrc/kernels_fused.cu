@@ -15,6 +15,8 @@
 //                 the Krylov basis; materialise the new seed's p after a switch
 // Reference: src/solver_dynamic.c:147-381 (seed step :156-210, shift loop
 // :239-256, convergence test :278-303, seed switch :312-359).
+#include <vector>
+
 #include "hbk_device.cuh"
 
 using namespace hbk;
@@ -50,7 +52,9 @@ __device__ __forceinline__ double *vec_q(const Ctx &c, const hbk_scalars *sc) {
     return c.v.deferred ? c.v.V + (size_t)sc->slots * ldn(c.v.n) : c.v.q;
 }
 
-__device__ __forceinline__ bool stopped(const hbk_scalars *sc) { return sc->finished != 0; }
+// (an L2 load: in a persistent launch another CTA may have set the flag
+// since this SM last read it)
+__device__ __forceinline__ bool stopped(const hbk_scalars *sc) { return __ldcg(&sc->finished) != 0; }
 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(NT) k_init(Ctx c, int seed, double tol) {
@@ -118,8 +122,8 @@ __global__ void __launch_bounds__(NT) k_init_coef(Ctx c) {
 
 // ---------------------------------------------------------------------------
 // K1: s = (A + sigma_s I) p_s and (r^, s)
-template <int FMT>
-__global__ void __launch_bounds__(NT) k_seed_s(Ctx c) {
+template <int FMT, class G>
+__device__ __forceinline__ void seed_s_body(const Ctx &c, const G &g) {
     __shared__ double red[2 * NW];
     hbk_scalars *sc = c.sh.sc;
     if (stopped(sc)) return;
@@ -131,15 +135,15 @@ __global__ void __launch_bounds__(NT) k_seed_s(Ctx c) {
     const bool folded = c.v.sval_shift != nullptr;  // the product already holds sigma p
     double acc = 0.0;
     auto epi = [&](unsigned r, double ax) {
-        const double sv = folded ? ax : fma(sig, ps[r], ax);
+        const double sv = folded ? ax : fma(sig, HBK_LD(G, ps, r), ax);
         s[r] = sv;
-        acc = fma(rh[r], sv, acc);
+        acc = fma(HBK_LD(G, rh, r), sv, acc);
     };
-    spmv_rows<FMT>(c.A, ps, epi);
+    spmv_rows<FMT>(c.A, ps, epi, g);
     acc = block_sum(acc, red);
-    if (threadIdx.x == 0) c.sh.partials[blockIdx.x] = acc;
-    if (take_ticket(c.sh.counters + 0)) {
-        const double rs = sum_partials(c.sh.partials, gridDim.x, red);
+    if (threadIdx.x == 0) c.sh.partials[g.b()] = acc;
+    if (take_ticket(c.sh.counters + 0, g.nb())) {
+        const double rs = sum_partials(c.sh.partials, g.nb(), red);
         if (threadIdx.x == 0) {
             const int k = sc->k;
             const double a = dvd(sc->rr_hat, rs);
@@ -154,10 +158,13 @@ __global__ void __launch_bounds__(NT) k_seed_s(Ctx c) {
         }
     }
 }
+template <int FMT>
+__global__ void __launch_bounds__(NT) k_seed_s(Ctx c) { seed_s_body<FMT>(c, HwGrid()); }
 
 // K2: q = r_{k-1} - alpha s (deferred mode: q is a basis slot; its max |q| is
 // kept for the flush)
-__global__ void __launch_bounds__(NT) k_seed_q(Ctx c) {
+template <class G>
+__device__ __forceinline__ void seed_q_body(const Ctx &c, const G &g) {
     __shared__ unsigned long long smx[NW];
     const hbk_scalars *sc = c.sh.sc;
     if (stopped(sc)) return;
@@ -167,18 +174,19 @@ __global__ void __launch_bounds__(NT) k_seed_q(Ctx c) {
     double *__restrict__ q = vec_q(c, sc);
     const unsigned n = c.v.n;
     unsigned long long mx = 0;
-    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
-        const double qi = fma(-a, s[i], ro[i]);
+    for (size_t i = g.b() * (size_t)NT + threadIdx.x; i < n; i += (size_t)g.nb() * NT) {
+        const double qi = fma(-a, HBK_LD(G, s, i), HBK_LD(G, ro, i));
         q[i] = qi;
         const unsigned long long b = abs_bits(qi);
         mx = b > mx ? b : mx;
     }
     if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + (size_t)sc->slots * HBK_SLOT_SPREAD);
 }
+__global__ void __launch_bounds__(NT) k_seed_q(Ctx c) { seed_q_body(c, HwGrid()); }
 
 // K3: y = (A + sigma_s I) q, (q,q) and (q,y)
-template <int FMT>
-__global__ void __launch_bounds__(NT) k_seed_y(Ctx c) {
+template <int FMT, class G>
+__device__ __forceinline__ void seed_y_body(const Ctx &c, const G &g) {
     __shared__ double red[2 * NW];
     hbk_scalars *sc = c.sh.sc;
     if (stopped(sc)) return;
@@ -188,21 +196,21 @@ __global__ void __launch_bounds__(NT) k_seed_y(Ctx c) {
     const bool folded = c.v.sval_shift != nullptr;  // the product already holds sigma q
     double2 acc = make_double2(0.0, 0.0);
     auto epi = [&](unsigned r, double ax) {
-        const double qr = q[r];
+        const double qr = HBK_LD(G, q, r);
         const double yv = folded ? ax : fma(sig, qr, ax);
         y[r] = yv;
         acc.x = fma(qr, qr, acc.x);
         acc.y = fma(qr, yv, acc.y);
     };
-    spmv_rows<FMT>(c.A, q, epi);
+    spmv_rows<FMT>(c.A, q, epi, g);
     acc = block_sum2(acc, red);
     if (threadIdx.x == 0) {
-        c.sh.partials[blockIdx.x] = acc.x;
-        c.sh.partials[HBK_MAX_GRID + blockIdx.x] = acc.y;
+        c.sh.partials[g.b()] = acc.x;
+        c.sh.partials[HBK_MAX_GRID + g.b()] = acc.y;
     }
-    if (take_ticket(c.sh.counters + 1)) {
-        const double qq = sum_partials(c.sh.partials, gridDim.x, red);
-        const double qy = sum_partials(c.sh.partials + HBK_MAX_GRID, gridDim.x, red);
+    if (take_ticket(c.sh.counters + 1, g.nb())) {
+        const double qq = sum_partials(c.sh.partials, g.nb(), red);
+        const double qy = sum_partials(c.sh.partials + HBK_MAX_GRID, g.nb(), red);
         if (threadIdx.x == 0) {
             const int k = sc->k;
             const double w = dvd(qq, qy);
@@ -219,6 +227,8 @@ __global__ void __launch_bounds__(NT) k_seed_y(Ctx c) {
         }
     }
 }
+template <int FMT>
+__global__ void __launch_bounds__(NT) k_seed_y(Ctx c) { seed_y_body<FMT>(c, HwGrid()); }
 
 // ---------------------------------------------------------------------------
 // End of the seed step, run by the last block of K4: beta, the shift
@@ -433,7 +443,8 @@ __device__ void seed_step_scalars(const Ctx &c, double rr, double rrh) {
 // K4: x_s += alpha p_s + omega q ; r_k = q - omega y ; (r,r), (r^,r)
 // (at least 4 CTAs per SM: the streaming loop needs the warps; the scalar
 // stage that runs in one CTA per iteration may spill)
-__global__ void __launch_bounds__(NT, 4) k_seed_update(Ctx c) {
+template <class G>
+__device__ __forceinline__ void seed_update_body(const Ctx &c, const G &g) {
     __shared__ double sh[2 * NW];
     __shared__ unsigned long long smx[NW];
     hbk_scalars *sc = c.sh.sc;
@@ -454,30 +465,31 @@ __global__ void __launch_bounds__(NT, 4) k_seed_update(Ctx c) {
     const bool dm = c.v.deferred != 0;
     double *__restrict__ xrow = dm ? c.v.Xp : c.v.X + (size_t)seed * ldn(n);
     const int pm = c.v.pm;
-    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
-        const double qi = q[i];
+    for (size_t i = g.b() * (size_t)NT + threadIdx.x; i < n; i += (size_t)g.nb() * NT) {
+        const double qi = HBK_LD(G, q, i);
         double *xi = dm ? xrow + panel_idx(seed, (unsigned)i, pm) : xrow + i;
-        *xi = fma(w, qi, fma(a, ps[i], *xi));
-        const double r = fma(-w, y[i], qi);
+        *xi = fma(w, qi, fma(a, HBK_LD(G, ps, i), HBK_LD(G, xi, 0)));
+        const double r = fma(-w, HBK_LD(G, y, i), qi);
         rn[i] = r;
         acc.x = fma(r, r, acc.x);
-        acc.y = fma(rh[i], r, acc.y);
+        acc.y = fma(HBK_LD(G, rh, i), r, acc.y);
         const unsigned long long b = abs_bits(r);
         mx = b > mx ? b : mx;
     }
     if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + (size_t)(sc->slots + 1) * HBK_SLOT_SPREAD);  // r_k
     acc = block_sum2(acc, sh);
     if (threadIdx.x == 0) {
-        c.sh.partials[blockIdx.x] = acc.x;
-        c.sh.partials[HBK_MAX_GRID + blockIdx.x] = acc.y;
+        c.sh.partials[g.b()] = acc.x;
+        c.sh.partials[HBK_MAX_GRID + g.b()] = acc.y;
     }
-    if (take_ticket(c.sh.counters + 2)) {
-        const double rr = sum_partials(c.sh.partials, gridDim.x, sh);
-        const double rrh = sum_partials(c.sh.partials + HBK_MAX_GRID, gridDim.x, sh);
+    if (take_ticket(c.sh.counters + 2, g.nb())) {
+        const double rr = sum_partials(c.sh.partials, g.nb(), sh);
+        const double rrh = sum_partials(c.sh.partials + HBK_MAX_GRID, g.nb(), sh);
         seed_step_scalars(c, rr, rrh);
         if (threadIdx.x == 0) c.sh.counters[2] = 0;
     }
 }
+__global__ void __launch_bounds__(NT, 4) k_seed_update(Ctx c) { seed_update_body(c, HwGrid()); }
 
 // End of an iteration (one thread): apply the switch, advance k, test the loop.
 __device__ void finish_iteration(const Ctx &c, hbk_scalars *sc, double rrh_scaled) {
@@ -504,8 +516,8 @@ __device__ void finish_iteration(const Ctx &c, hbk_scalars *sc, double rrh_scale
 
 // K5 (incremental): p_s, then every running shift's x_j and p_j in one pass
 // over q, r_{k-1}, r_k (src/solver_dynamic.c:208-210, :248-255)
-template <int MAXS>
-__global__ void __launch_bounds__(NT) k_shift_update(Ctx c) {
+template <int MAXS, class G>
+__device__ __forceinline__ void shift_update_body(const Ctx &c, const G &g) {
     __shared__ double s_co[MAXS * 6];
     __shared__ int s_j[MAXS];
     __shared__ double sh[NW];
@@ -534,14 +546,14 @@ __global__ void __launch_bounds__(NT) k_shift_update(Ctx c) {
             for (int t = 0; t < 6; t++) s_co[a * 6 + t] = co[t];
         }
         __syncthreads();
-        for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
-            const double qi = q[i], oi = ro[i], ri = rn[i];
-            if (base == 0) ps[i] = fma(bw, s[i], fma(bk, ps[i], ri));
+        for (size_t i = g.b() * (size_t)NT + threadIdx.x; i < n; i += (size_t)g.nb() * NT) {
+            const double qi = HBK_LD(G, q, i), oi = HBK_LD(G, ro, i), ri = HBK_LD(G, rn, i);
+            if (base == 0) ps[i] = fma(bw, HBK_LD(G, s, i), fma(bk, HBK_LD(G, ps, i), ri));
             for (int a = 0; a < cnt; a++) {
                 const double *co = s_co + a * 6;
                 double *xj = c.v.X + (size_t)s_j[a] * ld;
                 double *pj = c.v.P + (size_t)s_j[a] * ld;
-                double x = xj[i], p = pj[i];
+                double x = HBK_LD(G, xj, i), p = HBK_LD(G, pj, i);
                 x = fma(co[0], qi, x);
                 x = fma(co[1], p, x);
                 p = fma(co[2], qi, p);
@@ -554,22 +566,24 @@ __global__ void __launch_bounds__(NT) k_shift_update(Ctx c) {
             if (sw && base + MAXS >= na) {
                 const double rs = ri * rsc;
                 rn[i] = rs;
-                acc = fma(rh[i], rs, acc);
+                acc = fma(HBK_LD(G, rh, i), rs, acc);
             }
         }
         __syncthreads();
         if (na <= MAXS) break;
     }
     acc = block_sum(acc, sh);
-    if (threadIdx.x == 0) c.sh.partials[blockIdx.x] = acc;
-    if (take_ticket(c.sh.counters + 3)) {
-        const double rrh = sum_partials(c.sh.partials, gridDim.x, sh);
+    if (threadIdx.x == 0) c.sh.partials[g.b()] = acc;
+    if (take_ticket(c.sh.counters + 3, g.nb())) {
+        const double rrh = sum_partials(c.sh.partials, g.nb(), sh);
         if (threadIdx.x == 0) {
             finish_iteration(c, sc, rrh);
             c.sh.counters[3] = 0;
         }
     }
 }
+template <int MAXS>
+__global__ void __launch_bounds__(NT) k_shift_update(Ctx c) { shift_update_body<MAXS>(c, HwGrid()); }
 
 // K5 (deferred): p_s update; on a switch the rescaled r_k goes to a new slot
 __global__ void __launch_bounds__(NT) k_seed_p_deferred(Ctx c) {
@@ -843,6 +857,107 @@ __global__ void __launch_bounds__(NT) k_panel_to_rows(const double *__restrict__
     }
 }
 
+// ---------------------------------------------------------------------------
+// Many families in one persistent launch (incremental shift mode, SELL-32).
+//
+// Each family's rows are cut into virtual blocks of HBK_GROUP_ROWS rows; the
+// CTAs of one cooperative launch take the virtual blocks of all families in
+// turn (virtual block v goes to CTA v mod grid, so a family's rows stay on
+// the same CTAs from step to step) and run, for every family at once, the
+// same five steps as the one-family kernels (K1..K5 above, with a virtual
+// block in place of the launch's block: same partial sums, same last-block
+// tickets and scalar stage per family).  A grid-wide barrier separates the
+// steps.  Families stop one by one (converged, max_iter, breakdown); their
+// virtual blocks then return at once.
+struct GroupFam {
+    Ctx c;
+    unsigned vb0, nvb;  // the family's virtual blocks [vb0, vb0 + nvb)
+};
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned *p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Barrier over every CTA of a cooperative launch: bar[0] counts arrivals,
+// bar[1] is the generation (the last CTA to arrive resets the count and bumps
+// it, with release order; the others wait for it with acquire loads).  A wait
+// longer than HBK_GROUP_WAIT_NS sets *err; every CTA that sees *err leaves the
+// wait, so the launch ends (with the error) instead of hanging.  Returns
+// false in every thread of the CTA when the launch must stop.
+__device__ bool grid_barrier(unsigned *bar, int *err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned gen = ld_acquire_u32(bar + 1);
+        const unsigned arrived = atom_add_acq_rel_u32(bar, 1u) + 1u;
+        if (arrived == gridDim.x) {
+            atomicExch(bar, 0u);
+            st_release_u32(bar + 1, gen + 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            while (ld_acquire_u32(bar + 1) == gen) {
+                if (*(volatile int *)err) {
+                    ok = 0;
+                    break;
+                }
+                if (global_ns() - t0 > HBK_GROUP_WAIT_NS) {
+                    atomicExch(err, HBK_GROUP_ERR_WAIT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+            __threadfence();
+        }
+        s_ok = ok && *(volatile int *)err == 0;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <int MAXS>
+__global__ void __launch_bounds__(NT) k_group(const GroupFam *__restrict__ fams, int nf,
+                                              const unsigned *__restrict__ vb_fam, unsigned nvb, unsigned *bar,
+                                              int *err, int iter_cap) {
+#define HBK_GROUP_STEP(body)                                                       \
+    for (unsigned vb = blockIdx.x; vb < nvb; vb += gridDim.x) {                    \
+        const GroupFam &F = fams[vb_fam[vb]];                                      \
+        body(F.c, VGrid{vb - F.vb0, F.nvb});                                       \
+    }                                                                              \
+    if (!grid_barrier(bar, err)) return;
+    for (int it = 0; it <= iter_cap; ++it) {
+        // any family still running?  (read between two barriers: no step
+        // writes a family's stop flag meanwhile, so every CTA sees the same)
+        int alive = 0;
+        for (int f = threadIdx.x; f < nf; f += NT) alive |= __ldcg(&fams[f].c.sh.sc->finished) == 0;
+        alive = __syncthreads_or(alive);
+        if (!grid_barrier(bar, err) || !alive) return;
+        HBK_GROUP_STEP(seed_s_body<HBK_FMT_SELL>)
+        HBK_GROUP_STEP(seed_q_body)
+        HBK_GROUP_STEP(seed_y_body<HBK_FMT_SELL>)
+        HBK_GROUP_STEP(seed_update_body)
+        HBK_GROUP_STEP(shift_update_body<MAXS>)
+    }
+#undef HBK_GROUP_STEP
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(err, HBK_GROUP_ERR_CAP);
+}
+
 }  // namespace
 
 extern "C" {
@@ -942,6 +1057,70 @@ int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shi
         k_materialize_ps<<<wave_grid<k_materialize_ps>(gv), NT, 0, st>>>(c);
     }
     return (int)cudaGetLastError();
+}
+
+static unsigned group_vblocks(unsigned n) {
+    const unsigned v = (n + HBK_GROUP_ROWS - 1) / HBK_GROUP_ROWS;
+    return v < 1 ? 1 : (v > HBK_MAX_GRID ? HBK_MAX_GRID : v);
+}
+
+static const size_t kGroupHead = 256;  // barrier words and the error flag
+
+static size_t group_bytes(int nf, size_t nvb) {
+    return kGroupHead + ((sizeof(GroupFam) * (size_t)nf + 255) / 256) * 256 + sizeof(unsigned) * nvb;
+}
+
+size_t hbk_group_ws_bytes(int nf, const hbk_vectors *v) {
+    size_t nvb = 0;
+    for (int f = 0; f < nf; ++f) nvb += group_vblocks(v[f].n);
+    return group_bytes(nf, nvb);
+}
+
+int hbk_group_ctas(int max_ctas) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_group<64>, NT, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const int one_wave = per_sm * sm_count();
+    return max_ctas > 0 && max_ctas < one_wave ? max_ctas : one_wave;
+}
+
+int hbk_group_run(int nf, const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, int iter_cap, int max_ctas,
+                  void *ws, size_t ws_bytes, int *err_out, cudaStream_t st) {
+    *err_out = 0;
+    if (nf <= 0) return 0;
+    int dev = 0, coop = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop) return (int)cudaErrorNotSupported;
+    std::vector<GroupFam> tab((size_t)nf);
+    std::vector<unsigned> map;
+    for (int f = 0; f < nf; ++f) {
+        if (A[f].fmt != HBK_FMT_SELL || v[f].deferred) return (int)cudaErrorInvalidValue;
+        tab[f].c = make_ctx(&A[f], &v[f], &sh[f]);
+        tab[f].vb0 = (unsigned)map.size();
+        tab[f].nvb = group_vblocks(v[f].n);
+        map.insert(map.end(), tab[f].nvb, (unsigned)f);
+    }
+    const unsigned nvb = (unsigned)map.size();
+    if (ws_bytes < group_bytes(nf, nvb)) return (int)cudaErrorInvalidValue;
+    char *base = (char *)ws;
+    unsigned *bar = (unsigned *)base;
+    int *err = (int *)(base + 64);
+    GroupFam *dtab = (GroupFam *)(base + kGroupHead);
+    unsigned *dmap = (unsigned *)(base + kGroupHead + ((sizeof(GroupFam) * (size_t)nf + 255) / 256) * 256);
+    int e;
+    if ((e = (int)cudaMemsetAsync(base, 0, kGroupHead, st))) return e;
+    if ((e = (int)cudaMemcpyAsync(dtab, tab.data(), sizeof(GroupFam) * (size_t)nf, cudaMemcpyHostToDevice, st)))
+        return e;
+    if ((e = (int)cudaMemcpyAsync(dmap, map.data(), sizeof(unsigned) * (size_t)nvb, cudaMemcpyHostToDevice, st)))
+        return e;
+    const int ctas = hbk_group_ctas(max_ctas);
+    const GroupFam *a0 = dtab;
+    const unsigned *a2 = dmap;
+    void *args[] = {(void *)&a0, (void *)&nf, (void *)&a2, (void *)&nvb, (void *)&bar, (void *)&err, (void *)&iter_cap};
+    if ((e = (int)cudaLaunchCooperativeKernel((const void *)k_group<64>, dim3(ctas), dim3(NT), args, 0, st))) return e;
+    /* pageable destination: returns once the launch has finished */
+    return (int)cudaMemcpyAsync(err_out, err, sizeof(int), cudaMemcpyDeviceToHost, st);
 }
 
 int hbk_loop_condition(const hbk_shifts *sh, cudaGraphConditionalHandle cond, int loop_cap, cudaStream_t st) {

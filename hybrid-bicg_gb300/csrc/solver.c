@@ -219,6 +219,8 @@ static int pick_mode(const hbicg_params *p, unsigned n, int m) {
     return HBICG_SHIFTS_INCREMENTAL;
 }
 
+int hbicg__shift_mode_for(const hbicg_params *p, unsigned n, int m) { return pick_mode(p, n, m); }
+
 /* Solver buffers come from a library-owned stream-ordered pool per device that
  * keeps freed memory for the next solver (release threshold: unlimited): a
  * one-shot call such as the reference's entry points, which sets up and tears
@@ -761,15 +763,23 @@ static int do_flush(hbicg_solver *s, int keep_p, int L, int k_last, int *launche
     return HBICG_OK;
 }
 
-static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, double *flush_ms) {
+/* first step of a fused solve: the device scalars, r and p_j (or the basis) from b */
+static int fused_init(hbicg_solver *s, int seed, int *launches) {
     cudaStream_t st = s->ctx->stream;
-    hbk_scalars *h = s->ctx->h_sc;
     HBK_TRY(hbk_fused_init(&s->A->k, &s->v, &s->sh, s->d_b, seed, s->p.tol, st));
     /* switching flag lives in the device scalars */
     int sw = s->p.switching ? 1 : 0;
     CUDA_TRY(cudaMemcpyAsync(&s->d_sc->switching, &sw, sizeof(int), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     *launches += 6 + (s->v.deferred ? 1 : s->m);
+    return HBICG_OK;
+}
+
+static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, double *flush_ms) {
+    cudaStream_t st = s->ctx->stream;
+    hbk_scalars *h = s->ctx->h_sc;
+    int rc0 = fused_init(s, seed, launches);
+    if (rc0) return rc0;
     const int use_graph = s->p.use_graph;
     /* every launch of a chunk advances k by chunk unless the solve ends or
      * the basis pauses it; bound the host loop all the same */
@@ -915,8 +925,26 @@ static void run_host_free(run_host_t *hb) {
     memset(hb, 0, sizeof *hb);
 }
 
-static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma, int seed, int in_where, double *x,
-                           double *r_out, int out_where, hbicg_stats *stats, touch_t *touch, run_host_t *hb);
+/* One solve in three steps: run_begin (inputs, host scratch, set-up),
+ * the iterations, run_end (corrections, outputs, statistics).  A batch runs
+ * the iterations of many solves in one launch between the steps
+ * (hbicg__group_solve). */
+typedef struct {
+    int seed, in_where, out_where;
+    double *x, *r_out;
+    hbicg_stats *stats;
+    touch_t touch;
+    run_host_t hb;
+    int k, n_sw, final_seed, status, launches, flushes;
+    double flush_ms;
+    const double *r_final;
+    double shared_ms; /* >= 0: the iterations ran in a launch shared with other solves, this long */
+} run_t;
+
+static void run_release(hbicg_solver *s, run_t *r);
+static int run_begin(hbicg_solver *s, const double *b, const double *sigma, run_t *r);
+static int run_iterate(hbicg_solver *s, run_t *r);
+static int run_end(hbicg_solver *s, run_t *r, int rc);
 
 /* params.refine: true residuals of every shift; a shift above tol gets
  * x_j += e with (A + sigma_j I) e = b - (A + sigma_j I) x_j solved (single
@@ -979,28 +1007,45 @@ out:
     return rc;
 }
 
-/* the page-touching helper is joined, and the host scratch freed, on every
- * return path of the solve */
+static void run_init(run_t *r, int seed, int in_where, double *x, double *r_out, int out_where, hbicg_stats *stats) {
+    memset(r, 0, sizeof *r);
+    r->seed = seed;
+    r->in_where = in_where;
+    r->x = x;
+    r->r_out = r_out;
+    r->out_where = out_where;
+    r->stats = stats;
+    r->shared_ms = -1.0;
+}
+
 int hbicg_solver_run(hbicg_solver *s, const double *b, const double *sigma, int seed, int in_where, double *x,
                      double *r_out, int out_where, hbicg_stats *stats) {
-    touch_t touch;
-    memset(&touch, 0, sizeof touch);
-    run_host_t hb;
-    memset(&hb, 0, sizeof hb);
-    const int rc = solver_run_impl(s, b, sigma, seed, in_where, x, r_out, out_where, stats, &touch, &hb);
-    touch_join(&touch);
-    run_host_free(&hb);
+    run_t r;
+    run_init(&r, seed, in_where, x, r_out, out_where, stats);
+    int rc = run_begin(s, b, sigma, &r);
+    if (rc == HBICG_OK) rc = run_end(s, &r, run_iterate(s, &r));
+    run_release(s, &r);
+    return rc;
+}
+
+/* the page-touching helper is joined, and the host scratch freed, on every
+ * return path of the solve */
+static void run_release(hbicg_solver *s, run_t *r) {
+    touch_join(&r->touch);
+    run_host_free(&r->hb);
     /* no copy into the caller's buffer outlives the call, whatever path returned */
     if (s->early_pending) cudaStreamSynchronize(s->ctx->cstream);
     s->early_x = NULL;
     s->early_pending = 0;
     free(s->early);
     s->early = NULL;
-    return rc;
 }
 
-static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma, int seed, int in_where, double *x,
-                           double *r_out, int out_where, hbicg_stats *stats, touch_t *touch, run_host_t *hb) {
+static int run_begin(hbicg_solver *s, const double *b, const double *sigma, run_t *r) {
+    const int seed = r->seed, in_where = r->in_where, out_where = r->out_where;
+    double *x = r->x, *r_out = r->r_out;
+    touch_t *touch = &r->touch;
+    run_host_t *hb = &r->hb;
     hbicg_context *ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     const unsigned n = s->A->k.n;
@@ -1010,7 +1055,6 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
         return HBICG_E_ARG;
     }
     const enum cudaMemcpyKind kin = in_where == HBICG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    const enum cudaMemcpyKind kout = out_where == HBICG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     double *h_sigma = hb->h_sigma = malloc(sizeof(double) * (m > 0 ? m : 1));
     int *act = hb->act = calloc((size_t)s->kcap + 1, sizeof(int));
     int *sw_k = hb->sw_k = calloc(m > 0 ? m : 1, sizeof(int)), *sw_seed = hb->sw_seed = calloc(m > 0 ? m : 1, sizeof(int));
@@ -1055,11 +1099,40 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
     if (s->p.form != HBICG_FORM_PLAIN && s->v.deferred && x_pinned && (s->early = calloc((size_t)m, 1)) != NULL)
         s->early_x = x;
     CUDA_TRY(cudaEventRecord(ctx->ev0, st));
-    int rc = HBICG_OK, launches = 0, flushes = 0;
-    double flush_ms = 0.0;
     s->flush_bytes = 0.0;
-    int k = 1, n_sw = 0, final_seed = seed, status = HBICG_OK;
-    const double *r_final = NULL;
+    r->k = 1;
+    r->final_seed = seed;
+    r->status = HBICG_OK;
+    return HBICG_OK;
+}
+
+/* after the fused iterations: scalars in the context's host copy (h_sc) */
+static int fused_collect(hbicg_solver *s, run_t *r) {
+    cudaStream_t st = s->ctx->stream;
+    const int m = s->m;
+    hbk_scalars *h = s->ctx->h_sc;
+    r->k = h->k;
+    r->n_sw = h->n_sw;
+    r->final_seed = h->seed;
+    if (h->status & (HBK_ST_BREAKDOWN | HBK_ST_SHIFT_FAIL)) r->status = HBICG_E_BREAKDOWN;
+    if (m > 0) {
+        CUDA_TRY(cudaMemcpyAsync(r->hb.conv, s->sh.conv_k, sizeof(int) * m, cudaMemcpyDeviceToHost, st));
+        int nl = r->n_sw < m ? r->n_sw : m;
+        if (nl) {
+            CUDA_TRY(cudaMemcpyAsync(r->hb.sw_k, s->sh.sw_k, sizeof(int) * nl, cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(cudaMemcpyAsync(r->hb.sw_seed, s->sh.sw_seed, sizeof(int) * nl, cudaMemcpyDeviceToHost, st));
+        }
+    }
+    CUDA_TRY(cudaMemcpyAsync(r->hb.act, s->sh.act_hist, sizeof(int) * ((size_t)s->kcap + 1), cudaMemcpyDeviceToHost, st));
+    r->r_final = s->v.deferred ? s->v.V + (size_t)h->slot_r_old * s->ld : s->v.rbuf[(h->k - 1) & 1];
+    return HBICG_OK;
+}
+
+static int run_iterate(hbicg_solver *s, run_t *r) {
+    const int seed = r->seed;
+    int *act = r->hb.act, *sw_k = r->hb.sw_k, *sw_seed = r->hb.sw_seed, *conv = r->hb.conv;
+    const double *h_sigma = r->hb.h_sigma;
+    int rc = HBICG_OK;
     if (s->p.form == HBICG_FORM_PLAIN) {
         plain_out o;
         memset(&o, 0, sizeof o);
@@ -1068,35 +1141,38 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
         o.conv_k = conv;
         o.act = act;
         rc = run_plain(s, h_sigma, seed, &o);
-        k = o.k;
-        n_sw = o.n_sw;
-        final_seed = o.final_seed;
-        launches = o.launches;
+        r->k = o.k;
+        r->n_sw = o.n_sw;
+        r->final_seed = o.final_seed;
+        r->launches = o.launches;
         if (rc == HBICG_E_BREAKDOWN) {
-            status = rc;
+            r->status = rc;
             rc = HBICG_OK;
         }
-        r_final = s->d_r;
+        r->r_final = s->d_r;
     } else {
-        rc = run_fused(s, seed, &launches, &flushes, &flush_ms);
-        if (rc == HBICG_OK) {
-            hbk_scalars *h = ctx->h_sc;
-            k = h->k;
-            n_sw = h->n_sw;
-            final_seed = h->seed;
-            if (h->status & (HBK_ST_BREAKDOWN | HBK_ST_SHIFT_FAIL)) status = HBICG_E_BREAKDOWN;
-            if (m > 0) {
-                CUDA_TRY(cudaMemcpyAsync(conv, s->sh.conv_k, sizeof(int) * m, cudaMemcpyDeviceToHost, st));
-                int nl = n_sw < m ? n_sw : m;
-                if (nl) {
-                    CUDA_TRY(cudaMemcpyAsync(sw_k, s->sh.sw_k, sizeof(int) * nl, cudaMemcpyDeviceToHost, st));
-                    CUDA_TRY(cudaMemcpyAsync(sw_seed, s->sh.sw_seed, sizeof(int) * nl, cudaMemcpyDeviceToHost, st));
-                }
-            }
-            CUDA_TRY(cudaMemcpyAsync(act, s->sh.act_hist, sizeof(int) * ((size_t)s->kcap + 1), cudaMemcpyDeviceToHost, st));
-            r_final = s->v.deferred ? s->v.V + (size_t)h->slot_r_old * s->ld : s->v.rbuf[(h->k - 1) & 1];
-        }
+        rc = run_fused(s, seed, &r->launches, &r->flushes, &r->flush_ms);
+        if (rc == HBICG_OK) rc = fused_collect(s, r);
     }
+    return rc;
+}
+
+static int run_end(hbicg_solver *s, run_t *r, int rc) {
+    hbicg_context *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    const unsigned n = s->A->k.n;
+    const int m = s->m;
+    const int out_where = r->out_where;
+    double *x = r->x, *r_out = r->r_out;
+    hbicg_stats *stats = r->stats;
+    touch_t *touch = &r->touch;
+    run_host_t *hb = &r->hb;
+    int *act = hb->act, *sw_k = hb->sw_k, *sw_seed = hb->sw_seed, *conv = hb->conv;
+    const double *h_sigma = hb->h_sigma;
+    const enum cudaMemcpyKind kout = out_where == HBICG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const int k = r->k, n_sw = r->n_sw, final_seed = r->final_seed;
+    int status = r->status;
+    const double *r_final = r->r_final;
     CUDA_TRY(cudaEventRecord(ctx->ev1, st));
     /* copies issued during the solve finish before anything rewrites X */
     if (s->early_pending) CUDA_TRY(cudaStreamSynchronize(ctx->cstream));
@@ -1151,17 +1227,18 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
     }
     if (stats) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        if (r->shared_ms >= 0.0) ms = (float)r->shared_ms;
+        else cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
         stats->k = k;
         stats->status = rc ? rc : status;
         stats->n_switches = n_sw;
         stats->final_seed = final_seed;
         stats->shift_mode = s->mode;
-        stats->basis_flushes = flushes;
-        stats->launches = launches;
+        stats->basis_flushes = r->flushes;
+        stats->launches = r->launches;
         stats->refined_shifts = refined;
         stats->solve_ms = ms;
-        stats->flush_ms = flush_ms;
+        stats->flush_ms = r->flush_ms;
         stats->max_true_residual = maxres;
         stats->bytes_algorithmic = algorithmic_bytes(s, k, act);
         stats->flush_bytes = s->flush_bytes;
@@ -1181,6 +1258,106 @@ static int solver_run_impl(hbicg_solver *s, const double *b, const double *sigma
     }
     if (rc) return rc;
     return status;
+}
+
+/* ------------------------------------------------------------------------ */
+/* many solves, one launch */
+
+int hbicg__group_eligible(const hbicg_solver *s) {
+    return s && s->p.form == HBICG_FORM_FUSED && s->mode == HBICG_SHIFTS_INCREMENTAL && !s->v.deferred &&
+           s->A->k.fmt == HBK_FMT_SELL && s->m > 0;
+}
+
+/* Solves of nf families whose iterations run in one persistent launch
+ * (hbk_group_run): every solver made on the same context, each eligible
+ * (hbicg__group_eligible); host inputs b[f], sigma[f] and outputs x[f] as
+ * hbicg_solver_run takes them.  Each solve's set-up (run_begin and the fused
+ * initialisation) runs first, then the one launch, then each solve's
+ * corrections, outputs and statistics (run_end).  st[f].solve_ms is the
+ * shared launch's time and st[f].launches counts it once.  rc[f]: the status
+ * hbicg_solver_run would return. */
+int hbicg__group_solve(hbicg_solver **S, int nf, const double *const *b, const double *const *sigma, const int *seed,
+                       double *const *x, hbicg_stats *st, int *rc, int max_ctas) {
+    if (nf <= 0) return HBICG_OK;
+    hbicg_context *ctx = S[0]->ctx;
+    cudaStream_t stream = ctx->stream;
+    run_t *R = calloc((size_t)nf, sizeof(run_t));
+    int *in = calloc((size_t)nf, sizeof(int));
+    hbk_matrix *A = calloc((size_t)nf, sizeof(hbk_matrix));
+    hbk_vectors *V = calloc((size_t)nf, sizeof(hbk_vectors));
+    hbk_shifts *H = calloc((size_t)nf, sizeof(hbk_shifts));
+    void *ws = NULL;
+    cudaEvent_t e0 = NULL, e1 = NULL;
+    int grc = HBICG_OK, ng = 0, cap = 0, err = 0;
+    if (!R || !in || !A || !V || !H) {
+        grc = HBICG_E_NOMEM;
+        goto out;
+    }
+    for (int f = 0; f < nf; ++f) {
+        run_init(&R[f], seed[f], HBICG_HOST, x[f], NULL, HBICG_HOST, st ? &st[f] : NULL);
+        if (!hbicg__group_eligible(S[f]) || S[f]->ctx != ctx) {
+            rc[f] = HBICG_E_ARG;
+            set_msg("family %d cannot join the shared launch", f);
+            continue;
+        }
+        rc[f] = run_begin(S[f], b[f], sigma[f], &R[f]);
+        if (rc[f] == HBICG_OK) rc[f] = fused_init(S[f], seed[f], &R[f].launches);
+        if (rc[f] != HBICG_OK) continue;
+        in[f] = 1;
+        A[ng] = S[f]->A->k;
+        V[ng] = S[f]->v;
+        H[ng] = S[f]->sh;
+        if (S[f]->kcap > cap) cap = S[f]->kcap;
+        ++ng;
+    }
+    if (ng) {
+        const size_t bytes = hbk_group_ws_bytes(ng, V);
+        float ms = 0.f;
+        int lrc = HBICG_OK;
+        if (pool_alloc(&ws, bytes, stream) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+            cudaEventCreate(&e1) != cudaSuccess) {
+            lrc = HBICG_E_NOMEM;
+        } else {
+            cudaEventRecord(e0, stream);
+            const int e = hbk_group_run(ng, A, V, H, cap, max_ctas, ws, bytes, &err, stream);
+            cudaEventRecord(e1, stream);
+            if (e || cudaStreamSynchronize(stream) != cudaSuccess) {
+                set_msg("shared launch: %s", hbk_error_string(e ? e : (int)cudaGetLastError()));
+                lrc = HBICG_E_CUDA;
+            } else if (err) {
+                set_msg("shared launch: %s", err == HBK_GROUP_ERR_WAIT ? "a grid barrier's wait timed out"
+                                                                        : "the iteration cap was reached");
+                lrc = HBICG_E_TIMEOUT;
+            }
+            cudaEventElapsedTime(&ms, e0, e1);
+        }
+        for (int f = 0; f < nf; ++f) {
+            if (!in[f]) continue;
+            int r = lrc;
+            if (r == HBICG_OK) {
+                cudaError_t ce = cudaMemcpyAsync(ctx->h_sc, S[f]->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost,
+                                                 stream);
+                if (!ce) ce = cudaStreamSynchronize(stream);
+                r = ce ? HBICG_E_CUDA : fused_collect(S[f], &R[f]);
+            }
+            R[f].launches += 1;
+            R[f].shared_ms = ms;
+            rc[f] = run_end(S[f], &R[f], r);
+        }
+    }
+out:
+    if (R)
+        for (int f = 0; f < nf; ++f) run_release(S[f], &R[f]);
+    if (ws) hbicg__dev_free(ws, stream);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamSynchronize(stream);
+    free(R);
+    free(in);
+    free(A);
+    free(V);
+    free(H);
+    return grc;
 }
 
 int hbicg_solve(unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *col, const double *val,

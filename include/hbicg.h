@@ -133,10 +133,11 @@ int hbicg_matrix_time_spmv(hbicg_matrix *A, const double *x, double *y, double s
  * SELL-32, slices of 32 consecutive rows padded to their longest row (rows of
  * at most 64 entries, padding under a third of the nonzeros); HYB, rows of
  * at most 32 entries in SELL-32 slices sorted by length inside windows of 256
- * rows and longer rows one warp each; or MERGE, rows of at most 192 entries in
- * blocks of 1536 row ends + nonzeros split evenly among 256 threads along the
- * merge path (nonzero-balanced, no copy of the values), longer rows one warp
- * each.  A new matrix takes SELL-32 where it qualifies, else MERGE. */
+ * rows and longer rows one warp each; or MERGE, rows of at most 255 entries in
+ * blocks of at most 256 row ends + nonzeros, one warp per block, split evenly
+ * among its 32 lanes along the merge path (nonzero-balanced, no copy of the
+ * values), longer rows one warp each.  A new matrix takes SELL-32 where it
+ * qualifies, else HYB; the autotuner picks among all four. */
 typedef enum { HBICG_SPMV_TILE = 0, HBICG_SPMV_SELL = 1, HBICG_SPMV_HYB = 2, HBICG_SPMV_MERGE = 3 } hbicg_spmv_format;
 int hbicg_matrix_format(const hbicg_matrix *A);
 /* Switch the SpMV form (builds that form's copy if needed; HBICG_E_ARG when a
@@ -238,6 +239,20 @@ typedef struct {
 } hbicg_family;
 int hbicg_batch_solve(hbicg_family *fams, int count, const hbicg_params *p, int workers, const char *autotune_cache,
                       double *wall_ms);
+/* The same with every option.  persistent = 1 (the default of
+ * hbicg_batch_solve too): the families that take the incremental shift mode
+ * (n m < 2^21 with shift_mode AUTO; no autotune, no residual output) run all
+ * their iterations in one persistent launch on the GPU, set up and finished
+ * by one host thread, while the workers take the other families. */
+typedef struct {
+    int workers;                /* host workers for the other families (default 8) */
+    int persistent;             /* default 1 */
+    int persistent_ctas;        /* CTAs of the persistent launch; 0 = one wave of the GPU */
+    const char *autotune_cache; /* as in hbicg_batch_solve */
+} hbicg_batch_opts;
+void hbicg_batch_opts_default(hbicg_batch_opts *o);
+int hbicg_batch_solve_opts(hbicg_family *fams, int count, const hbicg_params *p, const hbicg_batch_opts *opts,
+                           double *wall_ms);
 
 /* Adjoint (no counterpart in the reference, which only solves forward).
  * A^T as a new matrix on A's context, built on the GPU (stable by column). */

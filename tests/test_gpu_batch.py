@@ -15,9 +15,21 @@ def _families(pkg, count=10, seed=0):
     return pkg.workloads.batched_families(count, n_lo=500, n_hi=6000, seed=seed)
 
 
+def _k_envelope(oracle, f, tol, max_iter, samples=16):
+    """Iteration counts of the oracle (the reference's algorithm) on b and on
+    b perturbed by 1e-14 relative noise: on families whose residual creeps
+    along the tolerance at the end, the stopping iteration moves with the
+    last bits of the arithmetic (family 61 of the 256-family batch stops
+    anywhere in 61..69 over 40 such draws)."""
+    return [oracle.solve(f.a, f.b if t == 0 else f.b * (1 + 1e-14 * np.random.default_rng(t).standard_normal(f.a.n)),
+                         f.sigma, seed=f.seed, tol=tol, max_iter=max_iter).k for t in range(samples)]
+
+
 def test_batch_equals_individual_solves(cuda, pkg):
+    """Through the workers (no shared launch): each family's solve is the one
+    it gets alone, bit for bit."""
     fams = _families(pkg)
-    res, wall = pkg.batch_solve(fams, workers=4, tol=1e-10, max_iter=10000, true_residuals=True)
+    res, wall = pkg.batch_solve(fams, workers=4, tol=1e-10, max_iter=10000, true_residuals=True, persistent=False)
     assert wall > 0
     for f, r in zip(fams, res):
         one = pkg.solve(f.a, f.b, f.sigma, seed=f.seed, tol=1e-10, max_iter=10000)
@@ -25,14 +37,71 @@ def test_batch_equals_individual_solves(cuda, pkg):
         assert np.array_equal(r.x, one.x)  # same kernels, same order: bit for bit
 
 
-def test_batch_failure_stays_with_its_family(cuda, pkg):
+@pytest.mark.parametrize("persistent", [False, True])
+def test_batch_failure_stays_with_its_family(cuda, pkg, persistent):
     fams = _families(pkg, count=4, seed=1)
     bad = fams[2]
     bad.seed = len(bad.sigma) + 3  # out of range
-    res, _ = pkg.batch_solve(fams, workers=3, tol=1e-10, max_iter=10000)
+    res, _ = pkg.batch_solve(fams, workers=3, tol=1e-10, max_iter=10000, persistent=persistent)
     assert res[2].status != 0
     for i in (0, 1, 3):
         assert res[i].status == 0 and res[i].k > 1
+
+
+def test_persistent_launch_against_the_oracle(cuda, pkg, oracle):
+    """Small uneven families (n 500..6000, 2-D and 3-D stencils, 8..64
+    shifts) whose iterations all run in one persistent launch, against the
+    oracle (the reference's algorithm) on the same inputs: every x_j within
+    1e-8 relative, k within 2 % of the oracle's rounding envelope (the oracle
+    on b perturbed by 1e-14: the last iterations sit on a plateau where the
+    stopping iteration moves with the dot products' summation order), the
+    same switch count, every shift's true residual at tol or within 1.5x the
+    reference's own; and against the same families through the workers (one
+    solve per family): x within 1e-8."""
+    fams = _families(pkg, count=12, seed=4)
+    kw = dict(tol=1e-10, max_iter=10000, true_residuals=True, refine=False)
+    res, _ = pkg.batch_solve(fams, workers=4, persistent=True, **kw)
+    alone, _ = pkg.batch_solve(fams, workers=4, persistent=False, **kw)
+    for f, r, a in zip(fams, res, alone):
+        assert r.status == 0, (f.name, r.status)
+        want = oracle.solve(f.a, f.b, f.sigma, seed=f.seed, tol=1e-10, max_iter=10000)
+        scale = np.max(np.abs(want.x))
+        assert np.max(np.abs(r.x - want.x)) < 1e-8 * scale, f.name
+        ks = _k_envelope(oracle, f, 1e-10, 10000)
+        lo, hi = min(ks), max(ks)
+        assert lo - max(1, int(0.02 * lo)) <= r.k <= hi + max(1, int(0.02 * hi)), (f.name, r.k, ks)
+        assert r.switches == len(want.switches)
+        tr_ref = oracle.true_residuals(f.a, want.x, f.b, f.sigma)
+        assert np.all(r.true_residual <= np.maximum(1e-10 * 1.02, 1.5 * tr_ref)), (f.name, r.max_true_residual)
+        assert np.max(np.abs(r.x - a.x)) < 1e-8 * scale
+
+
+def test_persistent_launch_with_switches_and_max_iter(cuda, pkg, oracle):
+    """Families that switch seeds and families stopped by max_iter in the
+    same persistent launch: the switch sequence and k of the oracle on
+    families with several switches (the golden stencil with two switches and
+    a seed other than 0), and max_iter reached exactly (the reference's k and
+    x after max_iter iterations) while the other families run on."""
+    import conftest
+
+    g = conftest.golden("stencil2d_two_switches")
+    fams = _families(pkg, count=3, seed=6)
+    sw = pkg.workloads.Family("sw", conftest.GoldenCsr(g), g["b"], g["sigma"], int(g["seed"]), float(g["tol"]),
+                              int(g["max_iter"]), {})
+    capped = _families(pkg, count=1, seed=7)[0]
+    fams = [sw] + fams
+    res, _ = pkg.batch_solve(fams, workers=2, persistent=True, tol=float(g["tol"]), max_iter=int(g["max_iter"]),
+                             refine=False)
+    k_ref = int(g["k"])
+    assert res[0].status == 0 and res[0].switches == len(g["switches"]), (res[0].status, res[0].switches)
+    assert abs(res[0].k - k_ref) <= max(1, int(0.02 * k_ref)), (res[0].k, k_ref)
+    assert np.max(np.abs(res[0].x - g["x"])) < 1e-8 * np.max(np.abs(g["x"]))
+    for r in res[1:]:
+        assert r.status == 0
+    r5, _ = pkg.batch_solve([capped] + fams[1:], workers=2, persistent=True, tol=1e-10, max_iter=5, refine=False)
+    want = oracle.solve(capped.a, capped.b, capped.sigma, seed=capped.seed, tol=1e-10, max_iter=5)
+    assert r5[0].status == 4 and r5[0].k == want.k == 6
+    assert np.max(np.abs(r5[0].x - want.x)) < 1e-8 * np.max(np.abs(want.x))
 
 
 def test_autotune_cache_written_once_and_reused(cuda, pkg, tmp_path):
@@ -117,11 +186,12 @@ def test_manifest_runner_end_to_end(cuda, pkg, tmp_path):
 
 def test_config4_families_against_the_oracle(cuda, pkg, oracle):
     """Families of the 256-family batch itself (the eight smallest, 2-D and
-    3-D stencils with 8..64 shifts), solved together by the batch and each
-    checked against the oracle (the reference's algorithm) on the same inputs:
-    every x_j within 1e-8 relative, k within 2 % or the oracle's rounding
-    envelope, every shift's true residual at tol or within 1.5x the
-    reference's own (no true-residual correction: the reference's x)."""
+    3-D stencils with 8..64 shifts), solved together by the batch (in its one
+    persistent launch: they take the incremental shift mode) and each checked
+    against the oracle (the reference's algorithm) on the same inputs: every
+    x_j within 1e-8 relative, k within 2 % of the oracle's rounding envelope,
+    every shift's true residual at tol or within 1.5x the reference's own (no
+    true-residual correction: the reference's x)."""
     fams = pkg.workloads.batched_families(256)
     small = sorted(range(256), key=lambda i: fams[i].a.n)[:8]
     sel = [fams[i] for i in small]
@@ -131,8 +201,7 @@ def test_config4_families_against_the_oracle(cuda, pkg, oracle):
         want = oracle.solve(f.a, f.b, f.sigma, seed=f.seed, tol=f.tol, max_iter=f.max_iter)
         err = np.max(np.abs(r.x - want.x)) / np.max(np.abs(want.x))
         assert err < 1e-8, (f.name, err)
-        ks = [want.k] + [oracle.solve(f.a, f.b * (1 + 1e-14 * np.random.default_rng(t).standard_normal(f.a.n)),
-                                      f.sigma, seed=f.seed, tol=f.tol, max_iter=f.max_iter).k for t in (1, 2, 3)]
+        ks = _k_envelope(oracle, f, f.tol, f.max_iter)
         assert min(ks) - max(1, int(0.02 * min(ks))) <= r.k <= max(ks) + max(1, int(0.02 * max(ks))), (f.name, r.k, ks)
         tr = oracle.true_residuals(f.a, r.x, f.b, f.sigma)
         tr_ref = oracle.true_residuals(f.a, want.x, f.b, f.sigma)
