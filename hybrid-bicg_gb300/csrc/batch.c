@@ -75,82 +75,98 @@ static void family_stats(hbicg_family *f, const hbicg_stats *st) {
     f->max_true_residual = st->max_true_residual;
 }
 
-/* families of one persistent launch (see the file comment) */
+/* Families of one persistent launch (see the file comment).  Up to
+ * GROUP_THREADS host threads, each with its own high-priority context, take
+ * the families from a shared index and set them up (matrix, solver, the
+ * solve's first step: hbicg__group_add); once all have, thread 0 signals the
+ * batch (which then starts its workers) and runs the one launch; then every
+ * thread finishes its own families (hbicg__group_finish). */
+#define GROUP_THREADS 4
 typedef struct {
     hbicg_family *fams;
     const int *idx;
     int count;
     const hbicg_params *p;
-    int ctas;
+    hbicg__group *g;
+    int next;              /* shared index (atomic) */
+    int nthreads;          /* threads taking part (lowered when one fails to start) */
+    int arrived[2];        /* threads at each of the two meeting points */
+    int setup_done;
+    pthread_mutex_t m;
+    pthread_cond_t cv;
+    int *slot;             /* [count] slot in g, -1: solved on its own */
+    hbicg_stats *st;       /* [count] */
+    hbicg_matrix **A;      /* [count] */
+    hbicg_solver **S;      /* [count] */
 } group_t;
 
-static void *group_run(void *arg) {
-    group_t *g = arg;
+typedef struct {
+    group_t *G;
+    int tid;
+} part_t;
+
+static void meet(group_t *G, int point) {
+    pthread_mutex_lock(&G->m);
+    G->arrived[point]++;
+    pthread_cond_broadcast(&G->cv);
+    while (G->arrived[point] < G->nthreads) pthread_cond_wait(&G->cv, &G->m);
+    pthread_mutex_unlock(&G->m);
+}
+
+static void *group_part(void *arg) {
+    part_t *pa = arg;
+    group_t *G = pa->G;
     const double t0 = now_ms();
-    const int n = g->count;
     hbicg_context *ctx = NULL;
-    int crc = hbicg_context_create(&ctx);
-    hbicg_matrix **A = calloc((size_t)n, sizeof *A);
-    hbicg_solver **S = calloc((size_t)n, sizeof *S), **GS = calloc((size_t)n, sizeof *GS);
-    const double **B = calloc((size_t)n, sizeof *B), **SG = calloc((size_t)n, sizeof *SG);
-    double **X = calloc((size_t)n, sizeof *X);
-    int *seed = calloc((size_t)n, sizeof *seed), *rc = calloc((size_t)n, sizeof *rc), *who = calloc((size_t)n, sizeof *who);
-    hbicg_stats *ST = calloc((size_t)n, sizeof *ST);
-    if (!A || !S || !GS || !B || !SG || !X || !seed || !rc || !who || !ST) crc = HBICG_E_NOMEM;
-    int ng = 0;
-    for (int i = 0; i < n; ++i) {
-        hbicg_family *f = &g->fams[g->idx[i]];
-        if (crc != HBICG_OK) {
-            f->status = crc;
+    const int crc = hbicg__context_create_prio(&ctx, 1);
+    int *mine = malloc(sizeof(int) * (size_t)(G->count > 0 ? G->count : 1)), nm = 0;
+    for (;;) {
+        const int i = __atomic_fetch_add(&G->next, 1, __ATOMIC_RELAXED);
+        if (i >= G->count) break;
+        hbicg_family *f = &G->fams[G->idx[i]];
+        G->slot[i] = -1;
+        if (crc != HBICG_OK || !mine) {
+            f->status = crc != HBICG_OK ? crc : HBICG_E_NOMEM;
             continue;
         }
-        f->status = hbicg_matrix_create(ctx, f->n, f->nnz, f->ptr, f->col, f->val, HBICG_HOST, &A[i]);
+        mine[nm++] = i;
+        f->status = hbicg_matrix_create(ctx, f->n, f->nnz, f->ptr, f->col, f->val, HBICG_HOST, &G->A[i]);
         if (f->status == HBICG_OK) {
-            f->spmv_format = hbicg_matrix_format(A[i]);
-            f->status = hbicg_solver_create(ctx, A[i], f->m, g->p, &S[i]);
+            f->spmv_format = hbicg_matrix_format(G->A[i]);
+            f->status = hbicg_solver_create(ctx, G->A[i], f->m, G->p, &G->S[i]);
         }
         if (f->status != HBICG_OK) continue;
-        if (hbicg__group_eligible(S[i])) {
-            GS[ng] = S[i];
-            B[ng] = f->b;
-            SG[ng] = f->sigma;
-            X[ng] = f->x;
-            seed[ng] = f->seed;
-            ST[ng].true_residual = f->true_residual;
-            who[ng++] = g->idx[i];
+        G->st[i].true_residual = f->true_residual;
+        if (hbicg__group_eligible(G->S[i])) {
+            G->slot[i] = hbicg__group_add(G->g, G->S[i], f->b, f->sigma, f->seed, f->x, &G->st[i]);
         } else { /* another form after all (e.g. rows too long for SELL-32): a solve of its own */
-            hbicg_stats st;
-            memset(&st, 0, sizeof st);
-            st.true_residual = f->true_residual;
-            f->status = hbicg_solver_run(S[i], f->b, f->sigma, f->seed, HBICG_HOST, f->x, f->r, HBICG_HOST, &st);
-            family_stats(f, &st);
+            f->status = hbicg_solver_run(G->S[i], f->b, f->sigma, f->seed, HBICG_HOST, f->x, f->r, HBICG_HOST,
+                                         &G->st[i]);
+            family_stats(f, &G->st[i]);
         }
     }
-    if (ng) {
-        const int grc = hbicg__group_solve(GS, ng, B, SG, seed, X, ST, rc, g->ctas);
-        for (int q = 0; q < ng; ++q) {
-            hbicg_family *f = &g->fams[who[q]];
-            f->status = grc != HBICG_OK ? grc : rc[q];
-            family_stats(f, &ST[q]);
-        }
+    meet(G, 0);
+    if (pa->tid == 0) {
+        pthread_mutex_lock(&G->m);
+        G->setup_done = 1;
+        pthread_cond_broadcast(&G->cv);
+        pthread_mutex_unlock(&G->m);
+        hbicg__group_launch(G->g);
     }
-    for (int i = 0; i < n && S && A; ++i) {
-        hbicg_solver_destroy(S[i]);
-        hbicg_matrix_destroy(A[i]);
+    meet(G, 1);
+    for (int q = 0; q < nm; ++q) {
+        const int i = mine[q];
+        hbicg_family *f = &G->fams[G->idx[i]];
+        if (G->slot[i] >= 0) {
+            f->status = hbicg__group_finish(G->g, G->slot[i]);
+            family_stats(f, &G->st[i]);
+        }
+        hbicg_solver_destroy(G->S[i]);
+        hbicg_matrix_destroy(G->A[i]);
+        f->wall_ms = now_ms() - t0;
     }
     if (ctx) hbicg_context_destroy(ctx);
-    const double wall = now_ms() - t0;
-    for (int i = 0; i < n; ++i) g->fams[g->idx[i]].wall_ms = wall;
-    free(A);
-    free(S);
-    free(GS);
-    free(B);
-    free(SG);
-    free(X);
-    free(seed);
-    free(rc);
-    free(who);
-    free(ST);
+    free(mine);
     return NULL;
 }
 
@@ -232,12 +248,53 @@ int hbicg_batch_solve_opts(hbicg_family *fams, int count, const hbicg_params *p,
         else order[nw++] = order[i];
     }
     count = nw;
-    group_t gr = {fams, grp, ng, p, opts->persistent_ctas};
-    pthread_t gth;
+    group_t G;
+    memset(&G, 0, sizeof G);
+    part_t parts[GROUP_THREADS];
+    pthread_t gth[GROUP_THREADS];
     int g_started = 0;
     if (ng) {
-        if (pthread_create(&gth, NULL, group_run, &gr) == 0) g_started = 1;
-        else group_run(&gr);
+        G.fams = fams;
+        G.idx = grp;
+        G.count = ng;
+        G.p = p;
+        G.g = hbicg__group_new(ng, opts->persistent_ctas);
+        G.slot = malloc(sizeof(int) * (size_t)ng);
+        G.st = calloc((size_t)ng, sizeof(hbicg_stats));
+        G.A = calloc((size_t)ng, sizeof(hbicg_matrix *));
+        G.S = calloc((size_t)ng, sizeof(hbicg_solver *));
+        pthread_mutex_init(&G.m, NULL);
+        pthread_cond_init(&G.cv, NULL);
+        if (!G.g || !G.slot || !G.st || !G.A || !G.S) { /* no shared launch: the workers take them */
+            for (int i = 0; i < ng; i++) order[nw++] = grp[i];
+            count = nw;
+            ng = 0;
+        } else {
+            const int want = ng < GROUP_THREADS ? ng : GROUP_THREADS;
+            G.nthreads = want;
+            for (int t = 0; t < want; t++) {
+                parts[t].G = &G;
+                parts[t].tid = g_started;
+                if (pthread_create(&gth[g_started], NULL, group_part, &parts[t]) == 0) {
+                    g_started++;
+                } else {
+                    pthread_mutex_lock(&G.m);
+                    G.nthreads--;
+                    pthread_cond_broadcast(&G.cv);
+                    pthread_mutex_unlock(&G.m);
+                }
+            }
+            if (!g_started) { /* no thread: the whole group here, before the workers */
+                G.nthreads = 1;
+                parts[0].G = &G;
+                parts[0].tid = 0;
+                group_part(&parts[0]);
+            } else { /* the workers start once the group is set up (its many short steps then run on an idle GPU) */
+                pthread_mutex_lock(&G.m);
+                while (!G.setup_done) pthread_cond_wait(&G.cv, &G.m);
+                pthread_mutex_unlock(&G.m);
+            }
+        }
     }
     if (workers < 1) workers = 8;
     if (workers > count) workers = count > 0 ? count : 1;
@@ -251,7 +308,16 @@ int hbicg_batch_solve_opts(hbicg_family *fams, int count, const hbicg_params *p,
     }
     if (!started && count) worker(&b); /* no threads: run in the caller */
     for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
-    if (g_started) pthread_join(gth, NULL);
+    for (int t = 0; t < g_started; t++) pthread_join(gth[t], NULL);
+    if (G.g) hbicg__group_free(G.g);
+    if (G.count) {
+        pthread_mutex_destroy(&G.m);
+        pthread_cond_destroy(&G.cv);
+    }
+    free(G.slot);
+    free(G.st);
+    free(G.A);
+    free(G.S);
     count = nw + ng;
     free(order);
     free(grp);

@@ -64,9 +64,17 @@ void hbicg__dev_free(void *p, cudaStream_t st);
 /* the shift mode a solver made with p takes for n rows and m shifts */
 int hbicg__shift_mode_for(const hbicg_params *p, unsigned n, int m);
 /* many families' iterations in one persistent launch (solver.c) */
+typedef struct hbicg__group hbicg__group;
 int hbicg__group_eligible(const hbicg_solver *s);
-int hbicg__group_solve(hbicg_solver **S, int nf, const double *const *b, const double *const *sigma, const int *seed,
-                       double *const *x, hbicg_stats *st, int *rc, int max_ctas);
+hbicg__group *hbicg__group_new(int cap, int max_ctas);
+/* a family's first step; returns its slot (its status: hbicg__group_finish) */
+int hbicg__group_add(hbicg__group *g, hbicg_solver *s, const double *b, const double *sigma, int seed, double *x,
+                     hbicg_stats *st);
+int hbicg__group_launch(hbicg__group *g);
+int hbicg__group_finish(hbicg__group *g, int slot);
+void hbicg__group_free(hbicg__group *g);
+/* a context whose stream has the device's greatest priority when high = 1 */
+int hbicg__context_create_prio(hbicg_context **out, int high);
 const hbk_matrix *hbicg__matrix_kernel_view(const hbicg_matrix *A);
 hbicg_context *hbicg__matrix_context(const hbicg_matrix *A);
 /* y (+)= A x for host arrays, on a process-wide context (matrix.h's mult) */

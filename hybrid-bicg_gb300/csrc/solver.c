@@ -92,12 +92,19 @@ void hbicg__ctx_release(hbicg_context *c) {
     if (__atomic_sub_fetch(&c->refs, 1, __ATOMIC_ACQ_REL) == 0) ctx_free(c);
 }
 
-int hbicg_context_create(hbicg_context **out) {
+int hbicg_context_create(hbicg_context **out) { return hbicg__context_create_prio(out, 0); }
+
+/* high = 1: the context's stream at the device's greatest priority, so that
+ * its short steps are scheduled ahead of other streams' pending blocks */
+int hbicg__context_create_prio(hbicg_context **out, int high) {
     hbicg_context *c = calloc(1, sizeof *c);
     if (!c) return HBICG_E_NOMEM;
     c->refs = 1;
-    int rc = HBICG_OK;
-    CUDA_GOTO(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    int rc = HBICG_OK, lo = 0, hi = 0;
+    if (high && cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess)
+        CUDA_GOTO(cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, hi));
+    else
+        CUDA_GOTO(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CUDA_GOTO(cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking));
     CUDA_GOTO(cudaEventCreateWithFlags(&c->cev, cudaEventDisableTiming));
     CUDA_GOTO(cudaEventCreate(&c->ev0));
@@ -1268,96 +1275,155 @@ int hbicg__group_eligible(const hbicg_solver *s) {
            s->A->k.fmt == HBK_FMT_SELL && s->m > 0;
 }
 
-/* Solves of nf families whose iterations run in one persistent launch
- * (hbk_group_run): every solver made on the same context, each eligible
- * (hbicg__group_eligible); host inputs b[f], sigma[f] and outputs x[f] as
- * hbicg_solver_run takes them.  Each solve's set-up (run_begin and the fused
- * initialisation) runs first, then the one launch, then each solve's
- * corrections, outputs and statistics (run_end).  st[f].solve_ms is the
- * shared launch's time and st[f].launches counts it once.  rc[f]: the status
- * hbicg_solver_run would return. */
-int hbicg__group_solve(hbicg_solver **S, int nf, const double *const *b, const double *const *sigma, const int *seed,
-                       double *const *x, hbicg_stats *st, int *rc, int max_ctas) {
-    if (nf <= 0) return HBICG_OK;
-    hbicg_context *ctx = S[0]->ctx;
-    cudaStream_t stream = ctx->stream;
-    run_t *R = calloc((size_t)nf, sizeof(run_t));
-    int *in = calloc((size_t)nf, sizeof(int));
-    hbk_matrix *A = calloc((size_t)nf, sizeof(hbk_matrix));
-    hbk_vectors *V = calloc((size_t)nf, sizeof(hbk_vectors));
-    hbk_shifts *H = calloc((size_t)nf, sizeof(hbk_shifts));
+/* Solves of many families whose iterations run in one persistent launch
+ * (hbk_group_run).  hbicg__group_add does one solve's first step (run_begin
+ * and the fused initialisation, on the solver's own context and stream) and
+ * registers it; hbicg__group_launch runs every registered family's iterations
+ * in one cooperative launch on the group's own high-priority stream and
+ * waits for it; hbicg__group_finish does a family's last step (run_end:
+ * corrections, outputs, statistics) on its own stream.  Adds (and finishes)
+ * of families on different contexts may run on different host threads; a
+ * context's families are finished one after another (they share its pinned
+ * scalars).  stats.solve_ms is the shared launch's time and stats.launches
+ * counts it once. */
+struct hbicg__group {
+    pthread_mutex_t lock;
+    int cap, n, max_ctas, lrc;
+    double ms;
+    cudaStream_t stream;
+    hbicg_solver **S;
+    run_t *R;
+    int *rc, *in;
+};
+
+hbicg__group *hbicg__group_new(int cap, int max_ctas) {
+    hbicg__group *g = calloc(1, sizeof *g);
+    if (!g) return NULL;
+    int lo = 0, hi = 0;
+    g->cap = cap > 0 ? cap : 1;
+    g->max_ctas = max_ctas;
+    g->S = calloc((size_t)g->cap, sizeof *g->S);
+    g->R = calloc((size_t)g->cap, sizeof *g->R);
+    g->rc = calloc((size_t)g->cap, sizeof *g->rc);
+    g->in = calloc((size_t)g->cap, sizeof *g->in);
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (!e) e = cudaStreamCreateWithPriority(&g->stream, cudaStreamNonBlocking, hi);
+    if (!g->S || !g->R || !g->rc || !g->in || e) {
+        if (!e) cudaStreamDestroy(g->stream);
+        free(g->S);
+        free(g->R);
+        free(g->rc);
+        free(g->in);
+        free(g);
+        return NULL;
+    }
+    pthread_mutex_init(&g->lock, NULL);
+    return g;
+}
+
+void hbicg__group_free(hbicg__group *g) {
+    if (!g) return;
+    cudaStreamSynchronize(g->stream);
+    cudaStreamDestroy(g->stream);
+    pthread_mutex_destroy(&g->lock);
+    free(g->S);
+    free(g->R);
+    free(g->rc);
+    free(g->in);
+    free(g);
+}
+
+int hbicg__group_add(hbicg__group *g, hbicg_solver *s, const double *b, const double *sigma, int seed, double *x,
+                     hbicg_stats *st) {
+    pthread_mutex_lock(&g->lock);
+    const int slot = g->n < g->cap ? g->n++ : -1;
+    pthread_mutex_unlock(&g->lock);
+    if (slot < 0) return -1;
+    run_t *r = &g->R[slot];
+    run_init(r, seed, HBICG_HOST, x, NULL, HBICG_HOST, st);
+    g->S[slot] = s;
+    int rc = hbicg__group_eligible(s) ? HBICG_OK : HBICG_E_ARG;
+    if (rc) set_msg("a solver that is not fused, incremental and SELL-32 cannot join the shared launch");
+    if (rc == HBICG_OK) rc = run_begin(s, b, sigma, r);
+    if (rc == HBICG_OK) rc = fused_init(s, seed, &r->launches);
+    g->rc[slot] = rc;
+    g->in[slot] = rc == HBICG_OK;
+    return slot;
+}
+
+int hbicg__group_launch(hbicg__group *g) {
+    int ng = 0, cap = 0, err = 0, lrc = HBICG_OK;
+    hbk_matrix *A = calloc((size_t)g->n + 1, sizeof(hbk_matrix));
+    hbk_vectors *V = calloc((size_t)g->n + 1, sizeof(hbk_vectors));
+    hbk_shifts *H = calloc((size_t)g->n + 1, sizeof(hbk_shifts));
     void *ws = NULL;
     cudaEvent_t e0 = NULL, e1 = NULL;
-    int grc = HBICG_OK, ng = 0, cap = 0, err = 0;
-    if (!R || !in || !A || !V || !H) {
-        grc = HBICG_E_NOMEM;
+    float ms = 0.f;
+    if (!A || !V || !H) {
+        lrc = HBICG_E_NOMEM;
         goto out;
     }
-    for (int f = 0; f < nf; ++f) {
-        run_init(&R[f], seed[f], HBICG_HOST, x[f], NULL, HBICG_HOST, st ? &st[f] : NULL);
-        if (!hbicg__group_eligible(S[f]) || S[f]->ctx != ctx) {
-            rc[f] = HBICG_E_ARG;
-            set_msg("family %d cannot join the shared launch", f);
-            continue;
-        }
-        rc[f] = run_begin(S[f], b[f], sigma[f], &R[f]);
-        if (rc[f] == HBICG_OK) rc[f] = fused_init(S[f], seed[f], &R[f].launches);
-        if (rc[f] != HBICG_OK) continue;
-        in[f] = 1;
-        A[ng] = S[f]->A->k;
-        V[ng] = S[f]->v;
-        H[ng] = S[f]->sh;
-        if (S[f]->kcap > cap) cap = S[f]->kcap;
+    for (int f = 0; f < g->n; ++f) {
+        if (!g->in[f]) continue;
+        const hbicg_solver *s = g->S[f];
+        A[ng] = s->A->k;
+        V[ng] = s->v;
+        H[ng] = s->sh;
+        if (s->kcap > cap) cap = s->kcap;
         ++ng;
     }
-    if (ng) {
-        const size_t bytes = hbk_group_ws_bytes(ng, V);
-        float ms = 0.f;
-        int lrc = HBICG_OK;
-        if (pool_alloc(&ws, bytes, stream) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
-            cudaEventCreate(&e1) != cudaSuccess) {
-            lrc = HBICG_E_NOMEM;
-        } else {
-            cudaEventRecord(e0, stream);
-            const int e = hbk_group_run(ng, A, V, H, cap, max_ctas, ws, bytes, &err, stream);
-            cudaEventRecord(e1, stream);
-            if (e || cudaStreamSynchronize(stream) != cudaSuccess) {
-                set_msg("shared launch: %s", hbk_error_string(e ? e : (int)cudaGetLastError()));
-                lrc = HBICG_E_CUDA;
-            } else if (err) {
-                set_msg("shared launch: %s", err == HBK_GROUP_ERR_WAIT ? "a grid barrier's wait timed out"
-                                                                        : "the iteration cap was reached");
-                lrc = HBICG_E_TIMEOUT;
-            }
-            cudaEventElapsedTime(&ms, e0, e1);
-        }
-        for (int f = 0; f < nf; ++f) {
-            if (!in[f]) continue;
-            int r = lrc;
-            if (r == HBICG_OK) {
-                cudaError_t ce = cudaMemcpyAsync(ctx->h_sc, S[f]->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost,
-                                                 stream);
-                if (!ce) ce = cudaStreamSynchronize(stream);
-                r = ce ? HBICG_E_CUDA : fused_collect(S[f], &R[f]);
-            }
-            R[f].launches += 1;
-            R[f].shared_ms = ms;
-            rc[f] = run_end(S[f], &R[f], r);
-        }
+    if (!ng) goto out;
+    const size_t bytes = hbk_group_ws_bytes(ng, V);
+    if (pool_alloc(&ws, bytes, g->stream) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess) {
+        lrc = HBICG_E_NOMEM;
+        goto out;
     }
+    cudaEventRecord(e0, g->stream);
+    const int e = hbk_group_run(ng, A, V, H, cap, g->max_ctas, ws, bytes, &err, g->stream);
+    cudaEventRecord(e1, g->stream);
+    if (e || cudaStreamSynchronize(g->stream) != cudaSuccess) {
+        set_msg("shared launch: %s", hbk_error_string(e ? e : (int)cudaGetLastError()));
+        lrc = HBICG_E_CUDA;
+    } else if (err) {
+        set_msg("shared launch: %s",
+                err == HBK_GROUP_ERR_WAIT ? "a grid barrier's wait timed out" : "the iteration cap was reached");
+        lrc = HBICG_E_TIMEOUT;
+    }
+    cudaEventElapsedTime(&ms, e0, e1);
 out:
-    if (R)
-        for (int f = 0; f < nf; ++f) run_release(S[f], &R[f]);
-    if (ws) hbicg__dev_free(ws, stream);
+    if (ws) hbicg__dev_free(ws, g->stream);
+    cudaStreamSynchronize(g->stream);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
-    cudaStreamSynchronize(stream);
-    free(R);
-    free(in);
     free(A);
     free(V);
     free(H);
-    return grc;
+    g->lrc = lrc;
+    g->ms = ms;
+    return lrc;
+}
+
+int hbicg__group_finish(hbicg__group *g, int slot) {
+    if (slot < 0 || slot >= g->n) return HBICG_E_ARG;
+    hbicg_solver *s = g->S[slot];
+    run_t *r = &g->R[slot];
+    int rc = g->rc[slot];
+    if (g->in[slot]) {
+        int it = g->lrc;
+        if (it == HBICG_OK) {
+            cudaStream_t st = s->ctx->stream;
+            cudaError_t ce = cudaMemcpyAsync(s->ctx->h_sc, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st);
+            if (!ce) ce = cudaStreamSynchronize(st);
+            it = ce ? HBICG_E_CUDA : fused_collect(s, r);
+        }
+        r->launches += 1;
+        r->shared_ms = g->ms;
+        rc = run_end(s, r, it);
+    }
+    run_release(s, r);
+    g->rc[slot] = rc;
+    return rc;
 }
 
 int hbicg_solve(unsigned n, unsigned nnz, const unsigned *ptr, const unsigned *col, const double *val,
