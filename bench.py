@@ -606,6 +606,9 @@ def run_batch_c4(args, dist: Dist):
     over = [i for i, r in enumerate(res) if r.max_true_residual > 1e-10 * 1.01]
     iters = int(sum(r.k for r in res))
     work = lambda f, k: (f.a.nnz + 6.0 * len(f.sigma) * f.a.n) * max(k - 1, 1)
+    # the families of the shared persistent launch (incremental shift mode)
+    in_group = lambda f: (not args.no_persistent and args.shift_mode == "auto"
+                          and f.a.n * len(f.sigma) < (1 << 21))
     line = {"metric": "C4: time to solve 256 uneven shifted families (host arrays in/out), tol 1e-10",
             "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
@@ -615,11 +618,13 @@ def run_batch_c4(args, dist: Dist):
                        "workers": args.workers, "shift_mode": args.shift_mode, "refine": not args.no_refine,
                        "persistent": not args.no_persistent, "persistent_ctas": args.persistent_ctas,
                        "l2": "every family's working set is re-read from HBM"},
-            "persistent_families": sum(1 for f in fams if f.a.n * len(f.sigma) < (1 << 21))
-            if not args.no_persistent and args.shift_mode == "auto" else 0,
+            "persistent_families": sum(1 for f in fams if in_group(f)),
             "families_per_s": 256 / value, "total_iterations": iters, "status_failures": status_bad,
             "families_over_tol": over, "max_true_residual": max(r.max_true_residual for r in res),
-            "sum_device_solve_s": sum(r.solve_ms for r in res) / 1e3,
+            # device time of the worker-solved families, plus the shared launch once
+            "sum_device_solve_s": (sum(r.solve_ms for f, r in zip(fams, res) if not in_group(f))
+                                   + max([r.solve_ms for f, r in zip(fams, res) if in_group(f)] or [0.0])) / 1e3,
+            "persistent_launch_s": max([r.solve_ms for f, r in zip(fams, res) if in_group(f)] or [0.0]) / 1e3,
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": int(sum(12 * f.a.nnz + 4 * (f.a.n + 1) + 8 * f.a.n
                                                                              + 8 * len(f.sigma) for f in fams)),
                     "d2h_bytes_per_step": int(sum(8 * len(f.sigma) * f.a.n for f in fams))},
@@ -919,6 +924,29 @@ def run_mmread(args):
             "write_s": write_s, "entries_ok": bool(same)}
 
 
+def run_group_kernel(args):
+    """The shared persistent launch alone on a small case of config 4: the
+    first `--families` (default 64) families of the 256-family batch that take
+    the incremental shift mode, solved by hbicg_batch_solve_opts with the
+    shared launch; `--warmup` untimed and `--steps` timed calls.  Reports the
+    launch's device time (CUDA events around it) and the whole call's."""
+    pkg = graft.load_package()
+    fams = [f for f in pkg.workloads.batched_families(256) if f.a.n * len(f.sigma) < (1 << 21)][:args.families]
+    kw = dict(tol=1e-10, max_iter=10000, true_residuals=True, persistent=True, persistent_ctas=args.persistent_ctas)
+    for _ in range(args.warmup):
+        pkg.batch_solve(fams, workers=args.workers, **kw)
+    launch, wall, res = [], [], None
+    for _ in range(max(1, args.steps)):
+        res, w = pkg.batch_solve(fams, workers=args.workers, **kw)
+        launch.append(res[0].solve_ms)
+        wall.append(w)
+    return {"kernel": "k_group (shared persistent launch)", "families": len(fams),
+            "rows": int(sum(f.a.n for f in fams)), "shifts": int(sum(len(f.sigma) for f in fams)),
+            "launch_ms": float(np.median(launch)), "call_s": float(np.median(wall)),
+            "iterations_max": int(max(r.k for r in res)), "status_failures": sum(r.status != 0 for r in res),
+            "max_true_residual": max(r.max_true_residual for r in res)}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -937,9 +965,10 @@ def main(argv=None):
     ap.add_argument("--no-refine", action="store_true", help="keep the reference's x (no true-residual correction)")
     ap.add_argument("--row-classes", action="store_true",
                     help="--kernel spmv: also time the matrix with its rows of <= 32 / > 32 entries emptied")
-    ap.add_argument("--kernel", default=None, choices=["flush", "spmv", "coo2csr", "mmread"],
+    ap.add_argument("--kernel", default=None, choices=["flush", "spmv", "coo2csr", "mmread", "group"],
                     help="time one kernel alone on random data instead of the solve")
     ap.add_argument("--n", type=int, default=2097152, help="elements for --kernel")
+    ap.add_argument("--families", type=int, default=64, help="families for --kernel group")
     ap.add_argument("--workers", type=int, default=8, help="host workers for --workload c4")
     ap.add_argument("--no-persistent", action="store_true",
                     help="--workload c4: every family on the workers (no shared persistent launch)")
@@ -949,7 +978,7 @@ def main(argv=None):
     args = ap.parse_args(argv)
     if args.kernel:
         run = {"flush": run_flush_kernel, "spmv": run_spmv_kernel, "coo2csr": run_coo2csr_kernel,
-               "mmread": run_mmread}[args.kernel]
+               "mmread": run_mmread, "group": run_group_kernel}[args.kernel]
         print(json.dumps(run(args)), flush=True)
         return
     if args.impl == "ours" and args.warmup < 3:
