@@ -339,13 +339,17 @@ int hbicg_solver_create(hbicg_context *ctx, hbicg_matrix *A, int m, const hbicg_
         long cap = (long)(budget / (double)vb);
         long want = 2L * s->kcap + 8;
         if (cap > want) cap = want;
-        /* Blocks of at most 24 iterations by default: the coefficient
-         * representation over a long raw Krylov basis loses accuracy where a
-         * shift's recurrence nearly breaks down (|pi_k| << |pi_{k-1}|); forming
-         * x_j and p_j every block keeps the true residuals at the level of the
-         * incremental form (checked on the 256^3 family up to blocks of 32).
-         * basis_block < 0 lets the basis grow as far as memory allows. */
-        const int block = p.basis_block == 0 ? 24 : p.basis_block;
+        /* Blocks of at most 28 iterations by default (59 slots: within the
+         * tensor-core flush's 64): the coefficient representation over a long
+         * raw Krylov basis loses accuracy where a shift's recurrence nearly
+         * breaks down (|pi_k| << |pi_{k-1}|); forming x_j and p_j every block
+         * keeps the true residuals at the level of the incremental form.
+         * Measured on the 256^3 family: blocks of 24 and 28 end at the same
+         * residuals and solutions (28: 15 flushes instead of 18, 0.776 against
+         * 0.827 s); 26 left one shift for the true-residual correction, 30
+         * misses the tolerance.  basis_block < 0 lets the basis grow as far as
+         * memory allows. */
+        const int block = p.basis_block == 0 ? 28 : p.basis_block;
         if (block > 0 && cap > 2L * block + 3) cap = 2L * block + 3;
         if (cap < 8) {
             /* not enough memory for a useful basis: fall back */

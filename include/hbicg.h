@@ -59,7 +59,7 @@ typedef struct {
     double basis_mem_frac; /* deferred mode: share of free device memory for the basis (default 0.6) */
     int true_residuals;    /* compute ||b-(A+sigma_j I)x_j||/||b|| after the solve (default 0) */
     int basis_block;       /* deferred mode: iterations per basis block before x_j, p_j are formed
-                              (0 = automatic, 24; < 0 = as long as memory allows) */
+                              (0 = automatic, 28; < 0 = as long as memory allows) */
     int flush_mode;        /* deferred mode: hbicg_flush_mode (default AUTO) */
     int refine;            /* 1: after the solve, check every shift's true residual
                               ||b - (A + sigma_j I) x_j|| / ||b|| and correct shifts above

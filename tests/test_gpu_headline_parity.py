@@ -2,7 +2,7 @@
 stencil with 64 geometric shifts in [1e-4, 1], b ~ N(0,1) normalised, tol
 1e-10, seed 0, dynamic switching, solved in the form the benchmark times
 (fused, deferred shifts over the seed's Krylov basis, basis flushes on the
-tensor cores, blocks of 24 iterations, CUDA graphs) with the reference's
+tensor cores, blocks of 28 iterations, CUDA graphs) with the reference's
 semantics (no true-residual correction):
 
 * 64^3: every x_j against the oracle (the reference's algorithm on the same
