@@ -592,7 +592,8 @@ def run_batch_c4(args, dist: Dist):
     pkg = graft.load_package()
     fams = pkg.workloads.batched_families(256)
     kw = dict(tol=1e-10, max_iter=10000, shift_mode=args.shift_mode, flush=args.flush, true_residuals=True,
-              refine=not args.no_refine, basis_block=args.basis_block, persistent=not args.no_persistent,
+              refine=not args.no_refine, basis_block=args.basis_block,
+              persistent=False if args.no_persistent else ("all" if args.persistent_all else True),
               persistent_ctas=args.persistent_ctas)
     for _ in range(max(1, args.warmup)):
         pkg.batch_solve(fams, workers=args.workers, **kw)
@@ -607,8 +608,8 @@ def run_batch_c4(args, dist: Dist):
     iters = int(sum(r.k for r in res))
     work = lambda f, k: (f.a.nnz + 6.0 * len(f.sigma) * f.a.n) * max(k - 1, 1)
     # the families of the shared persistent launch (incremental shift mode)
-    in_group = lambda f: (not args.no_persistent and args.shift_mode == "auto"
-                          and f.a.n * len(f.sigma) < (1 << 21))
+    in_group = lambda f: (not args.no_persistent and (args.persistent_all or (args.shift_mode == "auto"
+                                                                              and f.a.n * len(f.sigma) < (1 << 21))))
     line = {"metric": "C4: time to solve 256 uneven shifted families (host arrays in/out), tol 1e-10",
             "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
@@ -616,10 +617,12 @@ def run_batch_c4(args, dist: Dist):
             "config": {"workload": "c4: 256 families, n log-uniform in [1e4, 5e5] (2-D 5-point / 3-D 7-point "
                                    "convection-diffusion), 8..64 shifts uniform in [1e-3, 1], b ~ N(0,1)",
                        "workers": args.workers, "shift_mode": args.shift_mode, "refine": not args.no_refine,
-                       "persistent": not args.no_persistent, "persistent_ctas": args.persistent_ctas,
+                       "persistent": "none" if args.no_persistent else ("all" if args.persistent_all else "incremental"),
+                       "persistent_ctas": args.persistent_ctas,
                        "l2": "every family's working set is re-read from HBM"},
             "persistent_families": sum(1 for f in fams if in_group(f)),
             "families_per_s": 256 / value, "total_iterations": iters, "status_failures": status_bad,
+            "failed_families": [[i, int(r.status), int(r.k)] for i, r in enumerate(res) if r.status != 0],
             "families_over_tol": over, "max_true_residual": max(r.max_true_residual for r in res),
             # device time of the worker-solved families, plus the shared launch once
             "sum_device_solve_s": (sum(r.solve_ms for f, r in zip(fams, res) if not in_group(f))
@@ -972,6 +975,8 @@ def main(argv=None):
     ap.add_argument("--workers", type=int, default=8, help="host workers for --workload c4")
     ap.add_argument("--no-persistent", action="store_true",
                     help="--workload c4: every family on the workers (no shared persistent launch)")
+    ap.add_argument("--persistent-all", action="store_true",
+                    help="--workload c4: every family in the shared persistent launch (both shift modes)")
     ap.add_argument("--persistent-ctas", type=int, default=0, help="CTAs of c4's persistent launch (0: one wave)")
     ap.add_argument("--ref-budget", type=float, default=1500.0,
                     help="--impl reference: longest projected full CPU solve (s) to measure; beyond it, estimate")

@@ -364,7 +364,8 @@ def batch_solve(families, workers: int = 8, autotune: bool = False, autotune_cac
     """hbicg_batch_solve_opts over workloads.Family-like objects (a, b,
     sigma, seed): every family solved with the same parameters (kw as
     params()); persistent: the incremental-mode families share one persistent
-    launch (persistent_ctas caps its CTAs, 0 = one wave).
+    launch ("all": every family, both shift modes; False: none;
+    persistent_ctas caps its CTAs, 0 = one wave).
     Returns ([FamilyResult], wall seconds)."""
     p = params(**kw)
     want_res = bool(kw.get("true_residuals", False))
@@ -389,7 +390,7 @@ def batch_solve(families, workers: int = 8, autotune: bool = False, autotune_cac
     opts = BatchOpts()
     lib().hbicg_batch_opts_default(C.byref(opts))
     opts.workers = int(workers)
-    opts.persistent = 1 if persistent else 0
+    opts.persistent = 2 if persistent == "all" else (1 if persistent else 0)
     opts.persistent_ctas = int(persistent_ctas)
     opts.autotune_cache = str(autotune_cache).encode() if autotune_cache else None
     lib().hbicg_batch_solve_opts(arr, len(families), C.byref(p), C.byref(opts), C.byref(wall))

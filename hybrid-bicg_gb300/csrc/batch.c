@@ -13,9 +13,11 @@
  *
  * Small families (incremental shift mode: n m < 2^21 with the automatic mode)
  * are latency-bound when each runs its own short kernels: they instead go to
- * one host thread that sets all of them up on one context and runs all their
- * iterations in ONE persistent cooperative launch (hbicg__group_solve,
- * hbk_group_run), while the workers take the larger families.
+ * a few host threads that set all of them up and run all their iterations in
+ * ONE persistent cooperative launch (hbicg__group_*, hbk_group_run), while
+ * the workers take the larger families.  With opts.persistent = 2 every
+ * family goes to the shared launch (those in the deferred shift mode pause
+ * there at each full basis; the host flushes them between rounds).
  * Failures are per family (status), never global. */
 #define _GNU_SOURCE
 #include <pthread.h>
@@ -243,7 +245,8 @@ int hbicg_batch_solve_opts(hbicg_family *fams, int count, const hbicg_params *p,
     for (int i = 0; i < count; i++) {
         const hbicg_family *f = &fams[order[i]];
         const int small = opts->persistent && p->form == HBICG_FORM_FUSED && !f->autotune && !f->r && f->m > 0 &&
-                          hbicg__shift_mode_for(p, f->n, f->m) == HBICG_SHIFTS_INCREMENTAL;
+                          (opts->persistent >= 2 ||
+                           hbicg__shift_mode_for(p, f->n, f->m) == HBICG_SHIFTS_INCREMENTAL);
         if (small) grp[ng++] = order[i];
         else order[nw++] = order[i];
     }

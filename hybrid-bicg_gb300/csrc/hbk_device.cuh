@@ -75,6 +75,8 @@ struct HwGrid {
     __device__ static __forceinline__ T ld(const T *p) { return *p; }
     template <class T>
     __device__ static __forceinline__ T ldx(const T *p) { return __ldg(p); }
+    template <class T>
+    __device__ static __forceinline__ T ldv(const T *p) { return __ldg(p); }
 };
 // element i of a vector the launch also writes (p indexed directly in a
 // one-step kernel, so its code is what it was without grid views)
@@ -97,6 +99,10 @@ struct VGrid {
     __device__ static __forceinline__ T ld(const T *p) { return __ldcg(p); }
     template <class T>
     __device__ static __forceinline__ T ldx(const T *p) { return __ldcg(p); }
+    // matrix values: the seed's private SELL-32 copy gets a new diagonal after
+    // a seed switch, inside the same persistent launch
+    template <class T>
+    __device__ static __forceinline__ T ldv(const T *p) { return __ldcg(p); }
 };
 
 // Called by the last block: sums partials[0..nparts) in a fixed order.
@@ -186,7 +192,7 @@ __device__ __forceinline__ void spmv_rows_sell(const hbk_matrix &A, const double
         double acc = 0.0;
 #pragma unroll 4
         for (unsigned e = 0; e < w; ++e) {
-            if (e < len) acc = fma(__ldg(vv + 32 * (size_t)e), G::ldx(x + __ldg(cc + 32 * (size_t)e)), acc);
+            if (e < len) acc = fma(G::ldv(vv + 32 * (size_t)e), G::ldx(x + __ldg(cc + 32 * (size_t)e)), acc);
         }
         if (r < n) epi(r, acc);
     }

@@ -586,7 +586,8 @@ template <int MAXS>
 __global__ void __launch_bounds__(NT) k_shift_update(Ctx c) { shift_update_body<MAXS>(c, HwGrid()); }
 
 // K5 (deferred): p_s update; on a switch the rescaled r_k goes to a new slot
-__global__ void __launch_bounds__(NT) k_seed_p_deferred(Ctx c) {
+template <class G>
+__device__ __forceinline__ void seed_p_deferred_body(const Ctx &c, const G &g) {
     __shared__ double sh[NW];
     __shared__ unsigned long long smx[NW];
     hbk_scalars *sc = c.sh.sc;
@@ -603,13 +604,13 @@ __global__ void __launch_bounds__(NT) k_seed_p_deferred(Ctx c) {
     const double *__restrict__ rh = c.v.r_hat;
     double acc = 0.0;
     unsigned long long mx = 0;
-    for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < n; i += (size_t)gridDim.x * NT) {
-        const double ri = rn[i];
-        ps[i] = fma(bw, s[i], fma(bk, ps[i], ri));
+    for (size_t i = g.b() * (size_t)NT + threadIdx.x; i < n; i += (size_t)g.nb() * NT) {
+        const double ri = HBK_LD(G, rn, i);
+        ps[i] = fma(bw, HBK_LD(G, s, i), fma(bk, HBK_LD(G, ps, i), ri));
         if (sw) {
             const double rs = ri * rsc;
             rsl[i] = rs;
-            acc = fma(rh[i], rs, acc);
+            acc = fma(HBK_LD(G, rh, i), rs, acc);
             const unsigned long long b = abs_bits(rs);
             mx = b > mx ? b : mx;
         }
@@ -617,21 +618,23 @@ __global__ void __launch_bounds__(NT) k_seed_p_deferred(Ctx c) {
     if (!sw) return;  // uniform: the reduction is needed only after a switch
     if (c.v.slot_max) block_max_to(mx, smx, c.v.slot_max + (size_t)(sc->slots + 2) * HBK_SLOT_SPREAD);  // rescaled r_k
     acc = block_sum(acc, sh);
-    if (threadIdx.x == 0) c.sh.partials[blockIdx.x] = acc;
-    if (take_ticket(c.sh.counters + 3)) {
-        const double rrh = sum_partials(c.sh.partials, gridDim.x, sh);
+    if (threadIdx.x == 0) c.sh.partials[g.b()] = acc;
+    if (take_ticket(c.sh.counters + 3, g.nb())) {
+        const double rrh = sum_partials(c.sh.partials, g.nb(), sh);
         if (threadIdx.x == 0) {
             sc->rs_switch = rrh;
             c.sh.counters[3] = 0;
         }
     }
 }
+__global__ void __launch_bounds__(NT) k_seed_p_deferred(Ctx c) { seed_p_deferred_body(c, HwGrid()); }
 
 // K6 (deferred): coefficient update of every running system over the basis
 // slots in use, then the end-of-iteration bookkeeping.  Per coefficient the
 // operations follow the vector update's order (x += c0 q; x += c1 p;
 // p += c2 q; p += c3 r_{k-1}; p *= beta_j; p += c5 r_k).
-__global__ void __launch_bounds__(NT) k_coef_update(Ctx c) {
+template <class G>
+__device__ __forceinline__ void coef_update_body(const Ctx &c, const G &g) {
     hbk_scalars *sc = c.sh.sc;
     if (stopped(sc)) return;
     const int na = sc->n_active;
@@ -639,13 +642,13 @@ __global__ void __launch_bounds__(NT) k_coef_update(Ctx c) {
     const int L = sc->slots + 2;
     const int cap = c.v.slot_cap;
     const size_t tot = (size_t)na * L;
-    for (size_t it = blockIdx.x * (size_t)NT + threadIdx.x; it < tot; it += (size_t)gridDim.x * NT) {
+    for (size_t it = g.b() * (size_t)NT + threadIdx.x; it < tot; it += (size_t)g.nb() * NT) {
         const int a = (int)(it / L), i = (int)(it % L);
-        const int j = c.sh.act_list[a];
+        const int j = HBK_LD(G, c.sh.act_list, a);
         const double *co = c.sh.coef + (size_t)j * HBK_NCOEF;
         double *xc = c.v.Xc + (size_t)j * cap + i;
         double *pc = c.v.Pc + (size_t)j * cap + i;
-        double x = *xc, p = *pc;
+        double x = HBK_LD(G, xc, 0), p = HBK_LD(G, pc, 0);
         if (i == sq) x = x + co[0];
         x = fma(co[1], p, x);
         if (i == sq) p = p + co[2];
@@ -656,58 +659,61 @@ __global__ void __launch_bounds__(NT) k_coef_update(Ctx c) {
         *pc = p;
         if (i == 0) {
             double *ow = c.v.own + 2 * (size_t)j;
-            ow[0] = fma(co[1], ow[1], ow[0]);
-            ow[1] = co[4] * ow[1];
+            ow[0] = fma(co[1], HBK_LD(G, ow, 1), HBK_LD(G, ow, 0));
+            ow[1] = co[4] * HBK_LD(G, ow, 1);
             c.sh.lslot[j] = L;
         }
     }
-    if (take_ticket(c.sh.counters + 4)) {
+    if (take_ticket(c.sh.counters + 4, g.nb())) {
         if (threadIdx.x == 0) {
             finish_iteration(c, sc, sc->rs_switch);
             c.sh.counters[4] = 0;
         }
     }
 }
+__global__ void __launch_bounds__(NT) k_coef_update(Ctx c) { coef_update_body(c, HwGrid()); }
 
 // K7 (deferred): after a switch, the new seed's p = own term + Pc[t] . V
-__global__ void __launch_bounds__(NT) k_materialize_ps(Ctx c) {
+template <class G>
+__device__ __forceinline__ void materialize_ps_body(const Ctx &c, const G &g) {
     __shared__ double s_c[1024];
     hbk_scalars *sc = c.sh.sc;
-    if (!sc->need_ps) return;
+    if (!__ldcg(&sc->need_ps)) return;
     const int t = sc->seed;
-    const int L = c.sh.lslot[t];
+    const int L = HBK_LD(G, c.sh.lslot, t);
     const unsigned n = c.v.n;
     const size_t ld = ldn(n);
     const double *pc = c.v.Pc + (size_t)t * c.v.slot_cap;
-    const double rho = c.v.own[2 * (size_t)t + 1];
+    const double rho = HBK_LD(G, c.v.own, 2 * (size_t)t + 1);
     const double *pmat = c.v.Pmat;  // panel-major
-    for (size_t i0 = (size_t)blockIdx.x * NT; i0 < n; i0 += (size_t)gridDim.x * NT) {
+    for (size_t i0 = (size_t)g.b() * NT; i0 < n; i0 += (size_t)g.nb() * NT) {
         const size_t i = i0 + threadIdx.x;
         double acc = (pmat && i < n) ? rho * pmat[panel_idx(t, (unsigned)i, c.v.pm)] : 0.0;
         for (int l0 = 0; l0 < L; l0 += 1024) {
             const int cnt = min(1024, L - l0);
             __syncthreads();
-            for (int l = threadIdx.x; l < cnt; l += NT) s_c[l] = pc[l0 + l];
+            for (int l = threadIdx.x; l < cnt; l += NT) s_c[l] = HBK_LD(G, pc, l0 + l);
             __syncthreads();
             if (i < n)
-                for (int l = 0; l < cnt; l++) acc = fma(s_c[l], c.v.V[(size_t)(l0 + l) * ld + i], acc);
+                for (int l = 0; l < cnt; l++) acc = fma(s_c[l], HBK_LD(G, c.v.V, (size_t)(l0 + l) * ld + i), acc);
         }
         if (i < n) c.v.ps[i] = acc;
     }
     if (c.v.sval_shift) {  // the new seed's shift on the diagonal of the seed kernels' products
         const double sg = c.sh.sigma[t];
-        for (size_t r = blockIdx.x * (size_t)NT + threadIdx.x; r < n; r += (size_t)gridDim.x * NT) {
+        for (size_t r = g.b() * (size_t)NT + threadIdx.x; r < n; r += (size_t)g.nb() * NT) {
             const unsigned long long d = c.v.sdiag[r];
             c.v.sval_shift[d] = c.v.sval_orig[d] + sg;
         }
     }
-    if (take_ticket(c.sh.counters + 5)) {
+    if (take_ticket(c.sh.counters + 5, g.nb())) {
         if (threadIdx.x == 0) {
             sc->need_ps = 0;
             c.sh.counters[5] = 0;
         }
     }
 }
+__global__ void __launch_bounds__(NT) k_materialize_ps(Ctx c) { materialize_ps_body(c, HwGrid()); }
 
 // Flush: X_j += xi_j Pmat_j + Xc_j . V ; when keep_p, Pmat_j = rho_j Pmat_j + Pc_j . V.
 // Each thread owns one row and GROUP systems; coefficients are staged in
@@ -858,17 +864,19 @@ __global__ void __launch_bounds__(NT) k_panel_to_rows(const double *__restrict__
 }
 
 // ---------------------------------------------------------------------------
-// Many families in one persistent launch (incremental shift mode, SELL-32).
+// Many families in one persistent launch (SELL-32, either shift mode).
 //
 // Each family's rows are cut into virtual blocks of HBK_GROUP_ROWS rows; the
 // CTAs of one cooperative launch take the virtual blocks of all families in
 // turn (virtual block v goes to CTA v mod grid, so a family's rows stay on
 // the same CTAs from step to step) and run, for every family at once, the
-// same five steps as the one-family kernels (K1..K5 above, with a virtual
-// block in place of the launch's block: same partial sums, same last-block
-// tickets and scalar stage per family).  A grid-wide barrier separates the
-// steps.  Families stop one by one (converged, max_iter, breakdown); their
-// virtual blocks then return at once.
+// same steps as the one-family kernels (K1..K5, and K6, K7 for the families
+// in the deferred mode, with a virtual block in place of the launch's block:
+// same partial sums, same last-block tickets and scalar stage per family).  A
+// grid-wide barrier separates the steps.  Families stop one by one
+// (converged, max_iter, breakdown) or pause with a full basis; their virtual
+// blocks then return at once, and the launch ends when every family has
+// stopped or paused (the host flushes the paused ones and launches again).
 struct GroupFam {
     Ctx c;
     unsigned vb0, nvb;  // the family's virtual blocks [vb0, vb0 + nvb)
@@ -931,10 +939,24 @@ __device__ bool grid_barrier(unsigned *bar, int *err) {
     return s_ok != 0;
 }
 
+// step 5: the shift update (incremental) or the seed's p update (deferred)
 template <int MAXS>
-__global__ void __launch_bounds__(NT) k_group(const GroupFam *__restrict__ fams, int nf,
-                                              const unsigned *__restrict__ vb_fam, unsigned nvb, unsigned *bar,
-                                              int *err, int iter_cap) {
+__device__ __forceinline__ void step5_body(const Ctx &c, const VGrid &g) {
+    if (c.v.deferred) seed_p_deferred_body(c, g);
+    else shift_update_body<MAXS>(c, g);
+}
+__device__ __forceinline__ void coef_update_if_deferred(const Ctx &c, const VGrid &g) {
+    if (c.v.deferred) coef_update_body(c, g);
+}
+__device__ __forceinline__ void materialize_if_deferred(const Ctx &c, const VGrid &g) {
+    if (c.v.deferred) materialize_ps_body(c, g);
+}
+
+// (3 CTAs per SM: the register cap costs a few spills in the scalar stage)
+template <int MAXS>
+__global__ void __launch_bounds__(NT, 3) k_group(const GroupFam *__restrict__ fams, int nf,
+                                                 const unsigned *__restrict__ vb_fam, unsigned nvb, unsigned *bar,
+                                                 int *err, int iter_cap, int any_deferred) {
 #define HBK_GROUP_STEP(body)                                                       \
     for (unsigned vb = blockIdx.x; vb < nvb; vb += gridDim.x) {                    \
         const GroupFam &F = fams[vb_fam[vb]];                                      \
@@ -952,7 +974,11 @@ __global__ void __launch_bounds__(NT) k_group(const GroupFam *__restrict__ fams,
         HBK_GROUP_STEP(seed_q_body)
         HBK_GROUP_STEP(seed_y_body<HBK_FMT_SELL>)
         HBK_GROUP_STEP(seed_update_body)
-        HBK_GROUP_STEP(shift_update_body<MAXS>)
+        HBK_GROUP_STEP(step5_body<MAXS>)
+        if (any_deferred) {
+            HBK_GROUP_STEP(coef_update_if_deferred)
+            HBK_GROUP_STEP(materialize_if_deferred)
+        }
     }
 #undef HBK_GROUP_STEP
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(err, HBK_GROUP_ERR_CAP);
@@ -1094,8 +1120,10 @@ int hbk_group_run(int nf, const hbk_matrix *A, const hbk_vectors *v, const hbk_s
     if (!coop) return (int)cudaErrorNotSupported;
     std::vector<GroupFam> tab((size_t)nf);
     std::vector<unsigned> map;
+    int any_deferred = 0;
     for (int f = 0; f < nf; ++f) {
-        if (A[f].fmt != HBK_FMT_SELL || v[f].deferred) return (int)cudaErrorInvalidValue;
+        if (A[f].fmt != HBK_FMT_SELL) return (int)cudaErrorInvalidValue;
+        any_deferred |= v[f].deferred != 0;
         tab[f].c = make_ctx(&A[f], &v[f], &sh[f]);
         tab[f].vb0 = (unsigned)map.size();
         tab[f].nvb = group_vblocks(v[f].n);
@@ -1117,7 +1145,8 @@ int hbk_group_run(int nf, const hbk_matrix *A, const hbk_vectors *v, const hbk_s
     const int ctas = hbk_group_ctas(max_ctas);
     const GroupFam *a0 = dtab;
     const unsigned *a2 = dmap;
-    void *args[] = {(void *)&a0, (void *)&nf, (void *)&a2, (void *)&nvb, (void *)&bar, (void *)&err, (void *)&iter_cap};
+    void *args[] = {(void *)&a0,  (void *)&nf,  (void *)&a2,       (void *)&nvb,
+                    (void *)&bar, (void *)&err, (void *)&iter_cap, (void *)&any_deferred};
     if ((e = (int)cudaLaunchCooperativeKernel((const void *)k_group<64>, dim3(ctas), dim3(NT), args, 0, st))) return e;
     /* pageable destination: returns once the launch has finished */
     return (int)cudaMemcpyAsync(err_out, err, sizeof(int), cudaMemcpyDeviceToHost, st);

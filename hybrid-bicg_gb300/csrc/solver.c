@@ -786,6 +786,65 @@ static int fused_init(hbicg_solver *s, int seed, int *launches) {
     return HBICG_OK;
 }
 
+/* A fused solve paused with a full basis (scalars in h_sc): form x_j and
+ * p_j, restart the basis (the reset lets the solve run on) and note the last
+ * iteration the flush covered. */
+static int fused_pause_flush(hbicg_solver *s, int *k_flushed, int *launches, int *flushes, double *flush_ms) {
+    cudaStream_t st = s->ctx->stream;
+    hbk_scalars *h = s->ctx->h_sc;
+    int rc = ensure_pmat(s);
+    if (rc) return rc;
+    float t = 0.f;
+    CUDA_TRY(cudaEventRecord(s->ctx->evf0, st));
+    rc = do_flush(s, 1, h->slots, *k_flushed, launches);
+    if (rc) return rc;
+    *k_flushed = h->k - 1;
+    if (s->early_x && (rc = early_copies(s, *k_flushed, launches))) return rc;
+    CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
+    CUDA_TRY(cudaEventSynchronize(s->ctx->evf1));
+    CUDA_TRY(cudaEventElapsedTime(&t, s->ctx->evf0, s->ctx->evf1));
+    *flush_ms += t;
+    (*flushes)++;
+    return HBICG_OK;
+}
+
+/* The end of a fused solve whose iterations are over (h_sc holds its
+ * scalars): in the deferred mode the last flush and x_j back to rows; the
+ * final scalars in h_sc. */
+static int fused_tail(hbicg_solver *s, int k_flushed, int *launches, double *flush_ms) {
+    cudaStream_t st = s->ctx->stream;
+    hbk_scalars *h = s->ctx->h_sc;
+    if (s->v.deferred) {
+        float t = 0.f;
+        CUDA_TRY(cudaEventRecord(s->ctx->evf0, st));
+        int rc = do_flush(s, 0, h->slots, k_flushed, launches);
+        if (rc) return rc;
+        CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
+        /* x_j were panel-major during the solve; rows already on their way to
+         * the host are rewritten with the same values only after those copies */
+        if (s->early_pending) {
+            CUDA_TRY(cudaEventRecord(s->ctx->cev, s->ctx->cstream));
+            CUDA_TRY(cudaStreamWaitEvent(st, s->ctx->cev, 0));
+        }
+        HBK_TRY(hbk_panel_to_rows(s->v.Xp, s->v.pm, s->A->k.n, s->v.X, s->ld, st));
+        ++*launches;
+        CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
+        int tc_err = 0;
+        if (s->d_tc_err) CUDA_TRY(cudaMemcpyAsync(&tc_err, s->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        CUDA_TRY(cudaEventElapsedTime(&t, s->ctx->evf0, s->ctx->evf1));
+        *flush_ms += t;
+        if (tc_err) {
+            set_msg("tensor-core flush: an mbarrier wait timed out");
+            return HBICG_E_TIMEOUT;
+        }
+        return HBICG_OK;
+    }
+    CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return HBICG_OK;
+}
+
 static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, double *flush_ms) {
     cudaStream_t st = s->ctx->stream;
     hbk_scalars *h = s->ctx->h_sc;
@@ -824,52 +883,13 @@ static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, dou
         }
         if (!h->finished) continue;
         if ((h->status & HBK_ST_BASIS_FULL) && !(h->status & HBK_ST_BREAKDOWN)) {
-            int rc = ensure_pmat(s);
+            int rc = fused_pause_flush(s, &k_flushed, launches, flushes, flush_ms);
             if (rc) return rc;
-            float t = 0.f;
-            CUDA_TRY(cudaEventRecord(s->ctx->evf0, st));
-            rc = do_flush(s, 1, h->slots, k_flushed, launches);
-            if (rc) return rc;
-            k_flushed = h->k - 1;
-            if (s->early_x && (rc = early_copies(s, k_flushed, launches))) return rc;
-            CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
-            CUDA_TRY(cudaEventSynchronize(s->ctx->evf1));
-            CUDA_TRY(cudaEventElapsedTime(&t, s->ctx->evf0, s->ctx->evf1));
-            *flush_ms += t;
-            (*flushes)++;
             continue;
         }
         break;
     }
-    if (s->v.deferred) {
-        float t = 0.f;
-        CUDA_TRY(cudaEventRecord(s->ctx->evf0, st));
-        int rc = do_flush(s, 0, h->slots, k_flushed, launches);
-        if (rc) return rc;
-        CUDA_TRY(cudaEventRecord(s->ctx->evf1, st));
-        /* x_j were panel-major during the solve; rows already on their way to
-         * the host are rewritten with the same values only after those copies */
-        if (s->early_pending) {
-            CUDA_TRY(cudaEventRecord(s->ctx->cev, s->ctx->cstream));
-            CUDA_TRY(cudaStreamWaitEvent(st, s->ctx->cev, 0));
-        }
-        HBK_TRY(hbk_panel_to_rows(s->v.Xp, s->v.pm, s->A->k.n, s->v.X, s->ld, st));
-        ++*launches;
-        CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
-        int tc_err = 0;
-        if (s->d_tc_err) CUDA_TRY(cudaMemcpyAsync(&tc_err, s->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(cudaStreamSynchronize(st));
-        CUDA_TRY(cudaEventElapsedTime(&t, s->ctx->evf0, s->ctx->evf1));
-        *flush_ms += t;
-        if (tc_err) {
-            set_msg("tensor-core flush: an mbarrier wait timed out");
-            return HBICG_E_TIMEOUT;
-        }
-        return HBICG_OK;
-    }
-    CUDA_TRY(cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    return HBICG_OK;
+    return fused_tail(s, k_flushed, launches, flush_ms);
 }
 
 /* compulsory HBM bytes of the fused schedule for one solve */
@@ -1275,8 +1295,7 @@ static int run_end(hbicg_solver *s, run_t *r, int rc) {
 /* many solves, one launch */
 
 int hbicg__group_eligible(const hbicg_solver *s) {
-    return s && s->p.form == HBICG_FORM_FUSED && s->mode == HBICG_SHIFTS_INCREMENTAL && !s->v.deferred &&
-           s->A->k.fmt == HBK_FMT_SELL && s->m > 0;
+    return s && s->p.form == HBICG_FORM_FUSED && s->A->k.fmt == HBK_FMT_SELL && s->m > 0;
 }
 
 /* Solves of many families whose iterations run in one persistent launch
@@ -1292,12 +1311,14 @@ int hbicg__group_eligible(const hbicg_solver *s) {
  * counts it once. */
 struct hbicg__group {
     pthread_mutex_t lock;
-    int cap, n, max_ctas, lrc;
+    int cap, n, max_ctas, lrc, rounds;
     double ms;
     cudaStream_t stream;
     hbicg_solver **S;
     run_t *R;
     int *rc, *in;
+    int *k_flushed; /* deferred mode: last iteration the family's previous flush covered */
+    int *itrc;      /* a family's own failure between rounds (a flush) */
 };
 
 hbicg__group *hbicg__group_new(int cap, int max_ctas) {
@@ -1310,14 +1331,18 @@ hbicg__group *hbicg__group_new(int cap, int max_ctas) {
     g->R = calloc((size_t)g->cap, sizeof *g->R);
     g->rc = calloc((size_t)g->cap, sizeof *g->rc);
     g->in = calloc((size_t)g->cap, sizeof *g->in);
+    g->k_flushed = calloc((size_t)g->cap, sizeof *g->k_flushed);
+    g->itrc = calloc((size_t)g->cap, sizeof *g->itrc);
     cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
     if (!e) e = cudaStreamCreateWithPriority(&g->stream, cudaStreamNonBlocking, hi);
-    if (!g->S || !g->R || !g->rc || !g->in || e) {
+    if (!g->S || !g->R || !g->rc || !g->in || !g->k_flushed || !g->itrc || e) {
         if (!e) cudaStreamDestroy(g->stream);
         free(g->S);
         free(g->R);
         free(g->rc);
         free(g->in);
+        free(g->k_flushed);
+        free(g->itrc);
         free(g);
         return NULL;
     }
@@ -1334,6 +1359,8 @@ void hbicg__group_free(hbicg__group *g) {
     free(g->R);
     free(g->rc);
     free(g->in);
+    free(g->k_flushed);
+    free(g->itrc);
     free(g);
 }
 
@@ -1347,7 +1374,7 @@ int hbicg__group_add(hbicg__group *g, hbicg_solver *s, const double *b, const do
     run_init(r, seed, HBICG_HOST, x, NULL, HBICG_HOST, st);
     g->S[slot] = s;
     int rc = hbicg__group_eligible(s) ? HBICG_OK : HBICG_E_ARG;
-    if (rc) set_msg("a solver that is not fused, incremental and SELL-32 cannot join the shared launch");
+    if (rc) set_msg("a solver that is not fused and SELL-32 cannot join the shared launch");
     if (rc == HBICG_OK) rc = run_begin(s, b, sigma, r);
     if (rc == HBICG_OK) rc = fused_init(s, seed, &r->launches);
     g->rc[slot] = rc;
@@ -1355,46 +1382,100 @@ int hbicg__group_add(hbicg__group *g, hbicg_solver *s, const double *b, const do
     return slot;
 }
 
+/* Rounds of the shared launch: each runs the iterations of every family
+ * still going until each has stopped or paused with a full basis (deferred
+ * mode); the paused ones are flushed (their own stream) and run on in the
+ * next round. */
 int hbicg__group_launch(hbicg__group *g) {
-    int ng = 0, cap = 0, err = 0, lrc = HBICG_OK;
-    hbk_matrix *A = calloc((size_t)g->n + 1, sizeof(hbk_matrix));
-    hbk_vectors *V = calloc((size_t)g->n + 1, sizeof(hbk_vectors));
-    hbk_shifts *H = calloc((size_t)g->n + 1, sizeof(hbk_shifts));
+    int err = 0, lrc = HBICG_OK, rounds = 0;
+    const int n = g->n;
+    hbk_matrix *A = calloc((size_t)n + 1, sizeof(hbk_matrix));
+    hbk_vectors *V = calloc((size_t)n + 1, sizeof(hbk_vectors));
+    hbk_shifts *H = calloc((size_t)n + 1, sizeof(hbk_shifts));
+    int *idx = calloc((size_t)n + 1, sizeof(int)), *run = calloc((size_t)n + 1, sizeof(int));
     void *ws = NULL;
+    size_t bytes = 0;
     cudaEvent_t e0 = NULL, e1 = NULL;
-    float ms = 0.f;
-    if (!A || !V || !H) {
+    double total_ms = 0.0;
+    int kmax = 0;
+    if (!A || !V || !H || !idx || !run) {
         lrc = HBICG_E_NOMEM;
         goto out;
     }
-    for (int f = 0; f < g->n; ++f) {
-        if (!g->in[f]) continue;
-        const hbicg_solver *s = g->S[f];
-        A[ng] = s->A->k;
-        V[ng] = s->v;
-        H[ng] = s->sh;
-        if (s->kcap > cap) cap = s->kcap;
-        ++ng;
+    for (int f = 0, q = 0; f < n; ++f) {
+        run[f] = g->in[f];
+        if (!run[f]) continue;
+        V[q++] = g->S[f]->v;
+        if (g->S[f]->kcap > kmax) kmax = g->S[f]->kcap;
+        bytes = hbk_group_ws_bytes(q, V); /* the first round takes every family: the most virtual blocks */
     }
-    if (!ng) goto out;
-    const size_t bytes = hbk_group_ws_bytes(ng, V);
+    if (!bytes) goto out;
     if (pool_alloc(&ws, bytes, g->stream) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
         cudaEventCreate(&e1) != cudaSuccess) {
         lrc = HBICG_E_NOMEM;
         goto out;
     }
-    cudaEventRecord(e0, g->stream);
-    const int e = hbk_group_run(ng, A, V, H, cap, g->max_ctas, ws, bytes, &err, g->stream);
-    cudaEventRecord(e1, g->stream);
-    if (e || cudaStreamSynchronize(g->stream) != cudaSuccess) {
-        set_msg("shared launch: %s", hbk_error_string(e ? e : (int)cudaGetLastError()));
-        lrc = HBICG_E_CUDA;
-    } else if (err) {
-        set_msg("shared launch: %s",
-                err == HBK_GROUP_ERR_WAIT ? "a grid barrier's wait timed out" : "the iteration cap was reached");
-        lrc = HBICG_E_TIMEOUT;
+    /* a round advances every running family by a basis block or to its end */
+    for (;; ++rounds) {
+        int ng = 0, cap = 0, resumed = 0;
+        for (int f = 0; f < n; ++f) {
+            if (!run[f]) continue;
+            const hbicg_solver *s = g->S[f];
+            A[ng] = s->A->k;
+            V[ng] = s->v;
+            H[ng] = s->sh;
+            idx[ng] = f;
+            if (s->kcap > cap) cap = s->kcap;
+            ++ng;
+        }
+        if (!ng) break;
+        if (rounds > kmax + 64) {
+            set_msg("shared launch: no family finished after %d rounds", rounds);
+            lrc = HBICG_E_TIMEOUT;
+            break;
+        }
+        float ms = 0.f;
+        cudaEventRecord(e0, g->stream);
+        const int e = hbk_group_run(ng, A, V, H, cap, g->max_ctas, ws, bytes, &err, g->stream);
+        cudaEventRecord(e1, g->stream);
+        if (e || cudaStreamSynchronize(g->stream) != cudaSuccess) {
+            set_msg("shared launch: %s", hbk_error_string(e ? e : (int)cudaGetLastError()));
+            lrc = HBICG_E_CUDA;
+            break;
+        }
+        if (err) {
+            set_msg("shared launch: %s",
+                    err == HBK_GROUP_ERR_WAIT ? "a grid barrier's wait timed out" : "the iteration cap was reached");
+            lrc = HBICG_E_TIMEOUT;
+            break;
+        }
+        cudaEventElapsedTime(&ms, e0, e1);
+        total_ms += ms;
+        for (int q = 0; q < ng; ++q) {
+            const int f = idx[q];
+            hbicg_solver *s = g->S[f];
+            run_t *r = &g->R[f];
+            hbk_scalars *h = s->ctx->h_sc;
+            r->launches += 1;
+            cudaError_t ce = cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, s->ctx->stream);
+            if (!ce) ce = cudaStreamSynchronize(s->ctx->stream);
+            if (ce) {
+                set_msg("shared launch: %s", cudaGetErrorString(ce));
+                g->itrc[f] = HBICG_E_CUDA;
+                run[f] = 0;
+            } else if (h->finished && (h->status & HBK_ST_BASIS_FULL) && !(h->status & HBK_ST_BREAKDOWN)) {
+                g->itrc[f] = fused_pause_flush(s, &g->k_flushed[f], &r->launches, &r->flushes, &r->flush_ms);
+                run[f] = g->itrc[f] == HBICG_OK;
+                resumed += run[f];
+            } else {
+                run[f] = 0; /* converged, at max_iter or broken down */
+            }
+        }
+        if (!resumed) {
+            ++rounds;
+            break;
+        }
     }
-    cudaEventElapsedTime(&ms, e0, e1);
 out:
     if (ws) hbicg__dev_free(ws, g->stream);
     cudaStreamSynchronize(g->stream);
@@ -1403,8 +1484,11 @@ out:
     free(A);
     free(V);
     free(H);
+    free(idx);
+    free(run);
     g->lrc = lrc;
-    g->ms = ms;
+    g->ms = total_ms;
+    g->rounds = rounds;
     return lrc;
 }
 
@@ -1414,14 +1498,18 @@ int hbicg__group_finish(hbicg__group *g, int slot) {
     run_t *r = &g->R[slot];
     int rc = g->rc[slot];
     if (g->in[slot]) {
-        int it = g->lrc;
-        if (it == HBICG_OK) {
-            cudaStream_t st = s->ctx->stream;
-            cudaError_t ce = cudaMemcpyAsync(s->ctx->h_sc, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st);
-            if (!ce) ce = cudaStreamSynchronize(st);
-            it = ce ? HBICG_E_CUDA : fused_collect(s, r);
+        int it = g->lrc != HBICG_OK ? g->lrc : g->itrc[slot];
+        if (it == HBICG_OK) { /* the final flush reads this family's scalars (its context's copy may hold another's) */
+            cudaError_t ce = cudaMemcpyAsync(s->ctx->h_sc, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost,
+                                             s->ctx->stream);
+            if (!ce) ce = cudaStreamSynchronize(s->ctx->stream);
+            if (ce) {
+                set_msg("shared launch: %s", cudaGetErrorString(ce));
+                it = HBICG_E_CUDA;
+            }
         }
-        r->launches += 1;
+        if (it == HBICG_OK) it = fused_tail(s, g->k_flushed[slot], &r->launches, &r->flush_ms);
+        if (it == HBICG_OK) it = fused_collect(s, r);
         r->shared_ms = g->ms;
         rc = run_end(s, r, it);
     }

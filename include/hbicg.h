@@ -243,10 +243,13 @@ int hbicg_batch_solve(hbicg_family *fams, int count, const hbicg_params *p, int 
  * hbicg_batch_solve too): the families that take the incremental shift mode
  * (n m < 2^21 with shift_mode AUTO; no autotune, no residual output) run all
  * their iterations in one persistent launch on the GPU, set up and finished
- * by one host thread, while the workers take the other families. */
+ * by a few host threads, while the workers take the other families.
+ * persistent = 2: every such family whatever its shift mode (deferred-mode
+ * families pause in the launch at each full basis and are flushed between
+ * rounds of it); 0: every family on the workers. */
 typedef struct {
     int workers;                /* host workers for the other families (default 8) */
-    int persistent;             /* default 1 */
+    int persistent;             /* 0, 1 (default) or 2 */
     int persistent_ctas;        /* CTAs of the persistent launch; 0 = one wave of the GPU */
     const char *autotune_cache; /* as in hbicg_batch_solve */
 } hbicg_batch_opts;

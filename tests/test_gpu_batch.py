@@ -1,7 +1,9 @@
 """Batched families (hbicg_batch_solve) and the SpMV-form autotuner on the
-GPU: every family of a concurrent batch gets exactly the solve it gets alone;
-a failing family fails alone; the autotune cache is written once and read
-back; the manifest runner end to end."""
+GPU: through the workers every family gets exactly the solve it gets alone;
+through the shared persistent launch (both shift modes) every family meets
+the oracle (the reference's algorithm) on the same inputs; a failing family
+fails alone; config 4's own families against the oracle; the autotune cache
+is written once and read back; the manifest runner end to end."""
 import json
 
 import numpy as np
@@ -206,3 +208,50 @@ def test_config4_families_against_the_oracle(cuda, pkg, oracle):
         tr = oracle.true_residuals(f.a, r.x, f.b, f.sigma)
         tr_ref = oracle.true_residuals(f.a, want.x, f.b, f.sigma)
         assert np.all(tr <= np.maximum(f.tol * 1.02, 1.5 * tr_ref)), (f.name, tr.max(), tr_ref.max())
+
+
+def test_persistent_launch_deferred_families_against_the_oracle(cuda, pkg, oracle):
+    """Every family in the shared launch in the deferred shift mode (the
+    Krylov basis, paused at each full basis and flushed on the tensor cores
+    between rounds of the launch): every x_j within 1e-8 of the oracle's, k
+    within 2 % of its rounding envelope, the switch count, every shift's true
+    residual at tol or within 1.5x the reference's own; and within 1e-8 of the
+    same families solved one by one in the deferred mode."""
+    fams = _families(pkg, count=8, seed=9)
+    kw = dict(tol=1e-10, max_iter=10000, true_residuals=True, refine=False, shift_mode="deferred")
+    res, _ = pkg.batch_solve(fams, workers=2, persistent="all", **kw)
+    alone, _ = pkg.batch_solve(fams, workers=2, persistent=False, **kw)
+    assert max(r.k for r in res) > 2 * 28, "no family ran through a flush and resumed"
+    for f, r, a in zip(fams, res, alone):
+        assert r.status == 0, (f.name, r.status)
+        want = oracle.solve(f.a, f.b, f.sigma, seed=f.seed, tol=1e-10, max_iter=10000)
+        scale = np.max(np.abs(want.x))
+        assert np.max(np.abs(r.x - want.x)) < 1e-8 * scale, f.name
+        ks = _k_envelope(oracle, f, 1e-10, 10000)
+        lo, hi = min(ks), max(ks)
+        assert lo - max(1, int(0.02 * lo)) <= r.k <= hi + max(1, int(0.02 * hi)), (f.name, r.k, ks)
+        assert r.switches == len(want.switches)
+        tr_ref = oracle.true_residuals(f.a, want.x, f.b, f.sigma)
+        assert np.all(r.true_residual <= np.maximum(1e-10 * 1.02, 1.5 * tr_ref)), (f.name, r.max_true_residual)
+        assert np.max(np.abs(r.x - a.x)) < 1e-8 * scale
+
+
+def test_persistent_launch_deferred_switches(cuda, pkg):
+    """A family with two seed switches in the deferred mode inside the shared
+    launch (the new seed's p formed from the basis and its shift moved onto
+    the diagonal of the seed's SELL-32 copy, both within the launch): the
+    reference's switches, k within 2 % and x within 1e-8 of the reference's."""
+    import conftest
+
+    g = conftest.golden("stencil2d_two_switches")
+    sw = pkg.workloads.Family("sw", conftest.GoldenCsr(g), g["b"], g["sigma"], int(g["seed"]), float(g["tol"]),
+                              int(g["max_iter"]), {})
+    fams = [sw] + _families(pkg, count=3, seed=10)
+    res, _ = pkg.batch_solve(fams, workers=2, persistent="all", shift_mode="deferred", tol=float(g["tol"]),
+                             max_iter=int(g["max_iter"]), refine=False)
+    k_ref = int(g["k"])
+    assert res[0].status == 0 and res[0].switches == len(g["switches"]), (res[0].status, res[0].switches)
+    assert abs(res[0].k - k_ref) <= max(1, int(0.02 * k_ref)), (res[0].k, k_ref)
+    assert np.max(np.abs(res[0].x - g["x"])) < 1e-8 * np.max(np.abs(g["x"]))
+    for r in res[1:]:
+        assert r.status == 0
