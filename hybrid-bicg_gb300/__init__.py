@@ -312,14 +312,17 @@ def solve(a, b, sigma, seed=0, *, tol=1e-12, max_iter=2000, switching=True, form
     return _result(st, bufs, m, x, r, true_residuals)
 
 
-def adjoint(a, b, sigma, w, c, seed: int = 0, **kw) -> dict:
+def adjoint(a, b, sigma, w, c, seed: int = 0, same_context: bool = False, **kw) -> dict:
     """J = sum_j w_j c^T x_j for (A + sigma_j I) x_j = b and its gradients
     with respect to A's values (on its pattern), b and the shifts
-    (hbicg_adjoint: one forward family, one transposed family).  numpy in/out."""
+    (hbicg_adjoint: one forward family, one transposed family, at once on two
+    contexts; same_context: A^T made here on A's context, so the two families
+    run one after the other).  numpy in/out."""
     ptr, col, val = _csr_arrays(a)
     n, m = int(ptr.shape[0] - 1), len(sigma)
     ctx = Context()
     A = Matrix(ctx, ptr, col, val)
+    At = A.transpose() if same_context else None
     p = params(**kw)
     bb = np.ascontiguousarray(b, dtype=np.float64)
     sig = np.ascontiguousarray(sigma, dtype=np.float64)
@@ -327,8 +330,10 @@ def adjoint(a, b, sigma, w, c, seed: int = 0, **kw) -> dict:
     cc = np.ascontiguousarray(c, dtype=np.float64)
     J = C.c_double()
     dval, db, ds, x = np.zeros(int(ptr[-1])), np.zeros(n), np.zeros(m), np.zeros((m, n))
-    rc = lib().hbicg_adjoint(A.h, None, _ptr(bb), _ptr(sig), m, int(seed), _ptr(ww), _ptr(cc), C.byref(p), C.byref(J),
-                             _ptr(dval), _ptr(db), _ptr(ds), _ptr(x), None, None)
+    rc = lib().hbicg_adjoint(A.h, At.h if At is not None else None, _ptr(bb), _ptr(sig), m, int(seed), _ptr(ww),
+                             _ptr(cc), C.byref(p), C.byref(J), _ptr(dval), _ptr(db), _ptr(ds), _ptr(x), None, None)
+    if At is not None:
+        At.close()
     A.close()
     ctx.close()
     if rc not in (0, 4):

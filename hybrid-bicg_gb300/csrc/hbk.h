@@ -221,6 +221,10 @@ size_t hbk_group_ws_bytes(int nf, const hbk_vectors *v);
 int hbk_group_ctas(int max_ctas);
 int hbk_group_run(int nf, const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, int iter_cap, int max_ctas,
                   void *ws, size_t ws_bytes, int *err_out, cudaStream_t st);
+/* test of the bounded barrier wait: the next hbk_group_run's CTA 0 does not
+ * arrive at its first barrier, so every CTA waits out HBK_GROUP_WAIT_NS and
+ * the launch ends with HBK_GROUP_ERR_WAIT (one shot) */
+void hbk_group_test_withhold(int on);
 /* deferred mode: x_j (and p_j when keep_p) = coefficients x basis, then reset the basis */
 int hbk_deferred_flush(const hbk_vectors *v, const hbk_shifts *sh, int keep_p, cudaStream_t st);
 /* ||b - (A + sigma_j I) x_j||^2 for every shift into out[m] (device) */

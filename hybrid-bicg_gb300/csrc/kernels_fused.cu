@@ -906,14 +906,16 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // it, with release order; the others wait for it with acquire loads).  A wait
 // longer than HBK_GROUP_WAIT_NS sets *err; every CTA that sees *err leaves the
 // wait, so the launch ends (with the error) instead of hanging.  Returns
-// false in every thread of the CTA when the launch must stop.
-__device__ bool grid_barrier(unsigned *bar, int *err) {
+// false in every thread of the CTA when the launch must stop.  withhold:
+// this CTA waits without arriving (the bounded-wait test: every CTA then
+// waits out the bound, and the launch ends with HBK_GROUP_ERR_WAIT).
+__device__ bool grid_barrier(unsigned *bar, int *err, bool withhold = false) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
         const unsigned gen = ld_acquire_u32(bar + 1);
-        const unsigned arrived = atom_add_acq_rel_u32(bar, 1u) + 1u;
+        const unsigned arrived = withhold ? 0u : atom_add_acq_rel_u32(bar, 1u) + 1u;
         if (arrived == gridDim.x) {
             atomicExch(bar, 0u);
             st_release_u32(bar + 1, gen + 1u);
@@ -956,7 +958,7 @@ __device__ __forceinline__ void materialize_if_deferred(const Ctx &c, const VGri
 template <int MAXS>
 __global__ void __launch_bounds__(NT, 3) k_group(const GroupFam *__restrict__ fams, int nf,
                                                  const unsigned *__restrict__ vb_fam, unsigned nvb, unsigned *bar,
-                                                 int *err, int iter_cap, int any_deferred) {
+                                                 int *err, int iter_cap, int any_deferred, int withhold) {
 #define HBK_GROUP_STEP(body)                                                       \
     for (unsigned vb = blockIdx.x; vb < nvb; vb += gridDim.x) {                    \
         const GroupFam &F = fams[vb_fam[vb]];                                      \
@@ -969,7 +971,7 @@ __global__ void __launch_bounds__(NT, 3) k_group(const GroupFam *__restrict__ fa
         int alive = 0;
         for (int f = threadIdx.x; f < nf; f += NT) alive |= __ldcg(&fams[f].c.sh.sc->finished) == 0;
         alive = __syncthreads_or(alive);
-        if (!grid_barrier(bar, err) || !alive) return;
+        if (!grid_barrier(bar, err, withhold && it == 0 && blockIdx.x == 0) || !alive) return;
         HBK_GROUP_STEP(seed_s_body<HBK_FMT_SELL>)
         HBK_GROUP_STEP(seed_q_body)
         HBK_GROUP_STEP(seed_y_body<HBK_FMT_SELL>)
@@ -1085,6 +1087,11 @@ int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shi
     return (int)cudaGetLastError();
 }
 
+// the next shared launch's CTA 0 withholds its first barrier arrival (one
+// shot; for the test of the bounded wait)
+static int g_group_withhold = 0;
+void hbk_group_test_withhold(int on) { g_group_withhold = on ? 1 : 0; }
+
 static unsigned group_vblocks(unsigned n) {
     const unsigned v = (n + HBK_GROUP_ROWS - 1) / HBK_GROUP_ROWS;
     return v < 1 ? 1 : (v > HBK_MAX_GRID ? HBK_MAX_GRID : v);
@@ -1143,10 +1150,12 @@ int hbk_group_run(int nf, const hbk_matrix *A, const hbk_vectors *v, const hbk_s
     if ((e = (int)cudaMemcpyAsync(dmap, map.data(), sizeof(unsigned) * (size_t)nvb, cudaMemcpyHostToDevice, st)))
         return e;
     const int ctas = hbk_group_ctas(max_ctas);
+    int withhold = g_group_withhold;
+    g_group_withhold = 0;
     const GroupFam *a0 = dtab;
     const unsigned *a2 = dmap;
     void *args[] = {(void *)&a0,  (void *)&nf,  (void *)&a2,       (void *)&nvb,
-                    (void *)&bar, (void *)&err, (void *)&iter_cap, (void *)&any_deferred};
+                    (void *)&bar, (void *)&err, (void *)&iter_cap, (void *)&any_deferred, (void *)&withhold};
     if ((e = (int)cudaLaunchCooperativeKernel((const void *)k_group<64>, dim3(ctas), dim3(NT), args, 0, st))) return e;
     /* pageable destination: returns once the launch has finished */
     return (int)cudaMemcpyAsync(err_out, err, sizeof(int), cudaMemcpyDeviceToHost, st);

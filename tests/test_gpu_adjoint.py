@@ -168,3 +168,18 @@ def test_adjoint_finite_differences_128cubed(cuda, pkg):
     rel = errs / ans
     assert np.median(rel) <= 1e-7, np.median(rel)
     assert np.all((rel <= 1e-6) | (ans < 0.05 * rms)), list(zip(rel, ans))
+
+
+def test_adjoint_families_at_once_equal_one_after_the_other(cuda, pkg):
+    """hbicg_adjoint runs the transposed family on a second context and host
+    thread beside the forward family; with A^T on A's own context the two run
+    one after the other.  Every grid and summation order is fixed by the
+    matrix and the device, so both give the same bits."""
+    a, b, sigma, w, c = _problem(pkg, side=24, m=12, seed=13)
+    kw = dict(seed=0, tol=1e-11, max_iter=10000)
+    at_once = pkg.adjoint(a, b, sigma, w, c, **kw)
+    in_turn = pkg.adjoint(a, b, sigma, w, c, same_context=True, **kw)
+    assert at_once["status"] == in_turn["status"] == 0
+    assert at_once["J"] == in_turn["J"]
+    for key in ("dval", "db", "dsigma", "x"):
+        assert np.array_equal(at_once[key], in_turn[key]), key

@@ -255,3 +255,22 @@ def test_persistent_launch_deferred_switches(cuda, pkg):
     assert np.max(np.abs(res[0].x - g["x"])) < 1e-8 * np.max(np.abs(g["x"]))
     for r in res[1:]:
         assert r.status == 0
+
+
+def test_persistent_launch_bounded_wait(cuda, pkg):
+    """The shared launch's grid barrier never hangs: when a CTA does not
+    arrive (here CTA 0 withholds its first arrival, through the test hook),
+    every CTA waits out the bound (2 s), the launch ends, and each family of
+    it reports HBICG_E_TIMEOUT (6); the GPU context stays usable and the next
+    batch solves normally."""
+    fams = _families(pkg, count=3, seed=11)
+    kw = dict(tol=1e-10, max_iter=10000, persistent=True)
+    pkg.lib().hbk_group_test_withhold(1)
+    try:
+        res, wall = pkg.batch_solve(fams, workers=2, **kw)
+    finally:
+        pkg.lib().hbk_group_test_withhold(0)
+    assert [r.status for r in res] == [6, 6, 6]
+    assert 1.5 < wall < 30.0
+    res, _ = pkg.batch_solve(fams, workers=2, **kw)
+    assert all(r.status == 0 for r in res)
