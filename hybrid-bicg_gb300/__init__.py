@@ -207,8 +207,10 @@ def params(tol=1e-12, max_iter=2000, switching=True, form="fused", shift_mode="a
     p.switching = 1 if switching else 0
     p.form = FORMS[form]
     p.shift_mode = SHIFT_MODES[shift_mode]
-    # True: graphs of iteration chunks; "loop": one graph with a device-side loop
-    p.use_graph = 2 if use_graph == "loop" else (1 if use_graph else 0)
+    # True: graphs of iteration chunks; "loop": one graph with a device-side
+    # loop; "persistent": one persistent cooperative launch per solve
+    p.use_graph = {"loop": 2, "persistent": 3}.get(use_graph, 1 if use_graph else 0) if isinstance(use_graph, str) \
+        else (1 if use_graph else 0)
     p.graph_chunk = int(graph_chunk)
     if basis_mem_frac:
         p.basis_mem_frac = float(basis_mem_frac)

@@ -206,21 +206,24 @@ int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shi
  * loop_cap bodies (a bound on the loop whatever the scalars say) */
 int hbk_loop_condition(const hbk_shifts *sh, cudaGraphConditionalHandle cond, int loop_cap, cudaStream_t st);
 /* Many families' iterations in one persistent cooperative launch: every
- * family in the fused form, incremental shift mode, SELL-32, already set up
- * by hbk_fused_init; the launch runs until every family has stopped (or
- * iter_cap iterations).  A[f], v[f], sh[f] describe family f; ws: device
- * memory of hbk_group_ws_bytes(nf, v) bytes; max_ctas > 0 caps the CTAs
- * (else one wave, hbk_group_ctas(0)).  Returns after the launch has ended;
- * *err_out: 0, HBK_GROUP_ERR_WAIT (a grid barrier's wait ran out) or
- * HBK_GROUP_ERR_CAP (iter_cap reached with a family still running). */
-#define HBK_GROUP_ROWS 1024              /* rows of a family per virtual block */
+ * family in the fused form on SELL-32, either shift mode, already set up by
+ * hbk_fused_init; the launch runs until every family has stopped or paused
+ * with a full basis (or iter_cap iterations).  A[f], v[f], sh[f] describe
+ * family f; rows_per_vb: rows of a family per virtual block (0:
+ * HBK_GROUP_ROWS); ws: device memory of hbk_group_ws_bytes(nf, v,
+ * rows_per_vb) bytes; max_ctas > 0 caps the CTAs (else one wave,
+ * hbk_group_ctas(0); never more than the virtual blocks).  Returns after the
+ * launch has ended; *err_out: 0, HBK_GROUP_ERR_WAIT (a grid barrier's wait
+ * ran out) or HBK_GROUP_ERR_CAP (iter_cap reached with a family still
+ * running). */
+#define HBK_GROUP_ROWS 1024              /* default rows of a family per virtual block */
 #define HBK_GROUP_WAIT_NS 2000000000ull  /* longest wait at a grid barrier */
 #define HBK_GROUP_ERR_WAIT 1
 #define HBK_GROUP_ERR_CAP 2
-size_t hbk_group_ws_bytes(int nf, const hbk_vectors *v);
+size_t hbk_group_ws_bytes(int nf, const hbk_vectors *v, unsigned rows_per_vb);
 int hbk_group_ctas(int max_ctas);
 int hbk_group_run(int nf, const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, int iter_cap, int max_ctas,
-                  void *ws, size_t ws_bytes, int *err_out, cudaStream_t st);
+                  unsigned rows_per_vb, void *ws, size_t ws_bytes, int *err_out, cudaStream_t st);
 /* test of the bounded barrier wait: the next hbk_group_run's CTA 0 does not
  * arrive at its first barrier, so every CTA waits out HBK_GROUP_WAIT_NS and
  * the launch ends with HBK_GROUP_ERR_WAIT (one shot) */

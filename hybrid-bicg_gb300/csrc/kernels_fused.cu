@@ -1092,8 +1092,9 @@ int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shi
 static int g_group_withhold = 0;
 void hbk_group_test_withhold(int on) { g_group_withhold = on ? 1 : 0; }
 
-static unsigned group_vblocks(unsigned n) {
-    const unsigned v = (n + HBK_GROUP_ROWS - 1) / HBK_GROUP_ROWS;
+static unsigned group_vblocks(unsigned n, unsigned rows) {
+    if (rows == 0) rows = HBK_GROUP_ROWS;
+    const unsigned v = (n + rows - 1) / rows;
     return v < 1 ? 1 : (v > HBK_MAX_GRID ? HBK_MAX_GRID : v);
 }
 
@@ -1103,9 +1104,9 @@ static size_t group_bytes(int nf, size_t nvb) {
     return kGroupHead + ((sizeof(GroupFam) * (size_t)nf + 255) / 256) * 256 + sizeof(unsigned) * nvb;
 }
 
-size_t hbk_group_ws_bytes(int nf, const hbk_vectors *v) {
+size_t hbk_group_ws_bytes(int nf, const hbk_vectors *v, unsigned rows_per_vb) {
     size_t nvb = 0;
-    for (int f = 0; f < nf; ++f) nvb += group_vblocks(v[f].n);
+    for (int f = 0; f < nf; ++f) nvb += group_vblocks(v[f].n, rows_per_vb);
     return group_bytes(nf, nvb);
 }
 
@@ -1118,7 +1119,7 @@ int hbk_group_ctas(int max_ctas) {
 }
 
 int hbk_group_run(int nf, const hbk_matrix *A, const hbk_vectors *v, const hbk_shifts *sh, int iter_cap, int max_ctas,
-                  void *ws, size_t ws_bytes, int *err_out, cudaStream_t st) {
+                  unsigned rows_per_vb, void *ws, size_t ws_bytes, int *err_out, cudaStream_t st) {
     *err_out = 0;
     if (nf <= 0) return 0;
     int dev = 0, coop = 0;
@@ -1133,7 +1134,7 @@ int hbk_group_run(int nf, const hbk_matrix *A, const hbk_vectors *v, const hbk_s
         any_deferred |= v[f].deferred != 0;
         tab[f].c = make_ctx(&A[f], &v[f], &sh[f]);
         tab[f].vb0 = (unsigned)map.size();
-        tab[f].nvb = group_vblocks(v[f].n);
+        tab[f].nvb = group_vblocks(v[f].n, rows_per_vb);
         map.insert(map.end(), tab[f].nvb, (unsigned)f);
     }
     const unsigned nvb = (unsigned)map.size();
@@ -1149,7 +1150,8 @@ int hbk_group_run(int nf, const hbk_matrix *A, const hbk_vectors *v, const hbk_s
         return e;
     if ((e = (int)cudaMemcpyAsync(dmap, map.data(), sizeof(unsigned) * (size_t)nvb, cudaMemcpyHostToDevice, st)))
         return e;
-    const int ctas = hbk_group_ctas(max_ctas);
+    int ctas = hbk_group_ctas(max_ctas);
+    if ((unsigned)ctas > nvb) ctas = (int)nvb; /* a CTA without a virtual block would only wait at barriers */
     int withhold = g_group_withhold;
     g_group_withhold = 0;
     const GroupFam *a0 = dtab;

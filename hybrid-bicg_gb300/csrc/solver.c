@@ -845,11 +845,66 @@ static int fused_tail(hbicg_solver *s, int k_flushed, int *launches, double *flu
     return HBICG_OK;
 }
 
+/* params.use_graph = 3: the whole solve as one persistent cooperative launch
+ * of the shared-launch kernel (hbk_group_run) with this one family, in
+ * rounds of one basis block in the deferred mode; its rows are cut into
+ * virtual blocks so that about two per SM exist (256..1024 rows each).
+ * Measured on GB300 it does not beat the graphs of the default: 5.3 against
+ * 5.0 ms on the 32^3 family, 10.3 against 8.4 ms at 48^3, 15.9 against
+ * 15.2 ms at 64^3 (deferred): a step's own latency, not the kernel boundary,
+ * sets an iteration's length at these sizes, and a grid barrier costs about
+ * what a boundary inside a graph does. */
+static int run_persistent(hbicg_solver *s, int *launches, int *flushes, double *flush_ms) {
+    cudaStream_t st = s->ctx->stream;
+    hbk_scalars *h = s->ctx->h_sc;
+    const unsigned n = s->A->k.n;
+    const unsigned want = (n + 2u * (unsigned)hbk_device_sm_count() - 1u) / (2u * (unsigned)hbk_device_sm_count());
+    const unsigned rows = want <= 256u ? 256u : (want >= 1024u ? 1024u : (want + 255u) / 256u * 256u);
+    const size_t bytes = hbk_group_ws_bytes(1, &s->v, rows);
+    void *ws = NULL;
+    int rc = HBICG_OK, k_flushed = 0;
+    CUDA_TRY(pool_alloc(&ws, bytes, st));
+    for (int round = 0;; ++round) {
+        if (round > s->kcap + 64) {
+            set_msg("persistent launch: no progress after %d rounds", round);
+            rc = HBICG_E_TIMEOUT;
+            break;
+        }
+        int err = 0;
+        const int e = hbk_group_run(1, &s->A->k, &s->v, &s->sh, s->kcap, 0, rows, ws, bytes, &err, st);
+        ++*launches;
+        if (e) {
+            set_msg("persistent launch: %s", hbk_error_string(e));
+            rc = HBICG_E_CUDA;
+            break;
+        }
+        if (err) {
+            set_msg("persistent launch: %s",
+                    err == HBK_GROUP_ERR_WAIT ? "a grid barrier's wait timed out" : "the iteration cap was reached");
+            rc = HBICG_E_TIMEOUT;
+            break;
+        }
+        cudaError_t ce = cudaMemcpyAsync(h, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost, st);
+        if (!ce) ce = cudaStreamSynchronize(st);
+        if (ce) {
+            set_msg("persistent launch: %s", cudaGetErrorString(ce));
+            rc = HBICG_E_CUDA;
+            break;
+        }
+        if (!(h->finished && (h->status & HBK_ST_BASIS_FULL) && !(h->status & HBK_ST_BREAKDOWN))) break;
+        if ((rc = fused_pause_flush(s, &k_flushed, launches, flushes, flush_ms)) != HBICG_OK) break;
+    }
+    hbicg__dev_free(ws, st);
+    if (rc) return rc;
+    return fused_tail(s, k_flushed, launches, flush_ms);
+}
+
 static int run_fused(hbicg_solver *s, int seed, int *launches, int *flushes, double *flush_ms) {
     cudaStream_t st = s->ctx->stream;
     hbk_scalars *h = s->ctx->h_sc;
     int rc0 = fused_init(s, seed, launches);
     if (rc0) return rc0;
+    if (s->p.use_graph == 3 && s->A->k.fmt == HBK_FMT_SELL && s->m > 0) return run_persistent(s, launches, flushes, flush_ms);
     const int use_graph = s->p.use_graph;
     /* every launch of a chunk advances k by chunk unless the solve ends or
      * the basis pauses it; bound the host loop all the same */
@@ -1407,7 +1462,7 @@ int hbicg__group_launch(hbicg__group *g) {
         if (!run[f]) continue;
         V[q++] = g->S[f]->v;
         if (g->S[f]->kcap > kmax) kmax = g->S[f]->kcap;
-        bytes = hbk_group_ws_bytes(q, V); /* the first round takes every family: the most virtual blocks */
+        bytes = hbk_group_ws_bytes(q, V, 0); /* the first round takes every family: the most virtual blocks */
     }
     if (!bytes) goto out;
     if (pool_alloc(&ws, bytes, g->stream) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
@@ -1436,7 +1491,7 @@ int hbicg__group_launch(hbicg__group *g) {
         }
         float ms = 0.f;
         cudaEventRecord(e0, g->stream);
-        const int e = hbk_group_run(ng, A, V, H, cap, g->max_ctas, ws, bytes, &err, g->stream);
+        const int e = hbk_group_run(ng, A, V, H, cap, g->max_ctas, 0, ws, bytes, &err, g->stream);
         cudaEventRecord(e1, g->stream);
         if (e || cudaStreamSynchronize(g->stream) != cudaSuccess) {
             set_msg("shared launch: %s", hbk_error_string(e ? e : (int)cudaGetLastError()));

@@ -54,7 +54,9 @@ typedef struct {
     int use_graph;         /* fused form: 0 = eager launches; 1 = CUDA graphs of graph_chunk iterations, the
                               host checks the scalars after each (default); 2 = one graph whose conditional
                               while node loops over iterations until the solve stops (chunks where the
-                              runtime refuses it) */
+                              runtime refuses it); 3 = the whole solve as one persistent cooperative launch
+                              (grid barriers between the steps; in the deferred mode one launch per basis
+                              block, SELL-32 matrices; other forms use 1) */
     int graph_chunk;       /* iterations per graph launch, 0 = automatic */
     double basis_mem_frac; /* deferred mode: share of free device memory for the basis (default 0.6) */
     int true_residuals;    /* compute ||b-(A+sigma_j I)x_j||/||b|| after the solve (default 0) */

@@ -26,8 +26,11 @@ MODES = [
     dict(form="fused", shift_mode="deferred"),
     dict(form="fused", shift_mode="incremental", use_graph=False),
     dict(form="fused", shift_mode="deferred", use_graph=False),
+    dict(form="fused", shift_mode="incremental", use_graph="persistent"),
+    dict(form="fused", shift_mode="deferred", use_graph="persistent"),
 ]
-MODE_IDS = ["plain", "fused-inc", "fused-def", "fused-inc-eager", "fused-def-eager"]
+MODE_IDS = ["plain", "fused-inc", "fused-def", "fused-inc-eager", "fused-def-eager", "fused-inc-persistent",
+            "fused-def-persistent"]
 
 
 def k_close(k, want):
@@ -111,7 +114,7 @@ def c1_envelope(seed):
 
 
 @pytest.mark.parametrize("seed", [0, 15])
-@pytest.mark.parametrize("mode", MODES[:3], ids=MODE_IDS[:3])
+@pytest.mark.parametrize("mode", MODES[:3] + MODES[5:], ids=MODE_IDS[:3] + MODE_IDS[5:])
 def test_c1_full(cuda, pkg, oracle, seed, mode):
     f = pkg.workloads.family("c1")
     want = oracle.solve(f.a, f.b, f.sigma, seed=seed, tol=f.tol, max_iter=f.max_iter)
