@@ -141,6 +141,7 @@ static void *group_part(void *arg) {
         G->st[i].true_residual = f->true_residual;
         if (hbicg__group_eligible(G->S[i])) {
             G->slot[i] = hbicg__group_add(G->g, G->S[i], f->b, f->sigma, f->seed, f->x, &G->st[i]);
+            if (G->slot[i] < 0) f->status = HBICG_E_ARG; /* no room in the shared launch (not expected) */
         } else { /* another form after all (e.g. rows too long for SELL-32): a solve of its own */
             f->status = hbicg_solver_run(G->S[i], f->b, f->sigma, f->seed, HBICG_HOST, f->x, f->r, HBICG_HOST,
                                          &G->st[i]);
