@@ -185,3 +185,15 @@ def test_noalloc_wrapper_rejects_bad_tensors(pkg):
     wide = torch.zeros(m, n + 6, **f64)
     with pytest.raises(ValueError, match="CUDA"):
         pkg._check_noalloc_args(n, wide, ok["b"], ok["sigma"], ok["res"])
+
+
+def test_batch_options_and_graph_modes_on_the_host(pkg):
+    """The batch options' defaults (hbicg_batch_opts_default) and the Python
+    mapping of the graph and shared-launch modes onto the C parameters."""
+    o = pkg.BatchOpts()
+    pkg.lib().hbicg_batch_opts_default(C.byref(o))
+    assert (o.workers, o.persistent, o.persistent_ctas, o.autotune_cache) == (8, 1, 0, None)
+    assert pkg.params().use_graph == 1
+    assert [pkg.params(use_graph=v).use_graph for v in (False, True, "loop", "persistent")] == [0, 1, 2, 3]
+    p = pkg.params()
+    assert (p.basis_block, p.refine, p.shift_mode) == (0, 1, 0)
