@@ -290,9 +290,14 @@ __device__ __forceinline__ void spmv_rows_hyb(const hbk_matrix &A, const double 
 // the sum of its pieces (each an FMA chain in stored order) over a fixed
 // shuffle tree.  The row values are then written to shared memory and
 // `epi(row, acc)` runs once per row, in row order across the lanes.
+// Item e of a block (and row q's value) sits at e + e / 8: one pad slot per 8
+// items, so that the walk, where lane l reads items 8 l .. 8 l + 7, reads
+// 72 bytes apart across lanes (no shared-memory bank conflicts) instead of 64.
+__device__ __forceinline__ unsigned merge_pad(unsigned e) { return e + (e >> 3); }
+constexpr int MERGE_PADDED = HBK_MERGE_ITEMS + HBK_MERGE_ITEMS / 8;
 struct MergeWarpSmem {
-    double val[HBK_MERGE_ITEMS];
-    double xv[HBK_MERGE_ITEMS];      // gathered x; after the walk, the rows' values
+    double val[MERGE_PADDED];
+    double xv[MERGE_PADDED];         // gathered x; after the walk, the rows' values
     unsigned rend[HBK_MERGE_ITEMS];  // end of each row of the block, relative to its first nonzero
 };
 struct MergeSmem {
@@ -352,8 +357,8 @@ __device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const doubl
             for (int k = 0; k < IPT; ++k) {
                 const unsigned e = lane + 32u * k;
                 if (e < nz) {
-                    ws.xv[e] = __ldg(x + c[k]);
-                    ws.val[e] = v[k];
+                    ws.xv[merge_pad(e)] = __ldg(x + c[k]);
+                    ws.val[merge_pad(e)] = v[k];
                 }
                 if (e < nr) ws.rend[e] = re[k] - e0;
             }
@@ -395,7 +400,7 @@ __device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const doubl
                 open = false;
                 ++i;
             } else if (valid) {
-                acc = fma(ws.val[e], ws.xv[e], acc);
+                acc = fma(ws.val[merge_pad(e)], ws.xv[merge_pad(e)], acc);
                 ++e;
                 open = true;
             }
@@ -422,10 +427,10 @@ __device__ __forceinline__ void spmv_rows_merge(const hbk_matrix &A, const doubl
         __syncwarp();  // every lane is done with the staged values
 #pragma unroll
         for (int q = 0; q < IPT; ++q)
-            if (rr[q] != kNoRow) ws.xv[rr[q]] = rv[q];
-        if (head_row != kNoRow) ws.xv[head_row] = ((lane > 0 && pk == head_row) ? ps : 0.0) + head_v;
+            if (rr[q] != kNoRow) ws.xv[merge_pad(rr[q])] = rv[q];
+        if (head_row != kNoRow) ws.xv[merge_pad(head_row)] = ((lane > 0 && pk == head_row) ? ps : 0.0) + head_v;
         __syncwarp();
-        for (unsigned q = lane; q < nr; q += 32) epi(r0 + q, ws.xv[q]);
+        for (unsigned q = lane; q < nr; q += 32) epi(r0 + q, ws.xv[merge_pad(q)]);
         __syncwarp();  // before the next unit overwrites this warp's staging
     }
 }
