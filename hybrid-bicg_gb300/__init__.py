@@ -535,6 +535,8 @@ class Matrix:
 
     def time_spmv(self, x, y, sigma: float = 0.0, iters: int = 20) -> float:
         """Mean milliseconds per SpMV launch (device tensors), CUDA events on the context stream."""
+        if isinstance(x, np.ndarray) or isinstance(y, np.ndarray):
+            raise TypeError("time_spmv takes device tensors; spmv takes host arrays")
         ms = C.c_double()
         _check(lib().hbicg_matrix_time_spmv(self.h, _ptr(x), _ptr(y), float(sigma), int(iters), C.byref(ms)),
                "hbicg_matrix_time_spmv")

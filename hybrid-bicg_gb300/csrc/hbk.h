@@ -41,7 +41,7 @@ extern "C" {
 #define HBK_SELL_MAX_LEN 64  /* longest row the SELL format takes */
 #define HBK_FMT_HYB 2        /* short rows in SELL-32 slices (length-sorted inside windows), long rows one warp each */
 #define HBK_HYB_SHORT 32     /* longest row of a HYB slice */
-#define HBK_HYB_WINDOW 256   /* rows are sorted by length only inside windows of this many consecutive rows */
+#define HBK_HYB_WINDOW 1024  /* rows are sorted by length only inside windows of this many consecutive rows */
 #define HBK_FMT_MERGE 3      /* CSR; rows up to HBK_MERGE_LONG entries in merge-path blocks, longer rows one warp each */
 #define HBK_MERGE_IPT 8      /* merge items (row ends + nonzeros) per lane of a block */
 #define HBK_MERGE_ITEMS (32 * HBK_MERGE_IPT) /* items per block (one warp) */
@@ -65,6 +65,10 @@ typedef struct {
     unsigned nslice;           /* HYB: slices of short rows */
     const unsigned *wrow;      /* HYB: rows longer than HBK_HYB_SHORT, longest first, one warp each */
     unsigned nwrow;
+    const unsigned *wrng;      /* HYB: first and end entry of long row i at 2 i, 2 i + 1 */
+    const unsigned *hwbeg;     /* HYB: work list of warp w = items hitem[hwbeg[w] .. hwbeg[w + 1]) */
+    const unsigned *hitem;     /* HYB: item i < nwrow is long row i, else slice i - nwrow */
+    unsigned hnw;              /* HYB: warps the lists were balanced for */
     const unsigned *mblk;      /* MERGE: [2 nmblk] first and end row of each block of short rows */
     unsigned nmblk;
     const unsigned *mlong;     /* MERGE: rows longer than HBK_MERGE_LONG, longest first, one warp each */
@@ -184,6 +188,9 @@ int hbk_merge_grid(unsigned units);
 /* SELL-32 build on the device: widths of the ceil(n/32) slices into w ... */
 int hbk_sell_widths(unsigned n, const unsigned *ptr, unsigned *w, cudaStream_t st);
 /* ... then, with sptr = exclusive prefix sum of 32*w (host), fill the arrays */
+/* one-wave grid (blocks) of the kernels that take the HYB form */
+int hbk_hyb_wave_fused(void);
+int hbk_hyb_wave_blas(void);
 /* HYB slices: slice s, lane l holds row srow[32 s + l] (entry e at sptr[s] + 32 e + l) */
 int hbk_hyb_fill(unsigned nslice, const unsigned *srow, unsigned n, const unsigned *ptr, const unsigned *col,
                  const double *val, const unsigned long long *sptr, double *sval, unsigned *scol, cudaStream_t st);

@@ -233,41 +233,48 @@ __device__ __forceinline__ void spmv_rows_tile(const hbk_matrix &A, const double
     }
 }
 
-// HYB path: persistent warps over work items; the first nwrow items are the
-// long rows (longest first), one warp each: lanes take every 32nd entry in
-// stored order and the 32 partial sums meet in a fixed shuffle tree.  The
-// rest are SELL-32 slices of short rows, one warp each, whose 32 rows were
-// sorted by length inside a window of HBK_HYB_WINDOW rows, so the lanes of a
-// warp have similar row lengths (an FP64 instruction costs the same whatever
-// its active lanes); each short row is summed in stored order with FMAs from
-// 0, as in the other paths.
+// HYB path: persistent warps over work items: the long rows (more than
+// HBK_HYB_SHORT entries), one warp each: lanes take every 32nd entry in stored
+// order and the 32 partial sums meet in a fixed shuffle tree; and SELL-32
+// slices of short rows, one warp each, whose 32 rows were sorted by length
+// inside a window of HBK_HYB_WINDOW rows, so the lanes of a warp have similar
+// row lengths (an FP64 instruction costs the same whatever its active lanes);
+// each short row is summed in stored order with FMAs from 0, as in the other
+// paths.  The host deals the items to A.hnw warp lists, longest first, each to
+// the list with the least work so far (cost: a header plus one step per 32
+// entries of a long row or per entry of a slice), so no warp is left with
+// several of the longest rows; warp w of the grid runs lists w, w + (warps of
+// the grid), ...  A row's arithmetic does not depend on the list it is in.
 template <class Epi>
 __device__ __forceinline__ void spmv_rows_hyb(const hbk_matrix &A, const double *__restrict__ x, Epi &epi) {
     const unsigned lane = threadIdx.x & 31;
     const unsigned nw = (gridDim.x * NT) >> 5;
-    const unsigned items = A.nwrow + A.nslice;
-    for (unsigned it = (blockIdx.x * NT + threadIdx.x) >> 5; it < items; it += nw) {
-        if (it < A.nwrow) {
-            const unsigned r = __ldg(A.wrow + it);
-            const unsigned e1 = __ldg(A.ptr + r + 1);
-            double acc = 0.0;
-            for (unsigned e = __ldg(A.ptr + r) + lane; e < e1; e += 32)
-                acc = fma(__ldg(A.val + e), __ldg(x + __ldg(A.col + e)), acc);
-            acc = warp_sum(acc);
-            if (lane == 0) epi(r, acc);
-        } else {
-            const unsigned s = it - A.nwrow;
-            const unsigned long long base = __ldg(A.sptr + s);
-            const unsigned w = (unsigned)((__ldg(A.sptr + s + 1) - base) >> 5);
-            const unsigned r = __ldg(A.srow + 32 * (size_t)s + lane);
-            const unsigned len = __ldg(A.slen + 32 * (size_t)s + lane);
-            const double *__restrict__ vv = A.sval + base + lane;
-            const unsigned *__restrict__ cc = A.scol + base + lane;
-            double acc = 0.0;
+    for (unsigned w = (blockIdx.x * NT + threadIdx.x) >> 5; w < A.hnw; w += nw) {
+        const unsigned k1 = __ldg(A.hwbeg + w + 1);
+        for (unsigned k = __ldg(A.hwbeg + w); k < k1; ++k) {
+            const unsigned it = __ldg(A.hitem + k);
+            if (it < A.nwrow) {
+                const uint2 rg = __ldg(reinterpret_cast<const uint2 *>(A.wrng) + it);
+                const unsigned r = __ldg(A.wrow + it);
+                double acc = 0.0;
+                for (unsigned e = rg.x + lane; e < rg.y; e += 32)
+                    acc = fma(__ldg(A.val + e), __ldg(x + __ldg(A.col + e)), acc);
+                acc = warp_sum(acc);
+                if (lane == 0) epi(r, acc);
+            } else {
+                const unsigned s = it - A.nwrow;
+                const unsigned long long base = __ldg(A.sptr + s);
+                const unsigned wd = (unsigned)((__ldg(A.sptr + s + 1) - base) >> 5);
+                const unsigned r = __ldg(A.srow + 32 * (size_t)s + lane);
+                const unsigned len = __ldg(A.slen + 32 * (size_t)s + lane);
+                const double *__restrict__ vv = A.sval + base + lane;
+                const unsigned *__restrict__ cc = A.scol + base + lane;
+                double acc = 0.0;
 #pragma unroll 4
-            for (unsigned e = 0; e < w; ++e)
-                if (e < len) acc = fma(__ldg(vv + 32 * (size_t)e), __ldg(x + __ldg(cc + 32 * (size_t)e)), acc);
-            if (r < A.n) epi(r, acc);
+                for (unsigned e = 0; e < wd; ++e)
+                    if (e < len) acc = fma(__ldg(vv + 32 * (size_t)e), __ldg(x + __ldg(cc + 32 * (size_t)e)), acc);
+                if (r < A.n) epi(r, acc);
+            }
         }
     }
 }

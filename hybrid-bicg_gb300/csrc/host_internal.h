@@ -41,6 +41,8 @@ struct hbicg_matrix {
     size_t slen_off;                    /* entries of the map before the lengths */
     unsigned long long *d_hsptr;
     unsigned nslice, nwrow;
+    unsigned hnw;  /* warp work lists in d_wrow (after the long rows' entry ranges and the long rows) */
+    int hyb_grid;  /* blocks of the HYB kernels: one list per warp */
     /* MERGE form (hbk.h HBK_FMT_MERGE): block row ranges, then the long rows,
      * in one allocation */
     unsigned *d_merge;

@@ -281,6 +281,13 @@ int hbk_spmv_grid(unsigned nblk) {
     return g < 1 ? 1 : g;
 }
 
+int hbk_hyb_wave_blas(void) {
+    int g = wave_grid<k_spmv<HBK_FMT_HYB>>(HBK_MAX_GRID);
+    const int a = wave_grid<k_spmv_acc<HBK_FMT_HYB>>(HBK_MAX_GRID), t = wave_grid<k_true_res<HBK_FMT_HYB>>(HBK_MAX_GRID);
+    if (a < g) g = a;
+    return t < g ? t : g;
+}
+
 // MERGE form: one wave of the product kernel (its units are dealt round-robin,
 // so a second wave would wait for whole CTAs of the first)
 int hbk_merge_grid(unsigned units) {

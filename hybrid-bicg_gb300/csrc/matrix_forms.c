@@ -20,6 +20,75 @@ static int cmp_u64(const void *a, const void *b) {
     return x < y ? -1 : x > y;
 }
 
+/* HYB work lists.  Items: long row i (i < nw, in the order of wrow), then
+ * slice s (item nw + s).  Cost of an item: a header of 2 (long row) or 3
+ * (slice: offsets, row map and lengths) plus one step per 32 entries of a long
+ * row or per entry of the slice's longest row.  The items are dealt in order
+ * of decreasing cost (ties: lower item first), each to the list with the least
+ * cost so far (ties: lower list), and every list keeps the order of dealing.
+ * hwbeg[hnw + 1], hitem[nw + ns]. */
+typedef struct {
+    unsigned long long load;
+    unsigned w;
+} hyb_slot;
+
+static int slot_less(const hyb_slot *a, const hyb_slot *b) {
+    return a->load < b->load || (a->load == b->load && a->w < b->w);
+}
+
+static int hyb_plan(size_t nw, const unsigned *wlen, size_t ns, const unsigned long long *sp, unsigned hnw,
+                    unsigned *hwbeg, unsigned *hitem) {
+    const size_t ni = nw + ns;
+    unsigned long long *key = malloc(sizeof *key * (ni + 1));
+    hyb_slot *h = malloc(sizeof *h * hnw);
+    unsigned *owner = malloc(sizeof *owner * (ni + 1));
+    unsigned *pos = malloc(sizeof *pos * hnw);
+    if (!key || !h || !owner || !pos) {
+        free(key);
+        free(h);
+        free(owner);
+        free(pos);
+        return HBICG_E_NOMEM;
+    }
+    for (size_t i = 0; i < ni; ++i) {
+        const unsigned long long c =
+            i < nw ? 2ull + (wlen[i] + 31ull) / 32 : 3ull + (sp[i - nw + 1] - sp[i - nw]) / 32;
+        key[i] = ((0xFFFFFFFFull - c) << 32) | i; /* costliest first, then by item */
+    }
+    qsort(key, ni, sizeof *key, cmp_u64);
+    for (unsigned w = 0; w < hnw; ++w) h[w] = (hyb_slot){0, w}; /* all zero: a valid heap */
+    memset(hwbeg, 0, sizeof *hwbeg * ((size_t)hnw + 1));
+    for (size_t k = 0; k < ni; ++k) {
+        const unsigned i = (unsigned)(key[k] & 0xFFFFFFFFu);
+        owner[i] = h[0].w;
+        hwbeg[h[0].w + 1]++;
+        h[0].load += 0xFFFFFFFFull - (key[k] >> 32);
+        for (size_t p = 0;;) { /* sift the grown root down */
+            const size_t l = 2 * p + 1, r = l + 1;
+            size_t m = p;
+            if (l < hnw && slot_less(&h[l], &h[m])) m = l;
+            if (r < hnw && slot_less(&h[r], &h[m])) m = r;
+            if (m == p) break;
+            const hyb_slot t = h[p];
+            h[p] = h[m];
+            h[m] = t;
+            p = m;
+        }
+    }
+    for (unsigned w = 0; w < hnw; ++w) hwbeg[w + 1] += hwbeg[w];
+    /* fill each list in the order of dealing */
+    memcpy(pos, hwbeg, sizeof *pos * hnw);
+    for (size_t k = 0; k < ni; ++k) {
+        const unsigned i = (unsigned)(key[k] & 0xFFFFFFFFu);
+        hitem[pos[owner[i]]++] = i;
+    }
+    free(key);
+    free(h);
+    free(owner);
+    free(pos);
+    return HBICG_OK;
+}
+
 /* HYB: rows of at most HBK_HYB_SHORT entries in SELL-32 slices, sorted by
  * length (longest first, stable) inside windows of HBK_HYB_WINDOW consecutive
  * rows, so that the 32 rows of a slice have similar lengths and the rows a
@@ -28,7 +97,9 @@ static int cmp_u64(const void *a, const void *b) {
  * each.  For power-law row lengths (most rows short, a few thousands long),
  * where a thread per row leaves most lanes of a warp idle.  The lengths of the
  * slice rows are kept as bytes after the lane -> row map, so that a warp reads
- * its 32 lengths in one line instead of 64 scattered row pointers. */
+ * its 32 lengths in one line instead of 64 scattered row pointers.  One
+ * allocation holds each long row's entry range, the long rows, and the warp
+ * work lists (hyb_plan) for one wave of the kernels that take this form. */
 static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
     cudaStream_t st = A->ctx->stream;
     if (!n || A->d_hval) return HBICG_OK;
@@ -49,10 +120,24 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
     const size_t srow_bytes = sizeof(unsigned) * (cap + 1) + cap + 1;
     unsigned *srow = malloc(srow_bytes);
     unsigned long long *wkey = malloc(sizeof(unsigned long long) * (nw + 1));
-    unsigned *wrow = malloc(sizeof(unsigned) * (nw + 1));
+    /* grid of the HYB kernels: one wave of the heaviest, so every warp of a
+     * launch runs exactly one list */
+    int hgrid = hbk_spmv_grid((n + HBK_THREADS - 1) / HBK_THREADS);
+    {
+        const int wf = hbk_hyb_wave_fused(), wb = hbk_hyb_wave_blas();
+        if (wf < hgrid) hgrid = wf;
+        if (wb < hgrid) hgrid = wb;
+        if (hgrid < 1) hgrid = 1;
+    }
+    const unsigned hnw = (unsigned)hgrid * (HBK_THREADS / 32);
+    /* [2 nw] entry ranges, [nw] rows, [hnw + 1] list starts, [nw + ns] items */
+    const size_t plan_words = 3 * nw + hnw + 1 + nw + ns;
+    unsigned *wrng = malloc(sizeof(unsigned) * plan_words);
+    unsigned *wrow = wrng ? wrng + 2 * nw : NULL;
+    unsigned *wlen = malloc(sizeof(unsigned) * (nw + 1));
     unsigned long long *sp = malloc(sizeof(unsigned long long) * (ns + 1));
     int rc = HBICG_OK;
-    if (!srow || !wkey || !wrow || !sp) {
+    if (!srow || !wkey || !wrng || !wlen || !sp) {
         rc = HBICG_E_NOMEM;
         goto done;
     }
@@ -84,7 +169,13 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
         for (size_t i = 0; i < cap; ++i)
             slen[i] = srow[i] < n ? (unsigned char)(h_ptr[srow[i] + 1] - h_ptr[srow[i]]) : 0;
         qsort(wkey, nw, sizeof *wkey, cmp_u64);
-        for (size_t i = 0; i < nw; ++i) wrow[i] = (unsigned)(wkey[i] & 0xFFFFFFFFu);
+        for (size_t i = 0; i < nw; ++i) {
+            const unsigned r = (unsigned)(wkey[i] & 0xFFFFFFFFu);
+            wrow[i] = r;
+            wrng[2 * i] = h_ptr[r];
+            wrng[2 * i + 1] = h_ptr[r + 1];
+            wlen[i] = h_ptr[r + 1] - h_ptr[r];
+        }
         sp[0] = 0;
         for (size_t s = 0; s < ns; ++s) {
             unsigned w = 0;
@@ -94,6 +185,8 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
             }
             sp[s + 1] = sp[s] + 32ull * w;
         }
+        rc = hyb_plan(nw, wlen, ns, sp, hnw, wrow + nw, wrow + nw + hnw + 1);
+        if (rc) goto done;
     }
 #define HTRY(call)                                                                               \
     do {                                                                                         \
@@ -108,10 +201,10 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
     HTRY(cudaMalloc((void **)&A->d_hval, sizeof(double) * (sp[ns] + 1)));
     HTRY(cudaMalloc((void **)&A->d_hcol, sizeof(unsigned) * (sp[ns] + 1)));
     HTRY(cudaMalloc((void **)&A->d_srow, srow_bytes));
-    HTRY(cudaMalloc((void **)&A->d_wrow, sizeof(unsigned) * (nw + 1)));
+    HTRY(cudaMalloc((void **)&A->d_wrow, sizeof(unsigned) * plan_words));
     HTRY(cudaMemcpyAsync(A->d_hsptr, sp, sizeof(unsigned long long) * (ns + 1), cudaMemcpyHostToDevice, st));
     if (cap) HTRY(cudaMemcpyAsync(A->d_srow, srow, srow_bytes, cudaMemcpyHostToDevice, st));
-    if (nw) HTRY(cudaMemcpyAsync(A->d_wrow, wrow, sizeof(unsigned) * nw, cudaMemcpyHostToDevice, st));
+    HTRY(cudaMemcpyAsync(A->d_wrow, wrng, sizeof(unsigned) * plan_words, cudaMemcpyHostToDevice, st));
     {
         const int e = hbk_hyb_fill((unsigned)ns, A->d_srow, n, A->d_ptr, A->d_col, A->d_val, A->d_hsptr, A->d_hval,
                                    A->d_hcol, st);
@@ -122,10 +215,13 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
     A->nslice = (unsigned)ns;
     A->nwrow = (unsigned)nw;
     A->slen_off = cap + 1;
+    A->hnw = hnw;
+    A->hyb_grid = hgrid;
 done:
     free(srow);
     free(wkey);
-    free(wrow);
+    free(wrng);
+    free(wlen);
     free(sp);
     return rc;
 }
@@ -138,10 +234,14 @@ static void use_hyb(hbicg_matrix *A) {
     A->k.sptr = A->d_hsptr;
     A->k.srow = A->d_srow;
     A->k.slen = A->d_srow ? (const unsigned char *)(A->d_srow + A->slen_off) : NULL;
-    A->k.wrow = A->d_wrow;
+    A->k.wrng = A->d_wrow;
+    A->k.wrow = A->d_wrow ? A->d_wrow + 2 * (size_t)A->nwrow : NULL;
+    A->k.hwbeg = A->k.wrow ? A->k.wrow + A->nwrow : NULL;
+    A->k.hitem = A->k.hwbeg ? A->k.hwbeg + A->hnw + 1 : NULL;
+    A->k.hnw = A->hnw;
     A->k.nslice = A->nslice;
     A->k.nwrow = A->nwrow;
-    A->k.grid = hbk_spmv_grid((A->k.n + HBK_THREADS - 1) / HBK_THREADS);
+    A->k.grid = A->hyb_grid > 0 ? A->hyb_grid : 1;
 }
 
 /* MERGE: rows of at most HBK_MERGE_LONG entries in blocks of consecutive
@@ -818,6 +918,10 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
         A->k.srow = NULL;
         A->k.slen = NULL;
         A->k.wrow = NULL;
+        A->k.wrng = NULL;
+        A->k.hwbeg = NULL;
+        A->k.hitem = NULL;
+        A->k.hnw = 0;
         A->k.nslice = 0;
         A->k.nwrow = 0;
     }

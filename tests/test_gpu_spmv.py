@@ -57,14 +57,26 @@ def _random_csr(pkg, n, lens, seed):
     return pkg.workloads.Csr(ptr, col, val)
 
 
-@pytest.mark.parametrize("case", ["window_edges", "all_long", "all_short_padded", "empty_windows"])
+def _hyb_window():
+    """The HYB sort window (HBK_HYB_WINDOW in the kernels' header)."""
+    import re
+    from pathlib import Path
+
+    text = (Path(__file__).resolve().parents[1] / "hybrid-bicg_gb300" / "csrc" / "hbk.h").read_text()
+    return int(re.search(r"#define HBK_HYB_WINDOW (\d+)", text).group(1))
+
+
+@pytest.mark.parametrize("case", ["window_edges", "all_long", "all_short_padded", "empty_windows",
+                                  "few_huge_rows", "more_items_than_warps"])
 def test_hyb_shapes(cuda, pkg, oracle, case):
-    """HYB edge cases: n not a multiple of the 256-row window, only warp rows,
+    """HYB edge cases: n not a multiple of the sort window, only warp rows,
     only slice rows (SELL-32 rejected for its padding), whole windows of empty
-    rows."""
+    rows, a few rows far longer than the rest (each alone in a warp's list),
+    and many more work items than warps (long lists)."""
     rng = np.random.default_rng(len(case))
+    win = _hyb_window()
     if case == "window_edges":
-        n = 256 * 7 + 37
+        n = win * 7 + 37
         lens = rng.choice([0, 1, 3, 31, 32, 33, 70, 600], size=n)
     elif case == "all_long":
         n = 300
@@ -72,10 +84,17 @@ def test_hyb_shapes(cuda, pkg, oracle, case):
     elif case == "all_short_padded":
         n = 5000
         lens = np.where(rng.random(n) < 0.05, 30, 1)
+    elif case == "few_huge_rows":
+        n = 40000
+        lens = rng.integers(0, 12, n)
+        lens[rng.choice(n, 5, replace=False)] = 20000
+    elif case == "more_items_than_warps":
+        n = 600000
+        lens = np.where(rng.random(n) < 0.03, rng.integers(33, 300, n), rng.integers(0, 9, n))
     else:
-        n = 256 * 4
+        n = win * 4
         lens = np.zeros(n, dtype=np.int64)
-        lens[256:512] = rng.integers(0, 40, 256)
+        lens[win:2 * win] = rng.integers(0, 40, win)
     a = _random_csr(pkg, n, lens, seed=3)
     x = rng.standard_normal(n)
     y = _gpu_spmv(pkg, a, x, fmt="hyb", want_fmt="hyb")
