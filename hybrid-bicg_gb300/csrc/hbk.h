@@ -42,6 +42,8 @@ extern "C" {
 #define HBK_FMT_HYB 2        /* short rows in SELL-32 slices (length-sorted inside windows), long rows one warp each */
 #define HBK_HYB_SHORT 32     /* longest row of a HYB slice */
 #define HBK_HYB_WINDOW 1024  /* rows are sorted by length only inside windows of this many consecutive rows */
+#define HBK_HYB_L4 128       /* long rows up to this length: 4 lanes each, 8 rows per warp */
+#define HBK_HYB_L16 512      /* longer rows up to this length: 16 lanes each, 2 rows per warp; longer: a warp */
 #define HBK_FMT_MERGE 3      /* CSR; rows up to HBK_MERGE_LONG entries in merge-path blocks, longer rows one warp each */
 #define HBK_MERGE_IPT 8      /* merge items (row ends + nonzeros) per lane of a block */
 #define HBK_MERGE_ITEMS (32 * HBK_MERGE_IPT) /* items per block (one warp) */
@@ -67,8 +69,10 @@ typedef struct {
     unsigned nwrow;
     const unsigned *wrng;      /* HYB: first and end entry of long row i at 2 i, 2 i + 1 */
     const unsigned *hwbeg;     /* HYB: work list of warp w = items hitem[hwbeg[w] .. hwbeg[w + 1]) */
-    const unsigned *hitem;     /* HYB: item i < nwrow is long row i, else slice i - nwrow */
+    const unsigned *hitem;     /* HYB: work items (hbk_hyb_classes), then slice i - hitl */
     unsigned hnw;              /* HYB: warps the lists were balanced for */
+    unsigned hrow32, hrow16;   /* HYB: long rows [0, hrow32) have 32 lanes each, [hrow32, hrow16) 16, the rest 4 */
+    unsigned hit16, hit4, hitl; /* HYB: first item of 16-lane rows, of 4-lane rows, of the slices */
     const unsigned *mblk;      /* MERGE: [2 nmblk] first and end row of each block of short rows */
     unsigned nmblk;
     const unsigned *mlong;     /* MERGE: rows longer than HBK_MERGE_LONG, longest first, one warp each */

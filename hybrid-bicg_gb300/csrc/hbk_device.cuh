@@ -10,6 +10,18 @@
 namespace hbk {
 
 constexpr int NT = HBK_THREADS;
+
+// Blocks per SM that the kernels taking the HYB form are compiled for (the
+// other forms keep the compiler's choice).  The HYB products are
+// latency-bound, and all HYB kernels share one warp-list plan sized for the
+// smallest one-wave grid among them.  Measured on GB300, config 3 (2 M
+// power-law rows): with K1 and K3 at 8 blocks (32 registers, a few bytes
+// spilled) the solve took as long as with them at 4 blocks (56 registers),
+// and the plain product, at the full wave of 8 blocks, took 0.166 against
+// 0.184 ms.
+#ifndef HBK_HYB_MINB
+#define HBK_HYB_MINB 8
+#endif
 constexpr int NW = NT / 32;
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -233,18 +245,22 @@ __device__ __forceinline__ void spmv_rows_tile(const hbk_matrix &A, const double
     }
 }
 
-// HYB path: persistent warps over work items: the long rows (more than
-// HBK_HYB_SHORT entries), one warp each: lanes take every 32nd entry in stored
-// order and the 32 partial sums meet in a fixed shuffle tree; and SELL-32
-// slices of short rows, one warp each, whose 32 rows were sorted by length
-// inside a window of HBK_HYB_WINDOW rows, so the lanes of a warp have similar
-// row lengths (an FP64 instruction costs the same whatever its active lanes);
-// each short row is summed in stored order with FMAs from 0, as in the other
-// paths.  The host deals the items to A.hnw warp lists, longest first, each to
-// the list with the least work so far (cost: a header plus one step per 32
-// entries of a long row or per entry of a slice), so no warp is left with
-// several of the longest rows; warp w of the grid runs lists w, w + (warps of
-// the grid), ...  A row's arithmetic does not depend on the list it is in.
+// HYB path: persistent warps over work items.  Long rows (more than
+// HBK_HYB_SHORT entries, longest first) take g lanes each: 32 (one row per
+// item) above HBK_HYB_L16 entries, 16 (two rows of similar length per item)
+// above HBK_HYB_L4, else 4 (eight rows per item).  Lane j of a row's group
+// sums entries j, j + g, ... in stored order with FMAs, and the g partial
+// sums meet in a fixed shuffle tree (log2 g FP64 adds, instead of 5 for every
+// row).  Short rows are in SELL-32 slices, one warp each, whose 32 rows were
+// sorted by length inside a window of HBK_HYB_WINDOW rows, so the lanes of a
+// warp have similar row lengths (an FP64 instruction costs the same whatever
+// its active lanes); each short row is summed in stored order with FMAs from
+// 0, as in the other paths.  The host deals the items to A.hnw warp lists,
+// costliest first, each to the list with the least work so far (cost: a
+// header, one step per g entries of the group's longest row or per entry of
+// a slice, and the tree), so no warp is left with several of the longest
+// rows; warp w of the grid runs lists w, w + (warps of the grid), ...  A row's
+// arithmetic does not depend on the list it is in.
 template <class Epi>
 __device__ __forceinline__ void spmv_rows_hyb(const hbk_matrix &A, const double *__restrict__ x, Epi &epi) {
     const unsigned lane = threadIdx.x & 31;
@@ -253,16 +269,35 @@ __device__ __forceinline__ void spmv_rows_hyb(const hbk_matrix &A, const double 
         const unsigned k1 = __ldg(A.hwbeg + w + 1);
         for (unsigned k = __ldg(A.hwbeg + w); k < k1; ++k) {
             const unsigned it = __ldg(A.hitem + k);
-            if (it < A.nwrow) {
-                const uint2 rg = __ldg(reinterpret_cast<const uint2 *>(A.wrng) + it);
-                const unsigned r = __ldg(A.wrow + it);
+            if (it < A.hitl) {
+                unsigned g, i, iend;
+                if (it < A.hit16) {
+                    g = 32;
+                    i = it;
+                    iend = A.hrow32;
+                } else if (it < A.hit4) {
+                    g = 16;
+                    i = A.hrow32 + 2 * (it - A.hit16) + (lane >> 4);
+                    iend = A.hrow16;
+                } else {
+                    g = 4;
+                    i = A.hrow16 + 8 * (it - A.hit4) + (lane >> 2);
+                    iend = A.nwrow;
+                }
+                const bool valid = i < iend;
+                uint2 rg = make_uint2(0u, 0u);
+                unsigned r = 0;
+                if (valid) {
+                    rg = __ldg(reinterpret_cast<const uint2 *>(A.wrng) + i);
+                    r = __ldg(A.wrow + i);
+                }
                 double acc = 0.0;
-                for (unsigned e = rg.x + lane; e < rg.y; e += 32)
+                for (unsigned e = rg.x + (lane & (g - 1)); e < rg.y; e += g)
                     acc = fma(__ldg(A.val + e), __ldg(x + __ldg(A.col + e)), acc);
-                acc = warp_sum(acc);
-                if (lane == 0) epi(r, acc);
+                for (unsigned o = g >> 1; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (valid && (lane & (g - 1)) == 0) epi(r, acc);
             } else {
-                const unsigned s = it - A.nwrow;
+                const unsigned s = it - A.hitl;
                 const unsigned long long base = __ldg(A.sptr + s);
                 const unsigned wd = (unsigned)((__ldg(A.sptr + s + 1) - base) >> 5);
                 const unsigned r = __ldg(A.srow + 32 * (size_t)s + lane);

@@ -43,6 +43,7 @@ struct hbicg_matrix {
     unsigned nslice, nwrow;
     unsigned hnw;  /* warp work lists in d_wrow (after the long rows' entry ranges and the long rows) */
     int hyb_grid;  /* blocks of the HYB kernels: one list per warp */
+    unsigned hrow32, hrow16, hit16, hit4, hitl; /* HYB lane classes of the long rows (hbk.h) */
     /* MERGE form (hbk.h HBK_FMT_MERGE): block row ranges, then the long rows,
      * in one allocation */
     unsigned *d_merge;

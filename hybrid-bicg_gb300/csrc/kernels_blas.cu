@@ -71,9 +71,9 @@ __global__ void __launch_bounds__(NT) k_spmv_acc(hbk_matrix A, const double *__r
 
 // out[j] = ||b - (A + sigma_j I) x_j||^2 ; one launch per shift block (grid.y = shift)
 template <int FMT>
-__global__ void __launch_bounds__(NT) k_true_res(hbk_matrix A, const double *__restrict__ X, size_t ld,
-                                                 const double *__restrict__ b, const double *__restrict__ sigma,
-                                                 double *partials, unsigned *counters, double *out) {
+__device__ __forceinline__ void true_res_body(const hbk_matrix &A, const double *__restrict__ X, size_t ld,
+                                              const double *__restrict__ b, const double *__restrict__ sigma,
+                                              double *partials, unsigned *counters, double *out) {
     __shared__ double sh[NW];
     const int j = blockIdx.y;
     const double *xj = X + (size_t)j * ld;
@@ -100,6 +100,19 @@ __global__ void __launch_bounds__(NT) k_true_res(hbk_matrix A, const double *__r
             counters[j] = 0;
         }
     }
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(NT) k_true_res(hbk_matrix A, const double *__restrict__ X, size_t ld,
+                                                 const double *__restrict__ b, const double *__restrict__ sigma,
+                                                 double *partials, unsigned *counters, double *out) {
+    true_res_body<FMT>(A, X, ld, b, sigma, partials, counters, out);
+}
+template <>
+__global__ void __launch_bounds__(NT, HBK_HYB_MINB) k_true_res<HBK_FMT_HYB>(
+    hbk_matrix A, const double *__restrict__ X, size_t ld, const double *__restrict__ b,
+    const double *__restrict__ sigma, double *partials, unsigned *counters, double *out) {
+    true_res_body<HBK_FMT_HYB>(A, X, ld, b, sigma, partials, counters, out);
 }
 
 // SELL-32 build: slice widths, then one thread per row writes its entries

@@ -19,16 +19,6 @@
 
 #include "hbk_device.cuh"
 
-// Blocks per SM that K1 and K3 are compiled for in the HYB form (the other
-// forms keep the compiler's choice).  The HYB products are latency-bound, and
-// all HYB kernels share one warp-list plan sized for the smallest one-wave
-// grid among them.  Measured on GB300, config 3 (2 M power-law rows): with K1
-// and K3 at 8 blocks (32 registers, a few bytes spilled) the solve took as
-// long as with them at 4 blocks (56 registers), and the plain product, which
-// then keeps its full wave of 8 blocks, took 0.166 against 0.184 ms.
-#ifndef HBK_HYB_FUSED_MINB
-#define HBK_HYB_FUSED_MINB 8
-#endif
 
 using namespace hbk;
 
@@ -172,7 +162,7 @@ __device__ __forceinline__ void seed_s_body(const Ctx &c, const G &g) {
 template <int FMT>
 __global__ void __launch_bounds__(NT) k_seed_s(Ctx c) { seed_s_body<FMT>(c, HwGrid()); }
 template <>
-__global__ void __launch_bounds__(NT, HBK_HYB_FUSED_MINB) k_seed_s<HBK_FMT_HYB>(Ctx c) {
+__global__ void __launch_bounds__(NT, HBK_HYB_MINB) k_seed_s<HBK_FMT_HYB>(Ctx c) {
     seed_s_body<HBK_FMT_HYB>(c, HwGrid());
 }
 
@@ -245,7 +235,7 @@ __device__ __forceinline__ void seed_y_body(const Ctx &c, const G &g) {
 template <int FMT>
 __global__ void __launch_bounds__(NT) k_seed_y(Ctx c) { seed_y_body<FMT>(c, HwGrid()); }
 template <>
-__global__ void __launch_bounds__(NT, HBK_HYB_FUSED_MINB) k_seed_y<HBK_FMT_HYB>(Ctx c) {
+__global__ void __launch_bounds__(NT, HBK_HYB_MINB) k_seed_y<HBK_FMT_HYB>(Ctx c) {
     seed_y_body<HBK_FMT_HYB>(c, HwGrid());
 }
 

@@ -20,13 +20,10 @@ static int cmp_u64(const void *a, const void *b) {
     return x < y ? -1 : x > y;
 }
 
-/* HYB work lists.  Items: long row i (i < nw, in the order of wrow), then
- * slice s (item nw + s).  Cost of an item: a header of 2 (long row) or 3
- * (slice: offsets, row map and lengths) plus one step per 32 entries of a long
- * row or per entry of the slice's longest row.  The items are dealt in order
- * of decreasing cost (ties: lower item first), each to the list with the least
- * cost so far (ties: lower list), and every list keeps the order of dealing.
- * hwbeg[hnw + 1], hitem[nw + ns]. */
+/* HYB work lists: work items (use_hyb lists them) with their costs, dealt in order of
+ * decreasing cost (ties: lower item first), each to the list with the least
+ * cost so far (ties: lower list); every list keeps the order of dealing.
+ * hwbeg[hnw + 1], hitem[ni]. */
 typedef struct {
     unsigned long long load;
     unsigned w;
@@ -36,9 +33,7 @@ static int slot_less(const hyb_slot *a, const hyb_slot *b) {
     return a->load < b->load || (a->load == b->load && a->w < b->w);
 }
 
-static int hyb_plan(size_t nw, const unsigned *wlen, size_t ns, const unsigned long long *sp, unsigned hnw,
-                    unsigned *hwbeg, unsigned *hitem) {
-    const size_t ni = nw + ns;
+static int hyb_plan(size_t ni, const unsigned *cost, unsigned hnw, unsigned *hwbeg, unsigned *hitem) {
     unsigned long long *key = malloc(sizeof *key * (ni + 1));
     hyb_slot *h = malloc(sizeof *h * hnw);
     unsigned *owner = malloc(sizeof *owner * (ni + 1));
@@ -50,11 +45,7 @@ static int hyb_plan(size_t nw, const unsigned *wlen, size_t ns, const unsigned l
         free(pos);
         return HBICG_E_NOMEM;
     }
-    for (size_t i = 0; i < ni; ++i) {
-        const unsigned long long c =
-            i < nw ? 2ull + (wlen[i] + 31ull) / 32 : 3ull + (sp[i - nw + 1] - sp[i - nw]) / 32;
-        key[i] = ((0xFFFFFFFFull - c) << 32) | i; /* costliest first, then by item */
-    }
+    for (size_t i = 0; i < ni; ++i) key[i] = ((0xFFFFFFFFull - cost[i]) << 32) | i; /* costliest first, then by item */
     qsort(key, ni, sizeof *key, cmp_u64);
     for (unsigned w = 0; w < hnw; ++w) h[w] = (hyb_slot){0, w}; /* all zero: a valid heap */
     memset(hwbeg, 0, sizeof *hwbeg * ((size_t)hnw + 1));
@@ -130,14 +121,23 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
         if (hgrid < 1) hgrid = 1;
     }
     const unsigned hnw = (unsigned)hgrid * (HBK_THREADS / 32);
-    /* [2 nw] entry ranges, [nw] rows, [hnw + 1] list starts, [nw + ns] items */
-    const size_t plan_words = 3 * nw + hnw + 1 + nw + ns;
+    /* long rows by lanes per row (longest first, so each class is a range) */
+    size_t r32 = 0, r16 = 0;
+    for (unsigned r = 0; r < n; ++r) {
+        const unsigned len = h_ptr[r + 1] - h_ptr[r];
+        r32 += len > HBK_HYB_L16;
+        r16 += len > HBK_HYB_L4;
+    }
+    const size_t it16 = r32, it4 = it16 + (r16 - r32 + 1) / 2, itl = it4 + (nw - r16 + 7) / 8;
+    const size_t ni = itl + ns;
+    /* [2 nw] entry ranges, [nw] rows, [hnw + 1] list starts, [ni] items */
+    const size_t plan_words = 3 * nw + hnw + 1 + ni;
     unsigned *wrng = malloc(sizeof(unsigned) * plan_words);
     unsigned *wrow = wrng ? wrng + 2 * nw : NULL;
-    unsigned *wlen = malloc(sizeof(unsigned) * (nw + 1));
+    unsigned *cost = malloc(sizeof(unsigned) * (ni + 1));
     unsigned long long *sp = malloc(sizeof(unsigned long long) * (ns + 1));
     int rc = HBICG_OK;
-    if (!srow || !wkey || !wrng || !wlen || !sp) {
+    if (!srow || !wkey || !wrng || !cost || !sp) {
         rc = HBICG_E_NOMEM;
         goto done;
     }
@@ -174,7 +174,6 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
             wrow[i] = r;
             wrng[2 * i] = h_ptr[r];
             wrng[2 * i + 1] = h_ptr[r + 1];
-            wlen[i] = h_ptr[r + 1] - h_ptr[r];
         }
         sp[0] = 0;
         for (size_t s = 0; s < ns; ++s) {
@@ -185,7 +184,24 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
             }
             sp[s + 1] = sp[s] + 32ull * w;
         }
-        rc = hyb_plan(nw, wlen, ns, sp, hnw, wrow + nw, wrow + nw + hnw + 1);
+        /* item costs: a header (2 for rows, 3 for a slice), one step per g
+         * entries of the group's longest row (the first: rows are longest
+         * first) or per entry of the slice, and log2 g steps of the tree */
+        for (size_t k = 0; k < ni; ++k) {
+            unsigned first, g, tree;
+            if (k < it16) {
+                first = (unsigned)k, g = 32, tree = 5;
+            } else if (k < it4) {
+                first = (unsigned)(r32 + 2 * (k - it16)), g = 16, tree = 4;
+            } else if (k < itl) {
+                first = (unsigned)(r16 + 8 * (k - it4)), g = 4, tree = 2;
+            } else {
+                cost[k] = 3u + (unsigned)((sp[k - itl + 1] - sp[k - itl]) / 32);
+                continue;
+            }
+            cost[k] = 2u + (wrng[2 * first + 1] - wrng[2 * first] + g - 1) / g + tree;
+        }
+        rc = hyb_plan(ni, cost, hnw, wrow + nw, wrow + nw + hnw + 1);
         if (rc) goto done;
     }
 #define HTRY(call)                                                                               \
@@ -217,16 +233,24 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
     A->slen_off = cap + 1;
     A->hnw = hnw;
     A->hyb_grid = hgrid;
+    A->hrow32 = (unsigned)r32;
+    A->hrow16 = (unsigned)r16;
+    A->hit16 = (unsigned)it16;
+    A->hit4 = (unsigned)it4;
+    A->hitl = (unsigned)itl;
 done:
     free(srow);
     free(wkey);
     free(wrng);
-    free(wlen);
+    free(cost);
     free(sp);
     return rc;
 }
 
-/* point the kernel view at the HYB arrays */
+/* point the kernel view at the HYB arrays.  Work items, in order: the long
+ * rows above HBK_HYB_L16 entries one each ([0, hrow32), 32 lanes per row),
+ * then pairs of rows above HBK_HYB_L4 ([hrow32, hrow16), 16 lanes per row),
+ * then groups of 8 rows ([hrow16, nwrow), 4 lanes per row), then the slices. */
 static void use_hyb(hbicg_matrix *A) {
     A->k.fmt = HBK_FMT_HYB;
     A->k.sval = A->d_hval;
@@ -239,6 +263,11 @@ static void use_hyb(hbicg_matrix *A) {
     A->k.hwbeg = A->k.wrow ? A->k.wrow + A->nwrow : NULL;
     A->k.hitem = A->k.hwbeg ? A->k.hwbeg + A->hnw + 1 : NULL;
     A->k.hnw = A->hnw;
+    A->k.hrow32 = A->hrow32;
+    A->k.hrow16 = A->hrow16;
+    A->k.hit16 = A->hit16;
+    A->k.hit4 = A->hit4;
+    A->k.hitl = A->hitl;
     A->k.nslice = A->nslice;
     A->k.nwrow = A->nwrow;
     A->k.grid = A->hyb_grid > 0 ? A->hyb_grid : 1;
@@ -922,6 +951,7 @@ int hbicg_matrix_autotune(hbicg_matrix *A, const char *cache_path, int *chosen, 
         A->k.hwbeg = NULL;
         A->k.hitem = NULL;
         A->k.hnw = 0;
+        A->k.hitl = 0;
         A->k.nslice = 0;
         A->k.nwrow = 0;
     }

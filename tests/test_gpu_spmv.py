@@ -67,12 +67,14 @@ def _hyb_window():
 
 
 @pytest.mark.parametrize("case", ["window_edges", "all_long", "all_short_padded", "empty_windows",
-                                  "few_huge_rows", "more_items_than_warps"])
+                                  "few_huge_rows", "more_items_than_warps", "lane_class_edges"])
 def test_hyb_shapes(cuda, pkg, oracle, case):
-    """HYB edge cases: n not a multiple of the sort window, only warp rows,
+    """HYB edge cases: n not a multiple of the sort window, only long rows,
     only slice rows (SELL-32 rejected for its padding), whole windows of empty
     rows, a few rows far longer than the rest (each alone in a warp's list),
-    and many more work items than warps (long lists)."""
+    many more work items than warps (long lists), and long rows at the edges
+    of the 4-, 16- and 32-lane classes with counts that leave a partial group
+    of 8 rows and a partial pair."""
     rng = np.random.default_rng(len(case))
     win = _hyb_window()
     if case == "window_edges":
@@ -88,6 +90,11 @@ def test_hyb_shapes(cuda, pkg, oracle, case):
         n = 40000
         lens = rng.integers(0, 12, n)
         lens[rng.choice(n, 5, replace=False)] = 20000
+    elif case == "lane_class_edges":
+        n = 3001
+        lens = rng.choice([0, 5, 32], size=n)
+        edges = [33] * 13 + [128] * 5 + [129] * 3 + [512] * 7 + [513] * 1 + [2000] * 2
+        lens[rng.choice(n, len(edges), replace=False)] = edges
     elif case == "more_items_than_warps":
         n = 600000
         lens = np.where(rng.random(n) < 0.03, rng.integers(33, 300, n), rng.integers(0, 9, n))
