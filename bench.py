@@ -622,7 +622,8 @@ def run_batch_c4(args, dist: Dist):
                        "l2": "every family's working set is re-read from HBM"},
             "persistent_families": sum(1 for f in fams if in_group(f)),
             "families_per_s": 256 / value, "total_iterations": iters, "status_failures": status_bad,
-            "failed_families": [[i, int(r.status), int(r.k)] for i, r in enumerate(res) if r.status != 0],
+            "failed_families": [[i, int(r.status), int(r.k)] + ([r.message] if r.message else [])
+                                for i, r in enumerate(res) if r.status != 0],
             "families_over_tol": over, "max_true_residual": max(r.max_true_residual for r in res),
             # device time of the worker-solved families, plus the shared launch once
             "sum_device_solve_s": (sum(r.solve_ms for f, r in zip(fams, res) if not in_group(f))

@@ -364,6 +364,7 @@ class FamilyResult:
     wall_ms: float
     max_true_residual: float
     true_residual: np.ndarray | None
+    message: str | None = None  # the first failing family (in order): what its failing call reported
 
 
 def batch_solve(families, workers: int = 8, autotune: bool = False, autotune_cache: str | None = None,
@@ -400,7 +401,8 @@ def batch_solve(families, workers: int = 8, autotune: bool = False, autotune_cac
     opts.persistent = 2 if persistent == "all" else (1 if persistent else 0)
     opts.persistent_ctas = int(persistent_ctas)
     opts.autotune_cache = str(autotune_cache).encode() if autotune_cache else None
-    lib().hbicg_batch_solve_opts(arr, len(families), C.byref(p), C.byref(opts), C.byref(wall))
+    rc = lib().hbicg_batch_solve_opts(arr, len(families), C.byref(p), C.byref(opts), C.byref(wall))
+    msg = lib().hbicg_last_message().decode(errors="replace") if rc != 0 else None
     out = []
     for i in range(len(families)):
         fa = arr[i]
@@ -408,6 +410,10 @@ def batch_solve(families, workers: int = 8, autotune: bool = False, autotune_cac
                                 final_seed=fa.final_seed, spmv_format=_FORMATS.get(fa.spmv_format, "tile"),
                                 solve_ms=fa.solve_ms, wall_ms=fa.wall_ms, max_true_residual=fa.max_true_residual,
                                 true_residual=keep[i][6][:len(keep[i][4])].copy() if want_res else None))
+    if msg is not None:
+        first = next((r for r in out if r.status != 0), None)
+        if first is not None:
+            first.message = msg
     return out, wall.value / 1e3
 
 

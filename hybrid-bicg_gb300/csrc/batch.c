@@ -34,8 +34,20 @@ typedef struct {
     int count;
     const hbicg_params *p;
     const char *cache;
-    int next;  /* queue position (atomic) */
+    int next;    /* queue position (atomic) */
+    char *msgs;  /* [families][FAIL_MSG]: what a failing family's call reported */
 } batch_t;
+
+/* The message of a family whose status is not OK: its thread's
+ * hbicg_last_message right after the failing call, kept per family so that
+ * the batch can hand the first failure's message to its caller. */
+#define FAIL_MSG 192
+static void keep_msg(char *msgs, const hbicg_family *base, const hbicg_family *f) {
+    if (!msgs || f->status == HBICG_OK) return;
+    char *dst = msgs + (size_t)(f - base) * FAIL_MSG;
+    strncpy(dst, hbicg_last_message(), FAIL_MSG - 1);
+    dst[FAIL_MSG - 1] = 0;
+}
 
 static double now_ms(void) {
     struct timespec ts;
@@ -100,6 +112,7 @@ typedef struct {
     hbicg_stats *st;       /* [count] */
     hbicg_matrix **A;      /* [count] */
     hbicg_solver **S;      /* [count] */
+    char *msgs;            /* as in batch_t, indexed by family */
 } group_t;
 
 typedef struct {
@@ -129,6 +142,7 @@ static void *group_part(void *arg) {
         G->slot[i] = -1;
         if (crc != HBICG_OK || !mine) {
             f->status = crc != HBICG_OK ? crc : HBICG_E_NOMEM;
+            keep_msg(G->msgs, G->fams, f);
             continue;
         }
         mine[nm++] = i;
@@ -137,16 +151,23 @@ static void *group_part(void *arg) {
             f->spmv_format = hbicg_matrix_format(G->A[i]);
             f->status = hbicg_solver_create(ctx, G->A[i], f->m, G->p, &G->S[i]);
         }
-        if (f->status != HBICG_OK) continue;
+        if (f->status != HBICG_OK) {
+            keep_msg(G->msgs, G->fams, f);
+            continue;
+        }
         G->st[i].true_residual = f->true_residual;
         if (hbicg__group_eligible(G->S[i])) {
             G->slot[i] = hbicg__group_add(G->g, G->S[i], f->b, f->sigma, f->seed, f->x, &G->st[i]);
-            if (G->slot[i] < 0) f->status = HBICG_E_ARG; /* no room in the shared launch (not expected) */
+            if (G->slot[i] < 0) { /* no room in the shared launch (not expected) */
+                f->status = HBICG_E_ARG;
+                hbicg__set_msg("no slot left in the shared persistent launch");
+            }
         } else { /* another form after all (e.g. rows too long for SELL-32): a solve of its own */
             f->status = hbicg_solver_run(G->S[i], f->b, f->sigma, f->seed, HBICG_HOST, f->x, f->r, HBICG_HOST,
                                          &G->st[i]);
             family_stats(f, &G->st[i]);
         }
+        keep_msg(G->msgs, G->fams, f);
     }
     meet(G, 0);
     if (pa->tid == 0) {
@@ -163,6 +184,7 @@ static void *group_part(void *arg) {
         if (G->slot[i] >= 0) {
             f->status = hbicg__group_finish(G->g, G->slot[i]);
             family_stats(f, &G->st[i]);
+            keep_msg(G->msgs, G->fams, f);
         }
         hbicg_solver_destroy(G->S[i]);
         hbicg_matrix_destroy(G->A[i]);
@@ -183,9 +205,11 @@ static void *worker(void *arg) {
         hbicg_family *f = &b->fams[b->order[i]];
         if (rc != HBICG_OK) {
             f->status = rc;
+            keep_msg(b->msgs, b->fams, f);
             continue;
         }
         solve_one(ctx, f, b->p, b->cache);
+        keep_msg(b->msgs, b->fams, f);
     }
     if (ctx) hbicg_context_destroy(ctx);
     return NULL;
@@ -227,9 +251,11 @@ int hbicg_batch_solve_opts(hbicg_family *fams, int count, const hbicg_params *p,
     const char *autotune_cache = opts->autotune_cache;
     int *order = malloc(sizeof(int) * (size_t)(count > 0 ? count : 1));
     int *grp = malloc(sizeof(int) * (size_t)(count > 0 ? count : 1));
+    char *msgs = calloc((size_t)(count > 0 ? count : 1), FAIL_MSG); /* optional: NULL keeps no messages */
     if (!order || !grp) {
         free(order);
         free(grp);
+        free(msgs);
         return HBICG_E_NOMEM;
     }
     for (int i = 0; i < count; i++) {
@@ -262,6 +288,7 @@ int hbicg_batch_solve_opts(hbicg_family *fams, int count, const hbicg_params *p,
         G.idx = grp;
         G.count = ng;
         G.p = p;
+        G.msgs = msgs;
         G.g = hbicg__group_new(ng, opts->persistent_ctas);
         G.slot = malloc(sizeof(int) * (size_t)ng);
         G.st = calloc((size_t)ng, sizeof(hbicg_stats));
@@ -303,7 +330,7 @@ int hbicg_batch_solve_opts(hbicg_family *fams, int count, const hbicg_params *p,
     if (workers < 1) workers = 8;
     if (workers > count) workers = count > 0 ? count : 1;
     if (workers > 64) workers = 64;
-    batch_t b = {fams, order, count, p, autotune_cache, 0};
+    batch_t b = {fams, order, count, p, autotune_cache, 0, msgs};
     pthread_t th[64];
     int started = 0;
     for (int t = 0; t < workers; t++) {
@@ -326,7 +353,16 @@ int hbicg_batch_solve_opts(hbicg_family *fams, int count, const hbicg_params *p,
     free(order);
     free(grp);
     if (wall_ms) *wall_ms = now_ms() - t0;
+    int rc = HBICG_OK;
     for (int i = 0; i < count; i++)
-        if (fams[i].status != HBICG_OK) return fams[i].status < 0 ? HBICG_E_ARG : fams[i].status;
-    return HBICG_OK;
+        if (fams[i].status != HBICG_OK) {
+            rc = fams[i].status < 0 ? HBICG_E_ARG : fams[i].status;
+            if (msgs && msgs[(size_t)i * FAIL_MSG])
+                hbicg__set_msg("family %d: %s", i, msgs + (size_t)i * FAIL_MSG);
+            else
+                hbicg__set_msg("family %d: status %d", i, fams[i].status);
+            break;
+        }
+    free(msgs);
+    return rc;
 }

@@ -1364,6 +1364,7 @@ int hbicg__group_eligible(const hbicg_solver *s) {
  * context's families are finished one after another (they share its pinned
  * scalars).  stats.solve_ms is the shared launch's time and stats.launches
  * counts it once. */
+#define GROUP_MSG 192
 struct hbicg__group {
     pthread_mutex_t lock;
     int cap, n, max_ctas, lrc, rounds;
@@ -1374,7 +1375,17 @@ struct hbicg__group {
     int *rc, *in;
     int *k_flushed; /* deferred mode: last iteration the family's previous flush covered */
     int *itrc;      /* a family's own failure between rounds (a flush) */
+    /* what the failing call reported, for failures that happen on another
+     * thread than the family's finish: a family's set-up or its flush between
+     * rounds (per slot), and the launch itself */
+    char (*msg)[GROUP_MSG];
+    char lmsg[GROUP_MSG];
 };
+
+static void group_keep(char *dst) {
+    strncpy(dst, hbicg_last_message(), GROUP_MSG - 1);
+    dst[GROUP_MSG - 1] = 0;
+}
 
 hbicg__group *hbicg__group_new(int cap, int max_ctas) {
     hbicg__group *g = calloc(1, sizeof *g);
@@ -1388,9 +1399,10 @@ hbicg__group *hbicg__group_new(int cap, int max_ctas) {
     g->in = calloc((size_t)g->cap, sizeof *g->in);
     g->k_flushed = calloc((size_t)g->cap, sizeof *g->k_flushed);
     g->itrc = calloc((size_t)g->cap, sizeof *g->itrc);
+    g->msg = calloc((size_t)g->cap, sizeof *g->msg);
     cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
     if (!e) e = cudaStreamCreateWithPriority(&g->stream, cudaStreamNonBlocking, hi);
-    if (!g->S || !g->R || !g->rc || !g->in || !g->k_flushed || !g->itrc || e) {
+    if (!g->S || !g->R || !g->rc || !g->in || !g->k_flushed || !g->itrc || !g->msg || e) {
         if (!e) cudaStreamDestroy(g->stream);
         free(g->S);
         free(g->R);
@@ -1398,6 +1410,7 @@ hbicg__group *hbicg__group_new(int cap, int max_ctas) {
         free(g->in);
         free(g->k_flushed);
         free(g->itrc);
+        free(g->msg);
         free(g);
         return NULL;
     }
@@ -1416,6 +1429,7 @@ void hbicg__group_free(hbicg__group *g) {
     free(g->in);
     free(g->k_flushed);
     free(g->itrc);
+    free(g->msg);
     free(g);
 }
 
@@ -1434,6 +1448,7 @@ int hbicg__group_add(hbicg__group *g, hbicg_solver *s, const double *b, const do
     if (rc == HBICG_OK) rc = fused_init(s, seed, &r->launches);
     g->rc[slot] = rc;
     g->in[slot] = rc == HBICG_OK;
+    if (rc) group_keep(g->msg[slot]);
     return slot;
 }
 
@@ -1517,9 +1532,11 @@ int hbicg__group_launch(hbicg__group *g) {
             if (ce) {
                 set_msg("shared launch: %s", cudaGetErrorString(ce));
                 g->itrc[f] = HBICG_E_CUDA;
+                group_keep(g->msg[f]);
                 run[f] = 0;
             } else if (h->finished && (h->status & HBK_ST_BASIS_FULL) && !(h->status & HBK_ST_BREAKDOWN)) {
                 g->itrc[f] = fused_pause_flush(s, &g->k_flushed[f], &r->launches, &r->flushes, &r->flush_ms);
+                if (g->itrc[f]) group_keep(g->msg[f]);
                 run[f] = g->itrc[f] == HBICG_OK;
                 resumed += run[f];
             } else {
@@ -1542,6 +1559,7 @@ out:
     free(idx);
     free(run);
     g->lrc = lrc;
+    if (lrc) group_keep(g->lmsg);
     g->ms = total_ms;
     g->rounds = rounds;
     return lrc;
@@ -1552,8 +1570,10 @@ int hbicg__group_finish(hbicg__group *g, int slot) {
     hbicg_solver *s = g->S[slot];
     run_t *r = &g->R[slot];
     int rc = g->rc[slot];
+    if (rc) set_msg("%s", g->msg[slot]); /* its set-up failed */
     if (g->in[slot]) {
         int it = g->lrc != HBICG_OK ? g->lrc : g->itrc[slot];
+        if (it != HBICG_OK) set_msg("%s", g->lrc != HBICG_OK ? g->lmsg : g->msg[slot]);
         if (it == HBICG_OK) { /* the final flush reads this family's scalars (its context's copy may hold another's) */
             cudaError_t ce = cudaMemcpyAsync(s->ctx->h_sc, s->d_sc, sizeof(hbk_scalars), cudaMemcpyDeviceToHost,
                                              s->ctx->stream);

@@ -219,7 +219,9 @@ int hbicg_true_residuals_noalloc(hbicg_matrix *A, const double *x, unsigned long
  * interleaves the kernels of several small families.  Replaces the
  * reference's hard-coded sweep drivers (src/main_seed_diff.c:113-155).
  * All pointers are host memory.  Per-family status in fams[i].status; the
- * call returns the first failing status, or HBICG_OK.  autotune_cache: path
+ * call returns the first failing status (in family order), or HBICG_OK, and
+ * hbicg_last_message() on the calling thread then names that family and what
+ * its failing call reported.  autotune_cache: path
  * of the SpMV-form cache used by families with autotune set (may be NULL). */
 typedef struct {
     /* inputs */

@@ -41,13 +41,17 @@ def test_batch_equals_individual_solves(cuda, pkg):
 
 @pytest.mark.parametrize("persistent", [False, True])
 def test_batch_failure_stays_with_its_family(cuda, pkg, persistent):
-    fams = _families(pkg, count=4, seed=1)
-    bad = fams[2]
-    bad.seed = len(bad.sigma) + 3  # out of range
+    """A family with a bad input fails alone; the first failing family (in
+    family order) carries what its failing call reported."""
+    fams = _families(pkg, count=5, seed=1)
+    for i in (2, 4):
+        fams[i].seed = len(fams[i].sigma) + 3  # out of range
     res, _ = pkg.batch_solve(fams, workers=3, tol=1e-10, max_iter=10000, persistent=persistent)
-    assert res[2].status != 0
+    assert res[2].status != 0 and res[4].status != 0
+    assert res[2].message.startswith("family 2: ") and "out of range" in res[2].message, res[2].message
+    assert res[4].message is None
     for i in (0, 1, 3):
-        assert res[i].status == 0 and res[i].k > 1
+        assert res[i].status == 0 and res[i].k > 1 and res[i].message is None
 
 
 def test_persistent_launch_against_the_oracle(cuda, pkg, oracle):
