@@ -59,6 +59,12 @@ void hbicg__set_message(const char *msg);
 void hbicg__ctx_retain(hbicg_context *c);
 void hbicg__ctx_release(hbicg_context *c);
 
+/* HYB warp work lists (host only): ni items with costs dealt costliest first
+ * (ties: lower item), each to the list with the least cost so far (ties:
+ * lower list); hwbeg[hnw + 1] list starts, hitem[ni] the lists in order of
+ * dealing.  HBICG_OK or HBICG_E_NOMEM. */
+int hbicg__hyb_plan(size_t ni, const unsigned *cost, unsigned hnw, unsigned *hwbeg, unsigned *hitem);
+
 /* positions of A's SELL-32 diagonal entries (computed once per layout) */
 int hbicg__sell_diag(hbicg_matrix *A);
 /* device arrays from the library's stream-ordered pool (solver.c) */

@@ -33,7 +33,7 @@ static int slot_less(const hyb_slot *a, const hyb_slot *b) {
     return a->load < b->load || (a->load == b->load && a->w < b->w);
 }
 
-static int hyb_plan(size_t ni, const unsigned *cost, unsigned hnw, unsigned *hwbeg, unsigned *hitem) {
+int hbicg__hyb_plan(size_t ni, const unsigned *cost, unsigned hnw, unsigned *hwbeg, unsigned *hitem) {
     unsigned long long *key = malloc(sizeof *key * (ni + 1));
     hyb_slot *h = malloc(sizeof *h * hnw);
     unsigned *owner = malloc(sizeof *owner * (ni + 1));
@@ -90,7 +90,7 @@ static int hyb_plan(size_t ni, const unsigned *cost, unsigned hnw, unsigned *hwb
  * slice rows are kept as bytes after the lane -> row map, so that a warp reads
  * its 32 lengths in one line instead of 64 scattered row pointers.  One
  * allocation holds each long row's entry range, the long rows, and the warp
- * work lists (hyb_plan) for one wave of the kernels that take this form. */
+ * work lists (hbicg__hyb_plan) for one wave of the kernels that take this form. */
 static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
     cudaStream_t st = A->ctx->stream;
     if (!n || A->d_hval) return HBICG_OK;
@@ -201,7 +201,7 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
             }
             cost[k] = 2u + (wrng[2 * first + 1] - wrng[2 * first] + g - 1) / g + tree;
         }
-        rc = hyb_plan(ni, cost, hnw, wrow + nw, wrow + nw + hnw + 1);
+        rc = hbicg__hyb_plan(ni, cost, hnw, wrow + nw, wrow + nw + hnw + 1);
         if (rc) goto done;
     }
 #define HTRY(call)                                                                               \
