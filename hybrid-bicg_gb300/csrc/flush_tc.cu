@@ -20,18 +20,20 @@
 // splitting of Ozaki, Ogita, Oishi and Rump for matrix products, arranged here
 // so that the exact sums fit TMEM.)
 //
-// One CTA per SM (203 KB of shared memory), persistent over tiles of 48
-// vector elements (one panel of the panel-major x_j and p_j arrays, whose
-// values for all shifts lie in one contiguous block); 128 output rows per
-// group of 64 shifts, ordered so that
+// One CTA per SM (226 KB of shared memory, all 512 TMEM columns), persistent
+// over tiles of 48 vector elements (one panel of the panel-major x_j and p_j
+// arrays, whose values for all shifts lie in one contiguous block); 128
+// output rows per group of 64 shifts, ordered so that
 // TMEM lanes 32q..32q+15 hold the x rows of shifts 16q..16q+15 and lanes
-// 32q+16..32q+31 their p rows.  Warps 0-2 make the basis digits of a tile;
+// 32q+16..32q+31 their p rows.  Warps 0-2 make the basis digits of a tile
+// into one of two buffers (tile t+1's while the tensor core reads tile t's);
 // one thread of warp 3 issues its MMAs (M=128, N up to 256, K=16; 52 per
-// tile) into nine accumulators, so that the digit builders never wait behind
-// the MMA issue; warps 4-15 empty the accumulators into registers first, so
-// that the next tile's MMAs run while they round, add the own-vector terms
-// and write x and p.  Every wait is bounded: a timeout sets an error flag,
-// the CTA skips its remaining work and still frees its TMEM.
+// tile; coefficient digit slices 0-1 from TMEM, 2-8 from shared memory) into
+// nine accumulators, so that the digit builders never wait behind the MMA
+// issue; warps 4-15 empty the accumulators into registers first, so that the
+// next tile's MMAs run while they round, add the own-vector terms and write x
+// and p.  Every wait is bounded: a timeout sets an error flag, the CTA skips
+// its remaining work and still frees its TMEM.
 //
 // Only the live shifts are formed: a shift that had converged by the previous
 // flush has zero coefficients and own terms (0, 1) since that flush's reset,
@@ -56,8 +58,16 @@ constexpr int NDIG = 9;
 constexpr int NDIAG = 9;
 constexpr int A_SLICE = TC_M * TC_K * 2;  // 16384 B
 constexpr int B_SLICE = TC_N * TC_K * 2;  // 6144 B
-constexpr int A_BYTES = NDIG * A_SLICE;   // 147456 B
-constexpr int B_BYTES = NDIG * B_SLICE;   // 55296 B
+constexpr int A_BYTES = NDIG * A_SLICE;   // 147456 B (a group's coefficient digits in global memory)
+constexpr int B_BYTES = NDIG * B_SLICE;   // 55296 B (one buffer of a tile's basis digits)
+// Coefficient digit slices 0 and 1 live in TMEM (columns after the nine
+// accumulators), the other seven in shared memory: that leaves room for two
+// basis-digit buffers, so the builders write tile t+1's digits while the
+// tensor core works through tile t.
+constexpr int A_TMEM_SLICES = 2;
+constexpr int A_SMEM_BYTES = (NDIG - A_TMEM_SLICES) * A_SLICE;  // 114688 B
+constexpr int A_TCOL = NDIAG * TC_N;                             // first TMEM column of slice 0 (32 per slice)
+constexpr int NBUF = 2;                                          // basis-digit buffers
 constexpr int BUILD_WARPS = 3;            // warps 0-2: basis digits
 constexpr int MMA_WARP = 3;               // warp 3: coefficient copy + MMA issue (one thread)
 constexpr int EPI_WARP0 = MMA_WARP + 1;   // first epilogue warp (a multiple of 4: warp w reads TMEM quadrant w % 4)
@@ -69,7 +79,7 @@ constexpr int ITEMS = (TC_K / 8) * TC_N;          // (slot octet, element) pairs
 constexpr int ITEMS_PER = ITEMS / BUILD_THREADS;  // 4
 constexpr int TMEM_COLS = 512;
 constexpr int SMEM_MISC = 6144;
-constexpr int SMEM_BYTES = A_BYTES + B_BYTES + SMEM_MISC;
+constexpr int SMEM_BYTES = A_SMEM_BYTES + NBUF * B_BYTES + SMEM_MISC;  // 231424 B
 constexpr long long WAIT_LIMIT = 1ll << 26;  // polls of an mbarrier before giving up
 constexpr int EXP_NONE = -100000;            // exponent of an all-zero row or column
 // sum_s 64 * 2^(56 - 7 s): adding it to a 62-bit signed value makes every
@@ -86,7 +96,9 @@ static_assert(ITEMS % BUILD_THREADS == 0, "builder items");
 static_assert(EPI_WARP0 % 4 == 0 && EPI_WARP0 + EPI_WARPS == TC_THREADS / 32, "epilogue warps: whole quadrant sets");
 static_assert((TC_THREADS / 32 - 1 - EPI_WARP0) / 4 == EPI_WARPS / 4 - 1, "epilogue column groups");
 static_assert(EPI_COLS % 4 == 0 && TC_N % 8 == 0, "epilogue columns");
-static_assert(NDIAG * TC_N <= TMEM_COLS, "accumulators fit TMEM");
+static_assert(A_TCOL + 32 * A_TMEM_SLICES <= TMEM_COLS, "accumulators and the TMEM coefficient slices fit TMEM");
+static_assert(SMEM_BYTES <= 232448, "shared memory of one CTA");
+static_assert(A_SMEM_BYTES % 1024 == 0 && B_BYTES % 1024 == 0, "1024-byte aligned operand buffers");
 
 // byte offset of element (row, k) in a K-major, no-swizzle UMMA operand:
 // core matrices of 8 rows x 16 bytes; K-adjacent core matrices 128 B apart
@@ -353,22 +365,26 @@ __global__ void __launch_bounds__(TC_K) k_flush_prep(const double *__restrict__ 
 // ---- the tensor-core flush
 __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *sA = smem;
-    unsigned char *sB = smem + A_BYTES;
-    unsigned char *misc = smem + A_BYTES + B_BYTES;
+    unsigned char *sA = smem;                 // coefficient digit slices 2 .. 8
+    unsigned char *sB = smem + A_SMEM_BYTES;  // NBUF basis-digit buffers, tile it in buffer it % 2
+    unsigned char *misc = smem + A_SMEM_BYTES + NBUF * B_BYTES;
+    // Tiles alternate between the two basis-digit buffers, and the barriers
+    // that hand a buffer between the builders and the tensor core come in
+    // pairs (one per buffer): a parity wait is only sound while the waiter is
+    // at most one phase behind, and the builders now run two tiles ahead.
     uint64_t *bar_a = reinterpret_cast<uint64_t *>(misc);           // coefficient digits landed
-    uint64_t *bar_full = reinterpret_cast<uint64_t *>(misc + 8);     // basis digits of a tile written
-    uint64_t *bar_mma = reinterpret_cast<uint64_t *>(misc + 16);     // MMAs of a tile done
-    uint64_t *bar_ready = reinterpret_cast<uint64_t *>(misc + 24);   // MMAs issued (orders s_F for the epilogue)
-    uint64_t *bar_tfree = reinterpret_cast<uint64_t *>(misc + 32);   // accumulators read out
-    uint64_t *bar_cexp = reinterpret_cast<uint64_t *>(misc + 40);    // builders' partial exponents written
-    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(misc + 48);
-    int *s_fail = reinterpret_cast<int *>(misc + 52);
-    int *s_slotexp = reinterpret_cast<int *>(misc + 64);             // [64]
-    int *s_cexp = reinterpret_cast<int *>(misc + 320);               // [2][8][48] per slot octet
-    int *s_F = reinterpret_cast<int *>(misc + 3392);                 // [4][48] element exponents, ring
-    int *s_rowexp = reinterpret_cast<int *>(misc + 4160);            // [128]
-    double *s_rown = reinterpret_cast<double *>(misc + 4672);        // [128]
+    uint64_t *bar_full = reinterpret_cast<uint64_t *>(misc + 8);     // [2] basis digits of a tile written
+    uint64_t *bar_mma = reinterpret_cast<uint64_t *>(misc + 24);     // [2] MMAs of a tile done
+    uint64_t *bar_ready = reinterpret_cast<uint64_t *>(misc + 40);   // MMAs issued (orders s_F for the epilogue)
+    uint64_t *bar_tfree = reinterpret_cast<uint64_t *>(misc + 48);   // accumulators read out
+    uint64_t *bar_cexp = reinterpret_cast<uint64_t *>(misc + 56);    // builders' partial exponents written
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(misc + 64);
+    int *s_fail = reinterpret_cast<int *>(misc + 68);
+    int *s_slotexp = reinterpret_cast<int *>(misc + 128);            // [64]
+    int *s_cexp = reinterpret_cast<int *>(misc + 384);               // [2][8][48] per slot octet
+    int *s_F = reinterpret_cast<int *>(misc + 3456);                 // [4][48] element exponents, ring
+    int *s_rowexp = reinterpret_cast<int *>(misc + 4224);            // [128]
+    double *s_rown = reinterpret_cast<double *>(misc + 4736);        // [128], ends at 5760
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int g = blockIdx.y;
@@ -382,7 +398,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
     if (tid == 0) {
         mbar_init(bar_a, 1);
         mbar_init(bar_full, BUILD_THREADS);
+        mbar_init(bar_full + 1, BUILD_THREADS);
         mbar_init(bar_mma, 1);
+        mbar_init(bar_mma + 1, 1);
         mbar_init(bar_ready, 1);
         mbar_init(bar_tfree, (EPI_WARPS / 4) * live_quads);
         mbar_init(bar_cexp, BUILD_THREADS);
@@ -406,6 +424,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *s_tmem;
+    // coefficient digit slices 0 and 1 into TMEM: lane r holds row r, each
+    // 32-bit column two consecutive k (the lower k in the low half), slice s
+    // at columns A_TCOL + 32 s ..  Warps 4-7 each write their own quadrant.
+    if (warp >= EPI_WARP0 && warp < EPI_WARP0 + 4) {
+        const int r = 32 * (warp & 3) + lane;
+        const unsigned char *src = a.aimg + (size_t)g * A_BYTES;
+#pragma unroll
+        for (int s = 0; s < A_TMEM_SLICES; ++s) {
+            uint32_t col[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                const uint32_t lo = *reinterpret_cast<const unsigned short *>(src + s * A_SLICE + umma_off(r, 2 * c));
+                const uint32_t hi = *reinterpret_cast<const unsigned short *>(src + s * A_SLICE + umma_off(r, 2 * c + 1));
+                col[c] = lo | (hi << 16);
+            }
+            const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(A_TCOL + 32 * s);
+            asm volatile(
+                "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+                "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+                "r"(col[0]), "r"(col[1]), "r"(col[2]), "r"(col[3]), "r"(col[4]), "r"(col[5]), "r"(col[6]),
+                "r"(col[7]), "r"(col[8]), "r"(col[9]), "r"(col[10]), "r"(col[11]), "r"(col[12]), "r"(col[13]),
+                "r"(col[14]), "r"(col[15]), "r"(col[16]), "r"(col[17]), "r"(col[18]), "r"(col[19]), "r"(col[20]),
+                "r"(col[21]), "r"(col[22]), "r"(col[23]), "r"(col[24]), "r"(col[25]), "r"(col[26]), "r"(col[27]),
+                "r"(col[28]), "r"(col[29]), "r"(col[30]), "r"(col[31])
+                : "memory");
+        }
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
 
     const unsigned n = a.n;
     const unsigned ntiles = (n + TC_N - 1) / TC_N;
@@ -470,11 +519,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                 for (int o = 0; o < TC_K / 8; ++o) F = max(F, cexp[o * TC_N + ii[u]]);
                 Fv[u] = F;
             }
-            // phase B: the digit buffer is free once the previous tile's MMAs are done
-            if (it > 0 && !mbar_wait(bar_mma, (it - 1) & 1, s_fail)) {
+            // phase B: this tile's digit buffer is free once the MMAs of the
+            // tile before the previous one (the same buffer) are done
+            if (it >= NBUF && !mbar_wait(bar_mma + (it & 1), ((it >> 1) - 1) & 1, s_fail)) {
                 atomicExch(s_fail, 1);
                 break;
             }
+            unsigned char *sBt = sB + (it & 1) * B_BYTES;
 #pragma unroll
             for (int u = 0; u < ITEMS_PER; ++u) {
                 uint64_t U[8];
@@ -482,11 +533,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                 for (int w = 0; w < 8; ++w)
                     U[w] = biased62((uint64_t)__double_as_longlong(v[u][w]), Fv[u] + s_slotexp[8 * io[u] + w]);
                 if (io[u] == 0) s_F[(it & 3) * TC_N + ii[u]] = Fv[u];
-                store_digits<0>(sB, umma_off(ii[u], 8 * io[u]), U);
+                store_digits<0>(sBt, umma_off(ii[u], 8 * io[u]), U);
             }
             // digits written by threads must be visible to the tensor core (async proxy)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive(bar_full);
+            mbar_arrive(bar_full + (it & 1));
             // the next tile's basis values are in flight during this tile's MMAs
             if (t + gridDim.x < ntiles) load_tile(t + gridDim.x);
         }
@@ -494,22 +545,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
         // ---- one thread loads the coefficient digits and issues every MMA
         if (lane == 0) {
             // the coefficient digits of this group: one bulk copy per slice
+            // the coefficient digit slices kept in shared memory (2 .. 8)
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar_a)),
-                         "r"((uint32_t)A_BYTES)
+                         "r"((uint32_t)A_SMEM_BYTES)
                          : "memory");
             const unsigned char *src = a.aimg + (size_t)g * A_BYTES;
-            for (int s = 0; s < NDIG; ++s)
+            for (int s = A_TMEM_SLICES; s < NDIG; ++s)
                 asm volatile(
                     "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                        smem_u32(sA + s * A_SLICE)),
+                        smem_u32(sA + (s - A_TMEM_SLICES) * A_SLICE)),
                     "l"(src + (size_t)s * A_SLICE), "r"((uint32_t)A_SLICE), "r"(smem_u32(bar_a))
                     : "memory");
             a_ok = mbar_wait(bar_a, 0, s_fail);
             if (!a_ok) atomicExch(s_fail, 1);
-            const uint64_t ad0 = umma_desc(smem_u32(sA)), bd0 = umma_desc(smem_u32(sB));
+            const uint64_t ad0 = umma_desc(smem_u32(sA));
             int it = 0;
             for (unsigned t = blockIdx.x; t < ntiles && a_ok; t += gridDim.x, ++it) {
-                bool ok = mbar_wait(bar_full, it & 1, s_fail);
+                const uint64_t bd0 = umma_desc(smem_u32(sB + (it & 1) * B_BYTES));
+                bool ok = mbar_wait(bar_full + (it & 1), (it >> 1) & 1, s_fail);
                 // the previous tile's accumulators must have been read out
                 if (ok && it > 0) ok = mbar_wait(bar_tfree, (it - 1) & 1, s_fail);
                 if (!ok) {
@@ -535,20 +588,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
                             const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nn >> 3) << 17) |
                                                    ((uint32_t)(TC_M >> 4) << 24);
                             // start-address field: (offset >> 4) adds without carry (smem < 256 KB)
-                            const uint64_t ad = ad0 + (uint64_t)((s * A_SLICE + kk * 256) >> 4);
                             const uint64_t bd = bd0 + (uint64_t)((part * 256 / 8 * 1024 + kk * 256) >> 4);
                             const uint32_t acc = (kk | s) ? 1u : 0u;
-                            asm volatile(
-                                "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-                                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-                                    tmem + (uint32_t)(TC_N * s + 256 * part)),
-                                "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-                                : "memory");
+                            const uint32_t dt = tmem + (uint32_t)(TC_N * s + 256 * part);
+                            if (s < A_TMEM_SLICES) {  // A from TMEM: K = 16 is 8 columns
+                                const uint32_t at = tmem + (uint32_t)(A_TCOL + 32 * s + 8 * kk);
+                                asm volatile(
+                                    "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                                    " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(dt),
+                                    "r"(at), "l"(bd), "r"(idesc), "r"(acc)
+                                    : "memory");
+                            } else {
+                                const uint64_t ad =
+                                    ad0 + (uint64_t)(((s - A_TMEM_SLICES) * A_SLICE + kk * 256) >> 4);
+                                asm volatile(
+                                    "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
+                                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                                    : "memory");
+                            }
                         }
                     }
                 }
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                 smem_u32(bar_mma))
+                                 smem_u32(bar_mma + (it & 1)))
                              : "memory");
                 ++issued;
                 mbar_arrive(bar_ready);
@@ -597,7 +660,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
         for (unsigned t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
             // the warp decides as one: tcgen05.ld and the shuffles below are warp-collective
             bool bad = *(volatile int *)s_fail != 0;
-            if (!bad) bad = !mbar_wait(bar_ready, it & 1, s_fail) || !mbar_wait(bar_mma, it & 1, s_fail);
+            if (!bad)
+                bad = !mbar_wait(bar_ready, it & 1, s_fail) || !mbar_wait(bar_mma + (it & 1), (it >> 1) & 1, s_fail);
             if (__any_sync(0xffffffffu, bad)) {
                 if (lane == 0) atomicExch(s_fail, 1);
                 break;
@@ -662,7 +726,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_flush_tc(TcArgs a) {
     if (tid == 32 * MMA_WARP && *(volatile int *)s_fail) {
         int dummy = 0;
         if (!a_ok) mbar_wait(bar_a, 0, &dummy);
-        if (issued > 0) mbar_wait(bar_mma, (issued - 1) & 1, &dummy);
+        if (issued > 0) mbar_wait(bar_mma + ((issued - 1) & 1), ((issued - 1) >> 1) & 1, &dummy);
     }
     tc_fence_before();
     __syncthreads();
