@@ -92,7 +92,10 @@ def _reference(V, Xc, Pc, own, X, Pm, n, L):
     return x, p, sx, sp
 
 
-@pytest.mark.parametrize("m,L,n,keep_p", [(64, 51, 5003, 1), (5, 17, 1000, 1), (70, 64, 777, 1), (64, 51, 4801, 0)])
+# (20, 40, 29213): 609 tiles, so every CTA runs 4 or 5 tiles and both basis-digit
+# buffers are reused; two TMEM quadrants live; a partial last panel
+@pytest.mark.parametrize("m,L,n,keep_p", [(64, 51, 5003, 1), (5, 17, 1000, 1), (70, 64, 777, 1), (64, 51, 4801, 0),
+                                          (20, 40, 29213, 1)])
 def test_tc_flush_matches_extended_precision(cuda, pkg, m, L, n, keep_p):
     torch = cuda
     V, Xc, Pc, own, X, Pm, ld = _case(m, L, n, seed=m * 7 + L, zero_cols=(m == 5))
