@@ -239,6 +239,19 @@ static int build_hyb(hbicg_matrix *A, const unsigned *h_ptr, unsigned n) {
     A->hit4 = (unsigned)it4;
     A->hitl = (unsigned)itl;
 done:
+    if (rc != HBICG_OK) { /* no half-built form: a later request builds it again */
+        cudaStreamSynchronize(st);
+        cudaFree(A->d_hsptr);
+        cudaFree(A->d_hval);
+        cudaFree(A->d_hcol);
+        cudaFree(A->d_srow);
+        cudaFree(A->d_wrow);
+        A->d_hsptr = NULL;
+        A->d_hval = NULL;
+        A->d_hcol = NULL;
+        A->d_srow = NULL;
+        A->d_wrow = NULL;
+    }
     free(srow);
     free(wkey);
     free(wrng);
