@@ -1092,7 +1092,10 @@ int hbk_fused_iteration(const hbk_matrix *A, const hbk_vectors *v, const hbk_shi
     }
     k_seed_update<<<wave_grid<k_seed_update>(gv), NT, 0, st>>>(c);
     if (!v->deferred) {
-        k_shift_update<64><<<wave_grid<k_shift_update<64>>(gv), NT, 0, st>>>(c);
+        // one element per thread: the update is FP64-bound (6 operations per
+        // element and running shift), so on small systems it wants every SM's
+        // FP64 pipe, not the two elements per thread of the streaming kernels
+        k_shift_update<64><<<wave_grid<k_shift_update<64>>(grid_for(v->n, 1)), NT, 0, st>>>(c);
     } else {
         k_seed_p_deferred<<<wave_grid<k_seed_p_deferred>(gv), NT, 0, st>>>(c);
         k_coef_update<<<grid_for((unsigned)((size_t)sh->m * v->slot_cap), 1), NT, 0, st>>>(c);
